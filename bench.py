@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Benchmark of the explicit higher-order encoding operator on GB300.
+
+Metric: E+E^H voxel·samples/s on the 200x200, 12,000-sample, 16-coil,
+third-order + concomitant spiral workload (seeded synthetic inputs with the
+shapes and distributions of that configuration).  One step = one forward
+E x and one adjoint E^H y; it processes 2*nVox*nSam voxel·samples.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Multi-GPU: the operator runs on one GPU; under torchrun each rank runs an
+independent replica (no collective on the data path), the time is the max
+over ranks and ``value`` counts all ranks' work.
+
+The ``--impl reference`` arm times the reference path's CPU restatement (the
+FP64 oracle, OpenMP on all host cores) on a bounded sample of the same
+workload; the reference itself is Julia and cannot run here.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "highordermri.jl_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "E+E^H voxel·samples/s, TC vs plain FP32 on GB300 at <=1e-4 rel err vs FP64"
+UNIT = "voxel·samples/s"
+L2_FLUSH_BYTES = 256 << 20
+
+# DRAM traffic per launch of the dominant kernels from one ncu capture,
+# scaled to the full workload (see profiles/); None until captured.
+NCU_TRAFFIC_BYTES = {}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--engine", default="auto", choices=["auto", "tc", "fp32"])
+    ap.add_argument("--config", default="2", choices=["1", "2", "3"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip timing the second engine")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    return a
+
+
+def workload(cfg: str):
+    from hoexplicit import workloads
+    return {"1": workloads.config1, "2": workloads.config2, "3": workloads.config3}[cfg]()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        for row in csv.reader(io.StringIO(out)):
+            if len(row) >= 9:
+                self.rows.append([c.strip() for c in row])
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("bf16_tflops", 1900.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+def cpu_baseline(w, seconds: float, x_gpu=None, y_gpu=None, op=None):
+    """Time the oracle (FP64, all host threads) on a bounded sample of rows.
+
+    Also returns the relative error of the GPU forward/adjoint on the same
+    sample (the adjoint compared for data supported on the sampled rows)."""
+    import torch
+    from hoexplicit import workloads
+    from oracle import dense, oracle
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    nthreads = oracle.max_threads()
+    nSam = k.shape[1]
+    rng = np.random.default_rng(0)
+
+    def model_rows(rows):
+        return oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=w.kspha.shape[0])
+
+    xm = w.x[idx]
+    probe = max(8, min(nSam, 32))
+    rows = np.sort(rng.choice(nSam, probe, replace=False))
+    m = model_rows(rows)
+    t0 = time.perf_counter()
+    yo = oracle.forward(m, xm)
+    oracle.adjoint(m, yo)
+    dt = time.perf_counter() - t0
+    per_row = dt / probe
+    n_rows = int(min(nSam, max(probe, seconds / max(per_row, 1e-9))))
+    rows = np.sort(rng.choice(nSam, n_rows, replace=False))
+    m = model_rows(rows)
+    t0 = time.perf_counter()
+    yo = oracle.forward(m, xm)
+    xo = oracle.adjoint(m, yo)
+    dt = time.perf_counter() - t0
+    units = 2.0 * len(idx) * n_rows
+    res = {"value": units / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+           "sample": f"E and E^H over {n_rows} of {nSam} samples x {len(idx)} voxels x {w.nCha} coils "
+                     f"(FP64 C restatement of array_operator.jl:241-348, OpenMP), {dt:.1f} s"}
+    if op is not None and x_gpu is not None:
+        yg = (op * x_gpu).cpu().numpy().reshape(w.nCha, nSam)[:, rows].reshape(-1)
+        res["gpu_forward_rel_err_vs_fp64"] = dense.rel(yg, yo)
+        ysub = np.zeros((w.nCha, nSam), dtype=np.complex128)
+        ysub[:, rows] = yo.reshape(w.nCha, n_rows)
+        xg = (op.H * torch.from_numpy(ysub.reshape(-1).astype(np.complex64)).cuda()).cpu().numpy()
+        res["gpu_adjoint_rel_err_vs_fp64"] = dense.rel(xg[idx], xo)
+    return res
+
+
+def time_engine(op, x, y, steps, warmup, flush, stream):
+    """CUDA-event timing of K steps (forward + adjoint), L2 flushed between steps."""
+    import torch
+    yout = torch.empty(op.nrow, dtype=torch.complex64, device=x.device)
+    xout = torch.empty(op.ncol, dtype=torch.complex64, device=x.device)
+    for _ in range(warmup):
+        op.prod_(yout, x)
+        op.ctprod_(xout, y)
+    torch.cuda.synchronize()
+    l0 = op.timings()["launches"]
+    step_ms, fk, ak = [], [], []
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        op.prod_(yout, x)
+        op.ctprod_(xout, y)
+        ev1.record(stream)
+        ev1.synchronize()
+        step_ms.append(ev0.elapsed_time(ev1))
+        tm = op.timings()
+        fk.append(tm["forward_kernel_ms"])
+        ak.append(tm["adjoint_kernel_ms"])
+    launches = op.timings()["launches"] - l0
+    return dict(step_ms=step_ms, fwd_kernel_ms=fk, adj_kernel_ms=ak, launches=launches)
+
+
+def run_gb300(a):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    from hoexplicit import HighOrderExplicitOp, HoeError
+
+    w = workload(a.config)
+    engines_avail = []
+    op = None
+    want = ["tc", "fp32"] if a.engine == "auto" else [a.engine]
+    for e in want:
+        try:
+            op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine=e, **w.op_kwargs())
+            engines_avail.append(e)
+            break
+        except HoeError:
+            continue
+    if op is None:
+        raise SystemExit("no engine available")
+    engine = engines_avail[0]
+    op.set_timing(True)
+    info = op.info()
+    stream = torch.cuda.current_stream()
+    x = torch.from_numpy(w.x.astype(np.complex64)).to(dev)
+    y = op * x
+    g = torch.Generator(device=dev).manual_seed(0)
+    noise = torch.randn(y.shape, dtype=torch.complex64, device=dev, generator=g)
+    y = y + 0.01 * y.abs().pow(2).mean().sqrt() * noise
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    units = 2.0 * w.nVox * w.nSam
+
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        r = time_engine(op, x, y, a.steps, a.warmup, flush, stream)
+    torch.cuda.synchronize()
+    total_ms = sum(r["step_ms"])
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        torch.distributed.barrier()
+    ms_per_step = total_ms / a.steps
+    value = ws * units / (ms_per_step / 1e3)
+
+    # dominant kernel roofline (contraction flops: 8*nCha per voxel·sample per direction)
+    fk = statistics.mean(r["fwd_kernel_ms"])
+    ak = statistics.mean(r["adj_kernel_ms"])
+    dom, dom_ms = ("forward", fk) if fk >= ak else ("adjoint", ak)
+    flops_per_launch = 8.0 * w.nCha * w.nVox * w.nSam
+    achieved = flops_per_launch / (dom_ms / 1e3) / 1e12
+    bf16_peak, hbm_peak, peak_src = measured_peaks()
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved / bf16_peak, "traffic": NCU_TRAFFIC_BYTES.get((engine, dom)),
+                "kernel": f"{engine} {dom} contraction", "peak_source": f"bf16_tflops ({peak_src}, burst)",
+                "kernel_ms": dom_ms, "flops_per_launch": flops_per_launch,
+                "frac_of_split_peak": achieved / (bf16_peak / 3.0) if engine == "tc" else None,
+                "share_of_step": (fk + ak) / ms_per_step}
+    if engine == "fp32":
+        sm_mhz = clk.summary().get("sm_mhz") or 1900.0
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roofline["note"] = ("plain FP32 engine: contraction on CUDA cores; fp32 FMA issue peak "
+                            f"{fp32_peak:.1f} TFLOP/s at the sampled clock, frac {achieved / fp32_peak:.3f}")
+        roofline["fp32_simt_frac"] = achieved / fp32_peak
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16x3/f32-acc" if engine == "tc" else "f32",
+           "data": "synthetic (seeded, shapes/distributions of the named configuration)",
+           "config": {"workload": w.name, "nVox": w.nVox, "nSam": w.nSam, "nCha": w.nCha,
+                      "nTermEff": info["nTermEff"], "engine": engine, "parallelism": f"replicas x{ws}",
+                      "l2": "flushed between timed steps (256 MiB write)",
+                      "residual_phase_bound_cycles": info["residual_phase_bound"]},
+           "roofline": roofline, "clocks": clk.summary(),
+           "gpu_launches": int(r["launches"]),
+           "kernel_ms": {"forward": fk, "adjoint": ak}}
+
+    # second engine for the TC vs plain-FP32 ratio
+    if not a.no_compare and engine == "tc":
+        try:
+            op.set_engine("fp32")
+            r2 = time_engine(op, x, y, max(3, a.steps // 4), 3, flush, stream)
+            ms2 = statistics.mean(r2["step_ms"])
+            out["fp32_engine"] = {"value": units / (ms2 / 1e3), "ms_per_step": ms2,
+                                  "kernel_ms": {"forward": statistics.mean(r2["fwd_kernel_ms"]),
+                                                "adjoint": statistics.mean(r2["adj_kernel_ms"])}}
+            out["tc_vs_fp32"] = ms2 / ms_per_step
+            op.set_engine("tc")
+        except Exception as exc:  # report, do not substitute
+            out["fp32_engine"] = {"error": str(exc)}
+
+    # end-to-end through the public API with host (pinned) buffers
+    if not a.no_e2e:
+        xh = torch.from_numpy(w.x.astype(np.complex64)).pin_memory()
+        yh = y.cpu().pin_memory()
+        for _ in range(2):
+            op * xh
+            op.H * yh
+        torch.cuda.synchronize()
+        n_e2e = max(3, a.steps // 2)
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            yo = op * xh
+            xo = op.H * yh
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        out["e2e"] = {"value": ws * units / e2e_s, "unit": UNIT,
+                      "h2d_bytes_per_step": int(xh.numel() * 8 + yh.numel() * 8),
+                      "d2h_bytes_per_step": int(yo.numel() * 8 + xo.numel() * 8),
+                      "ms_per_step": e2e_s * 1e3}
+
+    if rank == 0 and ws == 1 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(w, a.cpu_seconds, x, y, op)
+        acc = {k: out["cpu_baseline"].pop(k) for k in list(out["cpu_baseline"]) if k.startswith("gpu_")}
+        out["accuracy_vs_fp64"] = acc
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    op.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(a):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from hoexplicit import workloads
+    from oracle import oracle
+    w = workload(a.config)
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    nSam = k.shape[1]
+    xm = w.x[idx]
+    rng = np.random.default_rng(0)
+    # size one step to ~ (budget / (steps + warmup)) seconds, at most ~6 s
+    budget = 150.0
+    per_step = min(6.0, budget / (a.steps + a.warmup))
+    probe = 16
+    rows = np.sort(rng.choice(nSam, probe, replace=False))
+    m = oracle.Model(bf, k[:, rows], t[rows], f, c)
+    t0 = time.perf_counter()
+    yo = oracle.forward(m, xm)
+    oracle.adjoint(m, yo)
+    per_row = (time.perf_counter() - t0) / probe
+    n_rows = int(min(nSam, max(probe, per_step / max(per_row, 1e-9))))
+    rows = np.sort(rng.choice(nSam, n_rows, replace=False))
+    m = oracle.Model(bf, k[:, rows], t[rows], f, c)
+    ysub = None
+    for _ in range(a.warmup):
+        ysub = oracle.forward(m, xm)
+        oracle.adjoint(m, ysub)
+    times = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        ysub = oracle.forward(m, xm)
+        oracle.adjoint(m, ysub)
+        times.append(time.perf_counter() - t0)
+    units = 2.0 * len(idx) * n_rows
+    s = statistics.mean(times)
+    value = units / s
+    sample = (f"each step: E and E^H over {n_rows} of {nSam} samples x {len(idx)} voxels x {w.nCha} coils "
+              "(FP64 C restatement of array_operator.jl:241-348; the Julia reference cannot run here)")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded, shapes/distributions of the named configuration)",
+           "config": {"workload": w.name, "nVox": w.nVox, "nSam": w.nSam, "nCha": w.nCha},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse_args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,595 @@
+// C ABI of libhoexplicit.so: handle lifetime, model preparation on the
+// device, and dispatch of forward / adjoint / normal / derivative / backward.
+//
+// Mirrors the resident single-GPU operator of the reference
+// (src/EncodingOperator/Explicit/explicit_gpu_operator.jl): the handle owns
+// the model arrays and scratch space (ExplicitGPUState, :3-29), applications
+// take caller-owned device vectors, `close` is idempotent and later use is an
+// error (:40-44, :435-446).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "hoe_internal.cuh"
+
+#define HOE_VERSION_STRING "hoexplicit 0.1.0 (sm_103a)"
+
+namespace {
+
+thread_local std::string g_err;  // failures without a usable handle
+
+int fail(hoe_handle *h, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(hoe_handle *h, cudaError_t e, const char *what) {
+  int code = (e == cudaErrorMemoryAllocation) ? HOE_ERR_OOM : HOE_ERR_CUDA;
+  return fail(h, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Host-side allocation-failure injection for tests of the cleanup path:
+// HOE_INJECT_ALLOC_FAIL=n makes the n-th device allocation of hoe_create fail.
+struct Allocator {
+  hoe_handle *h;
+  int count = 0;
+  int failAt = -1;
+  explicit Allocator(hoe_handle *hh) : h(hh) {
+    const char *e = getenv("HOE_INJECT_ALLOC_FAIL");
+    if (e && *e) failAt = atoi(e);
+  }
+  template <class T>
+  cudaError_t alloc(T **p, size_t elems) {
+    ++count;
+    if (failAt > 0 && count == failAt) return cudaErrorMemoryAllocation;
+    size_t bytes = std::max<size_t>(elems, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e == cudaSuccess) h->bytes += (int64_t)bytes;
+    return e;
+  }
+};
+
+template <class T>
+void dfree(T *&p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+void release_events(hoe_handle *h) {
+  for (auto &e : h->ev) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  h->timing = 0;
+}
+
+void release_device(hoe_handle *h) {
+  release_events(h);
+  hoe::tc_release(h);
+  auto &t = h->t;
+  dfree(t.dbeta); dfree(t.kappa); dfree(t.Atab); dfree(t.Btab); dfree(t.csm);
+  dfree(t.perm);  dfree(t.bfraw); dfree(t.kdot); dfree(t.times);
+  auto &s = h->s;
+  dfree(s.Z); dfree(s.Yt); dfree(s.part); dfree(s.gpart); dfree(s.dred);
+  h->bytes = 0;
+}
+
+inline uint64_t spread2(uint64_t v) {  // 32 bits -> even bit positions
+  v &= 0xffffffffull;
+  v = (v | (v << 16)) & 0x0000ffff0000ffffull;
+  v = (v | (v << 8)) & 0x00ff00ff00ff00ffull;
+  v = (v | (v << 4)) & 0x0f0f0f0f0f0f0f0full;
+  v = (v | (v << 2)) & 0x3333333333333333ull;
+  v = (v | (v << 1)) & 0x5555555555555555ull;
+  return v;
+}
+inline uint64_t spread3(uint64_t v) {  // 21 bits -> every third bit
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x1f00000000ffffull;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
+
+// FP64 table kernels: the range-reduced anchor phases.
+__global__ void k_table_A(const double *__restrict__ betabar,  // [nVt][R]
+                          const double *__restrict__ kap64,    // [nSamPad][R]
+                          float *__restrict__ A, int R, int nVt, int nSamPad, int nSam) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nVt * nSamPad) return;
+  int vt = (int)(i / nSamPad), s = (int)(i % nSamPad);
+  double a = 0.0;
+  if (s < nSam)
+    for (int l = 0; l < R; ++l) a = fma(betabar[(int64_t)vt * R + l], kap64[(int64_t)s * R + l], a);
+  A[i] = (float)(a - rint(a));
+}
+
+__global__ void k_table_B(const double *__restrict__ beta64,    // [nVoxPad][R]
+                          const double *__restrict__ gammabar,  // [nSt][R]
+                          const int *__restrict__ perm, float *__restrict__ B, int R, int nSt,
+                          int nVoxPad) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nSt * nVoxPad) return;
+  int st = (int)(i / nVoxPad), p = (int)(i % nVoxPad);
+  double b = 0.0;
+  if (perm[p] >= 0)
+    for (int l = 0; l < R; ++l) b = fma(beta64[(int64_t)p * R + l], gammabar[(int64_t)st * R + l], b);
+  B[i] = (float)(b - rint(b));
+}
+
+bool valid_handle(const hoe_handle *h) { return h && h->magic == HOE_MAGIC; }
+
+int check_usable(hoe_handle *h) {
+  if (!valid_handle(h)) return fail(nullptr, HOE_ERR_ARG, "invalid handle");
+  if (h->closed) return fail(h, HOE_ERR_CLOSED, "operator is closed");
+  return HOE_OK;
+}
+
+int finish(hoe_handle *h, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, what);
+  return HOE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hoe_version(void) { return HOE_VERSION_STRING; }
+int hoe_abi_version(void) { return HOE_ABI_VERSION; }
+
+const char *hoe_last_error(const hoe_handle *h) {
+  if (valid_handle(h) && !h->err.empty()) return h->err.c_str();
+  return g_err.c_str();
+}
+
+int hoe_is_closed(const hoe_handle *h) { return valid_handle(h) ? h->closed : 1; }
+
+int hoe_create(hoe_handle **out, const hoe_desc *d) {
+  if (!out) return fail(nullptr, HOE_ERR_ARG, "out must not be NULL");
+  *out = nullptr;
+  if (!d) return fail(nullptr, HOE_ERR_ARG, "descriptor must not be NULL");
+  if (d->abi_version != HOE_ABI_VERSION)
+    return fail(nullptr, HOE_ERR_ARG, "descriptor ABI version %d, library %d", d->abi_version,
+                HOE_ABI_VERSION);
+  if (d->nTerm != 9 && d->nTerm != 16)
+    return fail(nullptr, HOE_ERR_ARG, "kspha requires 9 or 16 terms, got %d", d->nTerm);
+  if (d->has_concomitant != 0 && d->has_concomitant != 1)
+    return fail(nullptr, HOE_ERR_ARG, "has_concomitant must be 0 or 1");
+  if (d->nX <= 0 || d->nY <= 0 || d->nZ <= 0)
+    return fail(nullptr, HOE_ERR_DIM, "grid sizes must be positive");
+  int64_t nFull = (int64_t)d->nX * d->nY * d->nZ;
+  if (nFull > (1ll << 30)) return fail(nullptr, HOE_ERR_DIM, "grid too large");
+  if (d->nVox <= 0) return fail(nullptr, HOE_ERR_ARG, "mask must contain voxels");
+  if (d->nVox > nFull) return fail(nullptr, HOE_ERR_DIM, "mask and grid");
+  if (d->nSam <= 0 || d->nCha <= 0)
+    return fail(nullptr, HOE_ERR_ARG, "samples and coils must be positive");
+  if ((int64_t)d->nSam * d->nCha > (1ll << 31) - 1)
+    return fail(nullptr, HOE_ERR_DIM, "nSam*nCha too large");
+  if (d->engine != HOE_ENGINE_FP32_SIMT && d->engine != HOE_ENGINE_TC_BF16X3)
+    return fail(nullptr, HOE_ERR_ARG, "unknown engine %d", d->engine);
+  if (!d->mask_idx || !d->bf || !d->kspha || !d->times)
+    return fail(nullptr, HOE_ERR_ARG, "mask_idx, bf, kspha and times are required");
+  if (!d->csm && d->nCha != 1)
+    return fail(nullptr, HOE_ERR_ARG, "csm may be omitted only for one coil");
+  for (int m = 0; m < d->nVox; ++m) {
+    if (d->mask_idx[m] < 0 || d->mask_idx[m] >= nFull)
+      return fail(nullptr, HOE_ERR_DIM, "mask index %d out of range", m);
+    if (m > 0 && d->mask_idx[m] <= d->mask_idx[m - 1])
+      return fail(nullptr, HOE_ERR_ARG, "mask indices must be strictly ascending");
+  }
+  if (d->tile_samples != 0 && d->tile_samples != hoe::kTileS)
+    return fail(nullptr, HOE_ERR_ARG, "tile_samples must be 0 or %d", hoe::kTileS);
+  if (d->tile_voxels != 0 && d->tile_voxels != hoe::kTileV)
+    return fail(nullptr, HOE_ERR_ARG, "tile_voxels must be 0 or %d", hoe::kTileV);
+
+  int ndev = 0;
+  cudaError_t ce = cudaGetDeviceCount(&ndev);
+  if (ce != cudaSuccess || ndev == 0) return fail(nullptr, HOE_ERR_CUDA, "no CUDA device");
+  int dev = d->device;
+  if (dev < 0) cudaGetDevice(&dev);
+  if (dev < 0 || dev >= ndev) return fail(nullptr, HOE_ERR_ARG, "invalid visible GPU ID");
+
+  hoe_handle *h = new hoe_handle();
+  h->device = dev;
+  DeviceGuard guard(dev);
+  if (!guard.ok) {
+    delete h;
+    return fail(nullptr, HOE_ERR_CUDA, "cannot select device %d", dev);
+  }
+  cudaDeviceGetAttribute(&h->numSMs, cudaDevAttrMultiProcessorCount, dev);
+  if (h->numSMs <= 0) h->numSMs = 148;
+
+  auto &t = h->t;
+  t.nX = d->nX; t.nY = d->nY; t.nZ = d->nZ; t.nFull = (int)nFull;
+  t.nSam = d->nSam; t.nCha = d->nCha; t.nTerm = d->nTerm;
+  t.R0 = d->nTerm + 4 * d->has_concomitant;
+  t.R = t.R0 + 1;
+  t.Rp = (t.R + 3) / 4 * 4;
+  t.nVox = d->nVox;
+  t.nSt = (t.nSam + t.ST - 1) / t.ST;
+  t.nVt = (t.nVox + t.VT - 1) / t.VT;
+  t.nSamPad = t.nSt * t.ST;
+  t.nVoxPad = t.nVt * t.VT;
+  t.nChaPad = t.nCha <= 4 ? 4 : (t.nCha <= 8 ? 8 : (t.nCha + 15) / 16 * 16);
+  t.hasKdot = d->kspha_dt != nullptr;
+  const int R = t.R, R0 = t.R0, Rp = t.Rp;
+  const int nVox = t.nVox, nSam = t.nSam;
+
+  // ---- voxel order: Morton order of grid indices, chunks of VT voxels ----
+  std::vector<int> order(nVox);
+  {
+    std::vector<uint64_t> code(nVox);
+    for (int m = 0; m < nVox; ++m) {
+      int64_t lin = d->mask_idx[m];
+      uint64_t i = lin % t.nX, j = (lin / t.nX) % t.nY, k = lin / ((int64_t)t.nX * t.nY);
+      code[m] = (t.nZ == 1) ? (spread2(i) | (spread2(j) << 1))
+                            : (spread3(i) | (spread3(j) << 1) | (spread3(k) << 2));
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return code[a] < code[b]; });
+  }
+
+  // ---- beta / gamma in FP64, tile anchors (component midrange) ----
+  std::vector<double> beta64((size_t)t.nVoxPad * R, 0.0), gam64((size_t)t.nSamPad * R, 0.0);
+  std::vector<int> perm(t.nVoxPad, -1);
+  for (int p = 0; p < nVox; ++p) {
+    int m = order[p];
+    perm[p] = d->mask_idx[m];
+    for (int l = 0; l < R0; ++l) beta64[(size_t)p * R + l] = d->bf[(size_t)m + (size_t)l * nVox];
+    beta64[(size_t)p * R + R0] = d->fieldmap ? d->fieldmap[m] : 0.0;
+  }
+  for (int s = 0; s < nSam; ++s) {
+    for (int l = 0; l < R0; ++l) gam64[(size_t)s * R + l] = d->kspha[(size_t)l + (size_t)s * R0];
+    gam64[(size_t)s * R + R0] = d->times[s];
+  }
+  for (size_t i = 0; i < beta64.size(); ++i)
+    if (!std::isfinite(beta64[i])) { delete h; return fail(nullptr, HOE_ERR_ARG, "bf/fieldmap must be finite"); }
+  for (size_t i = 0; i < gam64.size(); ++i)
+    if (!std::isfinite(gam64[i])) { delete h; return fail(nullptr, HOE_ERR_ARG, "kspha/times must be finite"); }
+
+  std::vector<double> betabar((size_t)t.nVt * R, 0.0), gambar((size_t)t.nSt * R, 0.0);
+  std::vector<double> dbmax((size_t)t.nVt * R, 0.0), kpmax((size_t)t.nSt * R, 0.0);
+  for (int vt = 0; vt < t.nVt; ++vt) {
+    int p0 = vt * t.VT, p1 = std::min(nVox, p0 + t.VT);
+    for (int l = 0; l < R; ++l) {
+      double lo = INFINITY, hi = -INFINITY;
+      for (int p = p0; p < p1; ++p) { double v = beta64[(size_t)p * R + l]; lo = std::min(lo, v); hi = std::max(hi, v); }
+      betabar[(size_t)vt * R + l] = 0.5 * (lo + hi);
+      dbmax[(size_t)vt * R + l] = 0.5 * (hi - lo);
+    }
+  }
+  for (int st = 0; st < t.nSt; ++st) {
+    int s0 = st * t.ST, s1 = std::min(nSam, s0 + t.ST);
+    for (int l = 0; l < R; ++l) {
+      double lo = INFINITY, hi = -INFINITY;
+      for (int s = s0; s < s1; ++s) { double v = gam64[(size_t)s * R + l]; lo = std::min(lo, v); hi = std::max(hi, v); }
+      gambar[(size_t)st * R + l] = 0.5 * (lo + hi);
+      kpmax[(size_t)st * R + l] = 0.5 * (hi - lo);
+    }
+  }
+  double bound = 0.0;
+  for (int vt = 0; vt < t.nVt; ++vt)
+    for (int st = 0; st < t.nSt; ++st) {
+      double b = 0.0;
+      for (int l = 0; l < R; ++l) b += dbmax[(size_t)vt * R + l] * kpmax[(size_t)st * R + l];
+      bound = std::max(bound, b);
+    }
+  t.residBound = bound;
+
+  std::vector<float> dbeta((size_t)t.nVoxPad * Rp, 0.f), kappa((size_t)t.nSamPad * Rp, 0.f);
+  std::vector<float> bfraw((size_t)t.nVoxPad * Rp, 0.f), kdot((size_t)t.nSamPad * Rp, 0.f);
+  std::vector<float> times_f(t.nSamPad, 0.f);
+  std::vector<double> kap64((size_t)t.nSamPad * R, 0.0);
+  for (int p = 0; p < nVox; ++p) {
+    int vt = p / t.VT;
+    for (int l = 0; l < R; ++l) {
+      dbeta[(size_t)p * Rp + l] = (float)(beta64[(size_t)p * R + l] - betabar[(size_t)vt * R + l]);
+      bfraw[(size_t)p * Rp + l] = (float)beta64[(size_t)p * R + l];
+    }
+  }
+  for (int s = 0; s < nSam; ++s) {
+    int st = s / t.ST;
+    for (int l = 0; l < R; ++l) {
+      double kv = gam64[(size_t)s * R + l] - gambar[(size_t)st * R + l];
+      kap64[(size_t)s * R + l] = kv;
+      kappa[(size_t)s * Rp + l] = (float)kv;
+    }
+    if (d->kspha_dt)
+      for (int l = 0; l < t.nTerm; ++l) kdot[(size_t)s * Rp + l] = (float)d->kspha_dt[(size_t)l + (size_t)s * t.nTerm];
+    times_f[s] = (float)d->times[s];
+  }
+  std::vector<float2> csm((size_t)t.nVoxPad * t.nChaPad, make_float2(0.f, 0.f));
+  for (int p = 0; p < nVox; ++p) {
+    int m = order[p];
+    for (int c = 0; c < t.nCha; ++c) {
+      float2 v = make_float2(1.f, 0.f);
+      if (d->csm) {
+        size_t o = 2 * ((size_t)m + (size_t)c * nVox);
+        v = make_float2((float)d->csm[o], (float)d->csm[o + 1]);
+      }
+      csm[(size_t)p * t.nChaPad + c] = v;
+    }
+  }
+
+  // ---- split-K choice for the SIMT engine ----
+  {
+    int target = 4 * h->numSMs;
+    int nCC = (t.nChaPad + 15) / 16;
+    int sf = std::max(1, std::min(t.nVt, (target + t.nSt * nCC - 1) / (t.nSt * nCC)));
+    int tps = (t.nVt + sf - 1) / sf;
+    h->splitF = (t.nVt + tps - 1) / tps;
+    int sa = std::max(1, std::min(t.nSt, (target + t.nVt * nCC - 1) / (t.nVt * nCC)));
+    tps = (t.nSt + sa - 1) / sa;
+    h->splitA = (t.nSt + tps - 1) / tps;
+    if (d->split_hint > 0) {
+      h->splitF = std::min(d->split_hint, t.nVt);
+      h->splitA = std::min(d->split_hint, t.nSt);
+    }
+  }
+
+  // ---- device allocations ----
+  Allocator al(h);
+  double *d_beta64 = nullptr, *d_kap64 = nullptr, *d_betabar = nullptr, *d_gambar = nullptr;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  A(al.alloc(&t.dbeta, dbeta.size()));
+  A(al.alloc(&t.kappa, kappa.size()));
+  A(al.alloc(&t.Atab, (size_t)t.nVt * t.nSamPad));
+  A(al.alloc(&t.Btab, (size_t)t.nSt * t.nVoxPad));
+  A(al.alloc(&t.csm, csm.size()));
+  A(al.alloc(&t.perm, perm.size()));
+  A(al.alloc(&t.bfraw, bfraw.size()));
+  A(al.alloc(&t.kdot, kdot.size()));
+  A(al.alloc(&t.times, times_f.size()));
+  A(al.alloc(&h->s.Z, (size_t)t.nVoxPad * t.nChaPad));
+  A(al.alloc(&h->s.Yt, (size_t)t.nSamPad * t.nChaPad));
+  h->s.partElems = std::max((size_t)h->splitF * t.nSamPad, (size_t)h->splitA * t.nVoxPad) * t.nChaPad;
+  A(al.alloc(&h->s.part, h->s.partElems));
+  if (e != cudaSuccess) {
+    release_device(h);
+    delete h;
+    return cuda_fail(nullptr, e, "hoe_create: device allocation");
+  }
+  // staging for the FP64 tables (freed before returning)
+  A(cudaMalloc(&d_beta64, beta64.size() * sizeof(double)));
+  A(cudaMalloc(&d_kap64, kap64.size() * sizeof(double)));
+  A(cudaMalloc(&d_betabar, betabar.size() * sizeof(double)));
+  A(cudaMalloc(&d_gambar, gambar.size() * sizeof(double)));
+  auto H2D = [&](void *dst, const void *src, size_t bytes) { A(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice)); };
+  if (e == cudaSuccess) {
+    H2D(t.dbeta, dbeta.data(), dbeta.size() * sizeof(float));
+    H2D(t.kappa, kappa.data(), kappa.size() * sizeof(float));
+    H2D(t.csm, csm.data(), csm.size() * sizeof(float2));
+    H2D(t.perm, perm.data(), perm.size() * sizeof(int));
+    H2D(t.bfraw, bfraw.data(), bfraw.size() * sizeof(float));
+    H2D(t.kdot, kdot.data(), kdot.size() * sizeof(float));
+    H2D(t.times, times_f.data(), times_f.size() * sizeof(float));
+    H2D(d_beta64, beta64.data(), beta64.size() * sizeof(double));
+    H2D(d_kap64, kap64.data(), kap64.size() * sizeof(double));
+    H2D(d_betabar, betabar.data(), betabar.size() * sizeof(double));
+    H2D(d_gambar, gambar.data(), gambar.size() * sizeof(double));
+  }
+  if (e == cudaSuccess) {
+    int64_t nA = (int64_t)t.nVt * t.nSamPad, nB = (int64_t)t.nSt * t.nVoxPad;
+    k_table_A<<<(unsigned)((nA + 255) / 256), 256>>>(d_betabar, d_kap64, t.Atab, R, t.nVt, t.nSamPad, nSam);
+    k_table_B<<<(unsigned)((nB + 255) / 256), 256>>>(d_beta64, d_gambar, t.perm, t.Btab, R, t.nSt, t.nVoxPad);
+    A(cudaGetLastError());
+    A(cudaDeviceSynchronize());
+  }
+  cudaFree(d_beta64); cudaFree(d_kap64); cudaFree(d_betabar); cudaFree(d_gambar);
+  if (e != cudaSuccess) {
+    release_device(h);
+    delete h;
+    return cuda_fail(nullptr, e, "hoe_create: model upload");
+  }
+  h->engine = d->engine;
+  if (h->engine == HOE_ENGINE_TC_BF16X3) {
+    std::string why;
+    if (!hoe::tc_supported(h, &why)) {
+      release_device(h);
+      delete h;
+      return fail(nullptr, HOE_ERR_UNSUPPORTED, "tensor-core engine unavailable: %s", why.c_str());
+    }
+    cudaError_t te = hoe::tc_prepare(h);
+    if (te != cudaSuccess) {
+      release_device(h);
+      delete h;
+      return cuda_fail(nullptr, te, "hoe_create: tensor-core operands");
+    }
+  }
+  *out = h;
+  return HOE_OK;
+}
+
+int hoe_close(hoe_handle *h) {
+  if (!valid_handle(h)) return fail(nullptr, HOE_ERR_ARG, "invalid handle");
+  if (h->closed) return HOE_OK;
+  DeviceGuard guard(h->device);
+  cudaDeviceSynchronize();
+  release_device(h);
+  h->closed = 1;
+  return HOE_OK;
+}
+
+void hoe_free(hoe_handle *h) {
+  if (!valid_handle(h)) return;
+  hoe_close(h);
+  h->magic = 0;
+  delete h;
+}
+
+int hoe_get_info(const hoe_handle *h, hoe_info *o) {
+  if (!valid_handle(h) || !o) return fail(nullptr, HOE_ERR_ARG, "invalid handle or output");
+  const auto &t = h->t;
+  o->nSam = t.nSam; o->nCha = t.nCha; o->nVox = t.nVox; o->nTermEff = t.R0; o->nFull = t.nFull;
+  o->engine = h->engine;
+  o->tile_samples = t.ST; o->tile_voxels = t.VT;
+  o->n_sample_tiles = t.nSt; o->n_voxel_tiles = t.nVt;
+  o->split_forward = h->splitF; o->split_adjoint = h->splitA;
+  o->residual_phase_bound = t.residBound;
+  o->device_bytes = h->bytes + (int64_t)h->tc.bytes;
+  return HOE_OK;
+}
+
+int hoe_set_engine(hoe_handle *h, int32_t engine) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (engine == HOE_ENGINE_FP32_SIMT) { h->engine = engine; return HOE_OK; }
+  if (engine != HOE_ENGINE_TC_BF16X3) return fail(h, HOE_ERR_ARG, "unknown engine %d", engine);
+  std::string why;
+  if (!hoe::tc_supported(h, &why))
+    return fail(h, HOE_ERR_UNSUPPORTED, "tensor-core engine unavailable: %s", why.c_str());
+  DeviceGuard guard(h->device);
+  if (!h->tc.ready) {
+    cudaError_t e = hoe::tc_prepare(h);
+    if (e != cudaSuccess) return cuda_fail(h, e, "tensor-core operands");
+  }
+  h->engine = engine;
+  return HOE_OK;
+}
+
+int hoe_set_timing(hoe_handle *h, int32_t enable) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  DeviceGuard guard(h->device);
+  if (enable && !h->ev[0]) {
+    for (auto &e : h->ev) {
+      cudaError_t ce = cudaEventCreate(&e);
+      if (ce != cudaSuccess) { release_events(h); return cuda_fail(h, ce, "hoe_set_timing"); }
+    }
+  }
+  h->timing = enable ? 1 : 0;
+  return HOE_OK;
+}
+
+int hoe_get_timings(hoe_handle *h, hoe_timings *o) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!o) return fail(h, HOE_ERR_ARG, "output must not be NULL");
+  memset(o, 0, sizeof(*o));
+  o->launches = h->launches;
+  if (!h->ev[0]) return HOE_OK;
+  DeviceGuard guard(h->device);
+  auto span = [&](int a, int b, float *out) {
+    if (cudaEventQuery(h->ev[b]) == cudaErrorNotReady) cudaEventSynchronize(h->ev[b]);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev[a], h->ev[b]) == cudaSuccess) *out = ms;
+    cudaGetLastError();  // events never recorded report an error; not a failure here
+  };
+  span(hoe::EV_FK0, hoe::EV_FK1, &o->forward_kernel_ms);
+  span(hoe::EV_AK0, hoe::EV_AK1, &o->adjoint_kernel_ms);
+  span(hoe::EV_F0, hoe::EV_F1, &o->forward_total_ms);
+  span(hoe::EV_A0, hoe::EV_A1, &o->adjoint_total_ms);
+  return HOE_OK;
+}
+
+int hoe_forward(hoe_handle *h, const void *x, void *y, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!x || !y) return fail(h, HOE_ERR_ARG, "x and y must be device pointers");
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  hoe::trace(h, hoe::EV_F0, st);
+  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
+  if (e == cudaSuccess)
+    e = (h->engine == HOE_ENGINE_TC_BF16X3)
+            ? hoe::tc_forward(h, nullptr, (float2 *)y, nullptr, hoe::FWD_TO_Y, st)
+            : hoe::simt_forward(h, nullptr, (float2 *)y, nullptr, hoe::FWD_TO_Y, st);
+  hoe::trace(h, hoe::EV_F1, st);
+  return finish(h, e, "hoe_forward");
+}
+
+int hoe_adjoint(hoe_handle *h, const void *y, void *x, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!x || !y) return fail(h, HOE_ERR_ARG, "x and y must be device pointers");
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  hoe::trace(h, hoe::EV_A0, st);
+  cudaError_t e = hoe::prep_Yt(h, (const float2 *)y, nullptr, st);
+  if (e == cudaSuccess)
+    e = (h->engine == HOE_ENGINE_TC_BF16X3) ? hoe::tc_adjoint_from_Yt(h, (float2 *)x, st)
+                                            : hoe::simt_adjoint_from_Yt(h, (float2 *)x, st);
+  hoe::trace(h, hoe::EV_A1, st);
+  return finish(h, e, "hoe_adjoint");
+}
+
+int hoe_normal(hoe_handle *h, const float *D, const void *x, void *out, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!x || !out) return fail(h, HOE_ERR_ARG, "x and out must be device pointers");
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
+  if (h->engine == HOE_ENGINE_TC_BF16X3) {
+    if (e == cudaSuccess) e = hoe::tc_forward(h, nullptr, nullptr, D, hoe::FWD_TO_YT_WEIGHTED, st);
+    if (e == cudaSuccess) e = hoe::tc_adjoint_from_Yt(h, (float2 *)out, st);
+  } else {
+    if (e == cudaSuccess) e = hoe::simt_forward(h, nullptr, nullptr, D, hoe::FWD_TO_YT_WEIGHTED, st);
+    if (e == cudaSuccess) e = hoe::simt_adjoint_from_Yt(h, (float2 *)out, st);
+  }
+  return finish(h, e, "hoe_normal");
+}
+
+int hoe_derivative(hoe_handle *h, const void *x, void *y, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!h->t.hasKdot) return fail(h, HOE_ERR_ARG, "operator was created without kspha_dt");
+  if (!x || !y) return fail(h, HOE_ERR_ARG, "x and y must be device pointers");
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
+  if (e == cudaSuccess) e = hoe::simt_forward(h, nullptr, (float2 *)y, nullptr, hoe::FWD_DERIV_TO_Y, st);
+  return finish(h, e, "hoe_derivative");
+}
+
+int hoe_backward(hoe_handle *h, const void *x, const void *r, float *dk, float *ddf, double *dt0,
+                 int32_t flags, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!x || !r) return fail(h, HOE_ERR_ARG, "x and r must be device pointers");
+  if ((flags & HOE_GRAD_T0_COEF) && !h->t.hasKdot)
+    return fail(h, HOE_ERR_ARG, "the coefficient part of dL/dt0 needs kspha_dt");
+  if ((flags & HOE_GRAD_KSPHA) && !dk) return fail(h, HOE_ERR_ARG, "dk must be given");
+  if ((flags & HOE_GRAD_FIELDMAP) && !ddf) return fail(h, HOE_ERR_ARG, "ddf must be given");
+  if ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) && !dt0) return fail(h, HOE_ERR_ARG, "dt0 must be given");
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
+  if (e == cudaSuccess)
+    e = hoe::simt_backward(h, (const float2 *)x, (const float2 *)r, dk, ddf, dt0, flags, st);
+  return finish(h, e, "hoe_backward");
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Internal declarations of libhoexplicit.so (not part of the C ABI).
+//
+// Phase decomposition used by every engine
+// ----------------------------------------
+// For voxel v let beta_v = [bf[v,0..R0-1], fieldmap[v]] and for sample s let
+// gamma_s = [kspha[0..R0-1,s], times[s]] (R = R0+1 components), so that the
+// reference phase (array_operator.jl:269) is phi[s,v] = beta_v . gamma_s in
+// cycles.  Voxels are grouped into voxel tiles (compact in space, Morton
+// order) and samples into sample tiles (consecutive in time).  With per-tile
+// anchors betabar (voxel tile) and gammabar (sample tile), exactly
+//
+//   phi[s,v] = A[vt(v), s] + B[st(s), v] + dbeta_v . kappa_s
+//   A[vt,s]  = betabar_vt . kappa_s            kappa_s = gamma_s - gammabar_st(s)
+//   B[st,v]  = beta_v . gammabar_st            dbeta_v = beta_v  - betabar_vt(v)
+//
+// A and B are evaluated once per operator in FP64 and range-reduced to their
+// fractional cycle in [-1/2, 1/2] before being stored as FP32.  Only the
+// residual dbeta.kappa, whose magnitude is bounded by the tile extents (a
+// few cycles at most, reported as residual_phase_bound), is formed per
+// (sample, voxel) pair in FP32.  The sum is range-reduced again before the
+// FP32 sine/cosine, so the argument of every sincos is in [-pi, pi].
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "hoexplicit.h"
+
+#define HOE_MAGIC 0x484f4531  // "HOE1"
+
+namespace hoe {
+
+constexpr int kTileS = 128;   // samples per sample tile (phase anchors, SIMT CTA rows)
+constexpr int kTileV = 128;   // voxels per voxel tile
+
+struct Tables {
+  // sizes
+  int nX = 0, nY = 0, nZ = 0, nFull = 0;
+  int nSam = 0, nCha = 0, nTerm = 0, R0 = 0, R = 0, Rp = 0, nVox = 0;
+  int ST = kTileS, VT = kTileV;
+  int nSt = 0, nVt = 0, nSamPad = 0, nVoxPad = 0, nChaPad = 0;
+  int hasKdot = 0;
+  double residBound = 0.0;
+  // model tables (device)
+  float  *dbeta = nullptr;   // [nVoxPad][Rp]  beta_v - betabar
+  float  *kappa = nullptr;   // [nSamPad][Rp]  gamma_s - gammabar
+  float  *Atab  = nullptr;   // [nVt][nSamPad] frac(betabar . kappa)
+  float  *Btab  = nullptr;   // [nSt][nVoxPad] frac(beta . gammabar)
+  float2 *csm   = nullptr;   // [nVoxPad][nChaPad]
+  int    *perm  = nullptr;   // [nVoxPad] linear grid index, -1 for padding
+  float  *bfraw = nullptr;   // [nVoxPad][Rp]  bf (R0 terms) and fieldmap at slot R0
+  float  *kdot  = nullptr;   // [nSamPad][Rp]  kspha_dt (nTerm terms), zero elsewhere
+  float  *times = nullptr;   // [nSamPad]
+};
+
+struct Scratch {
+  float2 *Z = nullptr;       // [nVoxPad][nChaPad] x .* csm in tile order
+  float2 *Yt = nullptr;      // [nSamPad][nChaPad] data transposed (coil fastest)
+  float2 *part = nullptr;    // split-K partial sums
+  size_t partElems = 0;
+  float  *gpart = nullptr;   // backward partials
+  size_t gpartElems = 0;
+  double *dred = nullptr;    // backward FP64 reduction slots
+};
+
+// Tensor-core operand staging (built lazily when the TC engine is selected).
+struct TcState {
+  bool ready = false;
+  void *buf = nullptr;       // one allocation for all TC operands
+  size_t bytes = 0;
+};
+
+}  // namespace hoe
+
+struct hoe_handle {
+  uint32_t magic = HOE_MAGIC;
+  // tracing (hoe_set_timing): events 0-3 forward, 4-7 adjoint
+  int timing = 0;
+  cudaEvent_t ev[8] = {};
+  mutable int64_t launches = 0;
+  int closed = 0;
+  int device = 0;
+  int engine = HOE_ENGINE_FP32_SIMT;
+  int numSMs = 0;
+  int splitF = 1, splitA = 1;
+  int64_t bytes = 0;
+  std::string err;
+  hoe::Tables t;
+  hoe::Scratch s;
+  hoe::TcState tc;
+};
+
+namespace hoe {
+
+// SIMT kernels (hoe_simt.cu).  All launches are asynchronous on `st`.
+cudaError_t simt_forward(const hoe_handle *h, const float2 *x, float2 *y,
+                         const float *D, int mode, cudaStream_t st);
+cudaError_t simt_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
+cudaError_t prep_Z(const hoe_handle *h, const float2 *x, cudaStream_t st);
+cudaError_t prep_Yt(const hoe_handle *h, const float2 *y, const float *D, cudaStream_t st);
+cudaError_t simt_backward(const hoe_handle *h, const float2 *x, const float2 *r,
+                          float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
+
+// Records trace event i on stream st when tracing is enabled.
+inline void trace(const hoe_handle *h, int i, cudaStream_t st) {
+  if (h->timing && h->ev[i]) cudaEventRecord(h->ev[i], st);
+}
+enum { EV_F0 = 0, EV_FK0 = 1, EV_FK1 = 2, EV_F1 = 3, EV_A0 = 4, EV_AK0 = 5, EV_AK1 = 6, EV_A1 = 7 };
+
+// forward modes
+enum { FWD_TO_Y = 0, FWD_TO_YT_WEIGHTED = 1, FWD_DERIV_TO_Y = 2 };
+
+// Tensor-core kernels (hoe_tc.cu).
+cudaError_t tc_prepare(hoe_handle *h);
+void tc_release(hoe_handle *h);
+cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y,
+                       const float *D, int mode, cudaStream_t st);
+cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
+bool tc_supported(const hoe_handle *h, std::string *why);
+
+}  // namespace hoe

@@ -1,0 +1,147 @@
+"""ctypes binding of libhoexplicit.so (declarations in include/hoexplicit.h).
+
+The library is the only compute path: if it cannot be loaded, every operator
+constructor raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent.parent
+LIB_PATH = Path(os.environ.get("HOE_LIBRARY", PKG_DIR / "libhoexplicit.so"))
+
+HOE_ABI_VERSION = 1
+HOE_OK = 0
+HOE_ERR_ARG = -1
+HOE_ERR_DIM = -2
+HOE_ERR_OOM = -3
+HOE_ERR_CUDA = -4
+HOE_ERR_TIMEOUT = -5
+HOE_ERR_CLOSED = -6
+HOE_ERR_UNSUPPORTED = -7
+
+HOE_ENGINE_FP32_SIMT = 0
+HOE_ENGINE_TC_BF16X3 = 1
+
+HOE_GRAD_KSPHA = 1
+HOE_GRAD_FIELDMAP = 2
+HOE_GRAD_T0_B0 = 4
+HOE_GRAD_T0_COEF = 8
+
+EXPORTED = (
+    "hoe_version", "hoe_abi_version", "hoe_create", "hoe_close", "hoe_free", "hoe_is_closed",
+    "hoe_last_error", "hoe_get_info", "hoe_set_engine", "hoe_forward", "hoe_adjoint",
+    "hoe_normal", "hoe_derivative", "hoe_backward", "hoe_set_timing", "hoe_get_timings",
+)
+
+
+class ArgumentError(ValueError):
+    """Julia ``ArgumentError`` counterpart."""
+
+
+class DimensionMismatch(ValueError):
+    """Julia ``DimensionMismatch`` counterpart."""
+
+
+class OutOfMemoryError(MemoryError):
+    """Julia ``OutOfMemoryError`` counterpart (device allocation failed)."""
+
+
+class HoeError(RuntimeError):
+    """CUDA runtime failure or unsupported mode reported by the library."""
+
+
+class HoeDesc(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_int32),
+        ("nX", ctypes.c_int32), ("nY", ctypes.c_int32), ("nZ", ctypes.c_int32),
+        ("nSam", ctypes.c_int32), ("nCha", ctypes.c_int32), ("nTerm", ctypes.c_int32),
+        ("has_concomitant", ctypes.c_int32), ("nVox", ctypes.c_int32),
+        ("engine", ctypes.c_int32), ("device", ctypes.c_int32),
+        ("tile_samples", ctypes.c_int32), ("tile_voxels", ctypes.c_int32),
+        ("split_hint", ctypes.c_int32),
+        ("mask_idx", ctypes.POINTER(ctypes.c_int32)),
+        ("bf", ctypes.POINTER(ctypes.c_double)),
+        ("kspha", ctypes.POINTER(ctypes.c_double)),
+        ("times", ctypes.POINTER(ctypes.c_double)),
+        ("fieldmap", ctypes.POINTER(ctypes.c_double)),
+        ("csm", ctypes.POINTER(ctypes.c_double)),
+        ("kspha_dt", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+class HoeTimings(ctypes.Structure):
+    _fields_ = [
+        ("forward_kernel_ms", ctypes.c_float), ("adjoint_kernel_ms", ctypes.c_float),
+        ("forward_total_ms", ctypes.c_float), ("adjoint_total_ms", ctypes.c_float),
+        ("launches", ctypes.c_int64),
+    ]
+
+
+class HoeInfo(ctypes.Structure):
+    _fields_ = [
+        ("nSam", ctypes.c_int32), ("nCha", ctypes.c_int32), ("nVox", ctypes.c_int32),
+        ("nTermEff", ctypes.c_int32), ("nFull", ctypes.c_int32), ("engine", ctypes.c_int32),
+        ("tile_samples", ctypes.c_int32), ("tile_voxels", ctypes.c_int32),
+        ("n_sample_tiles", ctypes.c_int32), ("n_voxel_tiles", ctypes.c_int32),
+        ("split_forward", ctypes.c_int32), ("split_adjoint", ctypes.c_int32),
+        ("residual_phase_bound", ctypes.c_double), ("device_bytes", ctypes.c_int64),
+    ]
+
+
+_lib = None
+
+
+def load():
+    """Load libhoexplicit.so once; raise if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"libhoexplicit.so not found at {LIB_PATH}; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(str(LIB_PATH))
+    vp = ctypes.c_void_p
+    H = ctypes.c_void_p
+    lib.hoe_version.restype = ctypes.c_char_p
+    lib.hoe_abi_version.restype = ctypes.c_int
+    lib.hoe_create.argtypes = [ctypes.POINTER(H), ctypes.POINTER(HoeDesc)]
+    lib.hoe_close.argtypes = [H]
+    lib.hoe_free.argtypes = [H]
+    lib.hoe_free.restype = None
+    lib.hoe_is_closed.argtypes = [H]
+    lib.hoe_last_error.argtypes = [H]
+    lib.hoe_last_error.restype = ctypes.c_char_p
+    lib.hoe_get_info.argtypes = [H, ctypes.POINTER(HoeInfo)]
+    lib.hoe_set_engine.argtypes = [H, ctypes.c_int32]
+    lib.hoe_forward.argtypes = [H, vp, vp, vp]
+    lib.hoe_adjoint.argtypes = [H, vp, vp, vp]
+    lib.hoe_normal.argtypes = [H, vp, vp, vp, vp]
+    lib.hoe_derivative.argtypes = [H, vp, vp, vp]
+    lib.hoe_backward.argtypes = [H, vp, vp, vp, vp, vp, ctypes.c_int32, vp]
+    lib.hoe_set_timing.argtypes = [H, ctypes.c_int32]
+    lib.hoe_get_timings.argtypes = [H, ctypes.POINTER(HoeTimings)]
+    for name in EXPORTED:
+        if name not in ("hoe_free",):
+            getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int
+    if lib.hoe_abi_version() != HOE_ABI_VERSION:
+        raise ImportError("libhoexplicit.so ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def check(rc: int, handle=None) -> None:
+    """Map a status code to the exception type the reference would raise."""
+    if rc == HOE_OK:
+        return
+    msg = load().hoe_last_error(handle).decode(errors="replace")
+    if rc in (HOE_ERR_ARG, HOE_ERR_CLOSED):
+        raise ArgumentError(msg)
+    if rc == HOE_ERR_DIM:
+        raise DimensionMismatch(msg)
+    if rc == HOE_ERR_OOM:
+        raise OutOfMemoryError(msg)
+    raise HoeError(f"[{rc}] {msg}")

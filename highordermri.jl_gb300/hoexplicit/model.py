@@ -1,0 +1,168 @@
+"""Host-side model preparation: grid, solid-harmonic basis, order selection,
+concomitant terms.  These run once per operator on the host, as in the
+reference (array_operator.jl:121-139; explicit_gpu_operator.jl:355-360).
+
+Arrays follow the reference's Julia conventions.  Spatial arrays are shaped
+``(nX, nY, nZ)`` (or ``(nX, nY)`` when nZ == 1) and flattened in Fortran order
+(x fastest); ``kspha`` is ``(nTerm, nSam)``; ``csm`` is ``(nX, nY[, nZ], nCha)``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from ._lib import ArgumentError, DimensionMismatch
+
+
+@dataclass
+class Grid:
+    """Centred Cartesian grid (src/Grid/Grid.jl:116-128, constructor :163-194).
+
+    ``r[j] = (j - (N+1)/2) * delta`` for 1-based j, x index fastest in the
+    flattened coordinate vectors, metres.
+    """
+
+    nX: int
+    nY: int
+    nZ: int
+    dx: float = 1.0
+    dy: float = 1.0
+    dz: float = 1.0
+    x: np.ndarray = field(default=None, repr=False)
+    y: np.ndarray = field(default=None, repr=False)
+    z: np.ndarray = field(default=None, repr=False)
+
+    def __post_init__(self):
+        if self.x is None:
+            i = np.arange(1, self.nX + 1, dtype=np.float64)
+            j = np.arange(1, self.nY + 1, dtype=np.float64)
+            k = np.arange(1, self.nZ + 1, dtype=np.float64)
+            ii = np.tile(i, self.nY * self.nZ)
+            jj = np.tile(np.repeat(j, self.nX), self.nZ)
+            kk = np.repeat(k, self.nX * self.nY)
+            self.x = (ii - (self.nX + 1) / 2.0) * self.dx
+            self.y = (jj - (self.nY + 1) / 2.0) * self.dy
+            self.z = (kk - (self.nZ + 1) / 2.0) * self.dz
+
+    @property
+    def matrixSize(self):
+        return (self.nX, self.nY, self.nZ)
+
+    @property
+    def resolution(self):
+        return (self.dx, self.dy, self.dz)
+
+    def struct_to_dict(self):
+        """Dictionary round trip of Grid.jl:196-209."""
+        return {"schema_version": 1, "nX": self.nX, "nY": self.nY, "nZ": self.nZ,
+                "delta_x": self.dx, "delta_y": self.dy, "delta_z": self.dz,
+                "x": np.asarray(self.x), "y": np.asarray(self.y), "z": np.asarray(self.z),
+                "matrix_size": [self.nX, self.nY, self.nZ],
+                "resolution": [self.dx, self.dy, self.dz]}
+
+    @classmethod
+    def from_dict(cls, d):
+        """Restore from ``struct_to_dict`` output (Grid.jl:224-250)."""
+        s = lambda v: np.asarray(v).reshape(-1)[0].item() if np.ndim(v) else v
+        return cls(int(s(d["nX"])), int(s(d["nY"])), int(s(d["nZ"])), float(s(d["delta_x"])),
+                   float(s(d["delta_y"])), float(s(d["delta_z"])),
+                   x=np.asarray(d["x"], dtype=np.float64).ravel(),
+                   y=np.asarray(d["y"], dtype=np.float64).ravel(),
+                   z=np.asarray(d["z"], dtype=np.float64).ravel())
+
+
+def _term(t: int, x, y, z):
+    r2 = x * x + y * y + z * z
+    if t == 1:
+        return np.ones_like(x)
+    if t == 2:
+        return x.copy()
+    if t == 3:
+        return y.copy()
+    if t == 4:
+        return z.copy()
+    if t == 5:
+        return x * y
+    if t == 6:
+        return z * y
+    if t == 7:
+        return 3 * z ** 2 - r2
+    if t == 8:
+        return x * z
+    if t == 9:
+        return x ** 2 - y ** 2
+    if t == 10:
+        return 3 * y * x ** 2 - y ** 3
+    if t == 11:
+        return x * z * y
+    if t == 12:
+        return (5 * z ** 2 - r2) * y
+    if t == 13:
+        return 5 * z ** 3 - 3 * z * r2
+    if t == 14:
+        return (5 * z ** 2 - r2) * x
+    if t == 15:
+        return x ** 2 * z - y ** 2 * z
+    if t == 16:
+        return x ** 3 - 3 * x * y ** 2
+    raise ArgumentError(f"basis term {t} is not used by the explicit operator (terms 1-16)")
+
+
+def basisfunc_spha(x, y, z, terms):
+    """Unnormalised real solid harmonics (basisfunction.jl:27-126), terms 1-16.
+
+    Returns ``(len(x), len(terms))``, columns in the requested order.
+    """
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    z = np.asarray(z, dtype=np.float64)
+    if np.isscalar(terms):
+        return _term(int(terms), x, y, z)
+    out = np.empty((x.size, len(terms)), dtype=np.float64, order="F")
+    for i, t in enumerate(terms):
+        out[:, i] = _term(int(t), x, y, z)
+    return out
+
+
+def prep_kspha(kspha, k_nominal, nTerm: int, recon_terms=None):
+    """Order selection of prep_kspha.jl:1-56; returns a modified copy.
+
+    A '0' digit zeroes its order, except first order, whose rows 2:4 are
+    replaced by ``k_nominal``.
+    """
+    if recon_terms is None:
+        recon_terms = "111" if nTerm == 9 else "1111"
+    expected = 3 if nTerm == 9 else (4 if nTerm == 16 else 0)
+    if expected == 0:
+        raise ArgumentError(f"nTerm must be 9 or 16, got {nTerm}")
+    if len(recon_terms) != expected:
+        raise ArgumentError(f"recon_terms must contain {expected} binary digits for nTerm={nTerm}")
+    if any(c not in "01" for c in recon_terms):
+        raise ArgumentError(f"recon_terms must contain only '0' and '1', got {recon_terms!r}")
+    flags = [c == "1" for c in recon_terms] + ([False] if nTerm == 9 else [])
+    out = np.array(kspha, dtype=np.float64, copy=True)
+    if not flags[0]:
+        out[0, :] = 0.0
+    if not flags[1]:
+        out[1:4, :] = np.asarray(k_nominal, dtype=np.float64)
+    if not flags[2]:
+        out[4:9, :] = 0.0
+    if nTerm == 16 and not flags[3]:
+        out[9:16, :] = 0.0
+    return out
+
+
+def prep_concomitant(bf, kspha, x, y, z, concomitant=None):
+    """Append the concomitant basis [z^2, x^2+y^2, xz, yz] and its 4
+    coefficient rows (prep_kspha.jl:78-98).  x, y, z are masked coordinates."""
+    if concomitant is None:
+        return bf, kspha
+    c = np.asarray(concomitant)
+    if np.iscomplexobj(c) or not np.issubdtype(c.dtype, np.number):
+        raise ArgumentError("concomitant must be a real array or nothing")
+    if c.shape != (4, kspha.shape[1]):
+        raise DimensionMismatch(f"concomitant must have size {(4, kspha.shape[1])}, got {c.shape}")
+    bf_c = np.stack([z ** 2, x ** 2 + y ** 2, x * z, y * z], axis=1)
+    return (np.asfortranarray(np.hstack([bf, bf_c])),
+            np.vstack([kspha, c.astype(np.float64)]))

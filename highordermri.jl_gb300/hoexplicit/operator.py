@@ -1,0 +1,440 @@
+"""The GB300 explicit encoding operator: host-side mirror of the reference's
+``HighOrderExplicitOp`` surface over the C ABI of libhoexplicit.so.
+
+Reference surface mirrored (paths inside HighOrderMRI.jl):
+  * constructor and validation — HighOrderExplicitOp.jl:44-51,
+    explicit_gpu_operator.jl:299-392, array_operator.jl:83-181
+  * ``op * x`` (prod!), ``adjoint(op) * y`` (ctprod!) — explicit_gpu_operator.jl:387-397
+  * ``normalOperator(op, D)`` with its weight checks — explicit_gpu_operator.jl:399-416
+  * ``explicit_gpu_normal(op; weights)`` — explicit_gpu_operator.jl:431-433
+  * ``close(op)``: idempotent, use after close raises ArgumentError — :40-44, :435-446
+  * ``kspha_dt`` derivative mode of the forward product — array_operator.jl:153-166
+
+Solver vectors are torch CUDA complex64 tensors on the operator's device
+(the counterpart of ``CuVector{ComplexF32}``, storage_type at
+explicit_gpu_operator.jl:115).  numpy arrays are also accepted: they are
+copied to the device and the result is copied back (host round trip).
+"""
+from __future__ import annotations
+
+import ctypes
+import weakref
+
+import numpy as np
+
+from . import _lib
+from ._lib import ArgumentError, DimensionMismatch
+from .model import Grid, basisfunc_spha, prep_concomitant, prep_kspha
+
+ENGINES = {"fp32": _lib.HOE_ENGINE_FP32_SIMT, "simt": _lib.HOE_ENGINE_FP32_SIMT,
+           "tc": _lib.HOE_ENGINE_TC_BF16X3, "bf16x3": _lib.HOE_ENGINE_TC_BF16X3}
+DEFAULT_ENGINE = "fp32"
+
+
+def _torch():
+    import torch  # device memory and streams only
+    return torch
+
+
+def _fortran_flat(a):
+    return np.asarray(a).reshape(-1, order="F")
+
+
+def _dptr(arr):
+    return arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if arr is not None else None
+
+
+class _Vec:
+    """Normalises a solver vector to a contiguous complex64 CUDA tensor."""
+
+    def __init__(self, op, v, n, name):
+        torch = _torch()
+        self.host = None
+        if isinstance(v, np.ndarray):
+            self.host = "numpy"
+            v = torch.from_numpy(np.ascontiguousarray(v.reshape(-1), dtype=np.complex64))
+        if not isinstance(v, torch.Tensor):
+            raise ArgumentError(f"{name} must be a torch tensor or numpy array")
+        if v.numel() != n:
+            raise DimensionMismatch(f"{name} has length {v.numel()}, expected {n}")
+        if v.device.type != "cuda":
+            if self.host is None:
+                self.host = "cpu"
+            v = v.to(device=op.torch_device, non_blocking=False)
+        elif v.device.index != op.device:
+            raise ArgumentError(f"{name} is on cuda:{v.device.index}, operator on cuda:{op.device}")
+        if v.dtype != torch.complex64:
+            v = v.to(torch.complex64)
+        self.t = v.reshape(-1).contiguous()
+
+    def out_like(self, result):
+        if self.host == "numpy":
+            return result.cpu().numpy()
+        if self.host == "cpu":
+            return result.cpu()
+        return result
+
+
+class ExplicitGB300Op:
+    """Resident explicit encoding operator on one GB300 (the ``:gb300`` backend).
+
+    Size ``(nSam*nCha, prod(grid.matrixSize))``, element type ComplexF32.
+    Not reentrant: the operator owns scratch space on its device.
+    """
+
+    symmetric = False
+    hermitian = False
+
+    def __init__(self, grid: Grid, kspha, times, *, fieldmap=None, csm=None, mask=None,
+                 concomitant=None, recon_terms=None, k_nominal=None, kspha_dt=None, kdot=None,
+                 engine: str = DEFAULT_ENGINE, gpus=None, split_hint: int = 0):
+        lib = _lib.load()
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise _lib.HoeError("the :gb300 explicit operator requires a CUDA device")
+        if engine not in ENGINES:
+            raise ArgumentError(f"unknown engine {engine!r}; choose one of {sorted(ENGINES)}")
+        if gpus is not None:
+            ids = [int(g) for g in gpus]
+            if len(ids) != 1:
+                raise ArgumentError("the :gb300 operator uses exactly one GPU")
+            if not 0 <= ids[0] < torch.cuda.device_count():
+                raise ArgumentError("invalid visible GPU ID")
+            device = ids[0]
+        else:
+            device = torch.cuda.current_device()
+
+        kspha = np.asarray(kspha)
+        if kspha.ndim != 2:
+            raise DimensionMismatch("kspha must be (nTerm, nSam)")
+        nTerm, nSam = kspha.shape
+        if nTerm not in (9, 16):
+            raise ArgumentError("kspha requires 9 or 16 terms")
+        times = np.asarray(times, dtype=np.float64).reshape(-1)
+        if times.size != nSam:
+            raise DimensionMismatch("times and kspha")
+        nFull = grid.nX * grid.nY * grid.nZ
+        mask = np.ones(nFull, dtype=bool) if mask is None else _fortran_flat(mask).astype(bool)
+        if mask.size != nFull:
+            raise DimensionMismatch("mask and grid")
+        fieldmap = np.zeros(nFull) if fieldmap is None else _fortran_flat(fieldmap).astype(np.float64)
+        if fieldmap.size != nFull:
+            raise DimensionMismatch("fieldmap and mask")
+        if csm is None:
+            csm_flat = np.ones((nFull, 1), dtype=np.complex128)
+        else:
+            csm = np.asarray(csm)
+            nCha_ = csm.shape[-1]
+            if csm.size != nFull * nCha_:
+                raise DimensionMismatch("csm and grid")
+            csm_flat = csm.reshape(nFull, nCha_, order="F").astype(np.complex128)
+        nCha = csm_flat.shape[1]
+        idx = np.flatnonzero(mask)
+        nVox = idx.size
+        if nVox == 0:
+            raise ArgumentError("mask must contain voxels")
+        if nSam <= 0 or nCha <= 0:
+            raise ArgumentError("samples and coils must be positive")
+        if k_nominal is None:
+            k_nominal = kspha[1:4, :]
+        k_nominal = np.asarray(k_nominal, dtype=np.float64)
+        if k_nominal.shape[0] != 3:
+            raise ArgumentError("k_nominal must have 3 terms (row) for kx, ky, kz")
+
+        prepared = prep_kspha(kspha, k_nominal, nTerm, recon_terms)
+        xm, ym, zm = grid.x[idx], grid.y[idx], grid.z[idx]
+        bf = basisfunc_spha(xm, ym, zm, list(range(1, nTerm + 1)))
+        self.derivative_mode = kspha_dt is not None
+        # the derivative mode ignores concomitant terms (array_operator.jl:139)
+        bf, prepared = prep_concomitant(bf, prepared, xm, ym, zm,
+                                        None if self.derivative_mode else concomitant)
+        has_conc = int(prepared.shape[0] != nTerm)
+        kd = kspha_dt if kspha_dt is not None else kdot
+        if kd is not None:
+            kd = np.asfortranarray(kd, dtype=np.float64)
+            if kd.shape != (nTerm, nSam):
+                raise ArgumentError("kspha_dt must have same size as kspha")
+
+        self._keep = dict(
+            mask_idx=np.ascontiguousarray(idx, dtype=np.int32),
+            bf=np.asfortranarray(bf, dtype=np.float64),
+            kspha=np.asfortranarray(prepared, dtype=np.float64),
+            times=np.ascontiguousarray(times),
+            fieldmap=np.ascontiguousarray(fieldmap[idx]),
+            csm=np.asfortranarray(csm_flat[idx, :]),
+            kspha_dt=kd,
+        )
+        k = self._keep
+        desc = _lib.HoeDesc()
+        desc.abi_version = _lib.HOE_ABI_VERSION
+        desc.nX, desc.nY, desc.nZ = grid.nX, grid.nY, grid.nZ
+        desc.nSam, desc.nCha, desc.nTerm = nSam, nCha, nTerm
+        desc.has_concomitant = has_conc
+        desc.nVox = nVox
+        desc.engine = ENGINES[engine]
+        desc.device = device
+        desc.split_hint = int(split_hint)
+        desc.mask_idx = k["mask_idx"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+        desc.bf = _dptr(k["bf"])
+        desc.kspha = _dptr(k["kspha"])
+        desc.times = _dptr(k["times"])
+        desc.fieldmap = _dptr(k["fieldmap"])
+        desc.csm = k["csm"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        desc.kspha_dt = _dptr(kd)
+        handle = ctypes.c_void_p()
+        torch.cuda.init()
+        _lib.check(lib.hoe_create(ctypes.byref(handle), ctypes.byref(desc)))
+        self._h = handle
+        self._finalizer = weakref.finalize(self, lib.hoe_free, handle)
+
+        self.grid = grid
+        self.device = device
+        self.torch_device = torch.device("cuda", device)
+        self.nSam, self.nCha, self.nVox, self.nTerm = nSam, nCha, nVox, nTerm
+        self.nTermEff = prepared.shape[0]
+        self.nrow = nSam * nCha
+        self.ncol = nFull
+        self.shape = (self.nrow, self.ncol)
+        self.mask = mask
+        self.engine = engine
+        self.nprod = self.ntprod = self.nctprod = 0
+        self.tprod = None
+
+    # ------------------------------------------------------------------ misc
+    def _handle(self):
+        if self._h is None or _lib.load().hoe_is_closed(self._h):
+            raise ArgumentError("operator is closed")
+        return self._h
+
+    def _stream(self):
+        return _torch().cuda.current_stream(self.device).cuda_stream
+
+    def info(self) -> dict:
+        inf = _lib.HoeInfo()
+        _lib.check(_lib.load().hoe_get_info(self._handle(), ctypes.byref(inf)), self._h)
+        return {name: getattr(inf, name) for name, _ in inf._fields_}
+
+    def set_timing(self, enable: bool = True) -> None:
+        """Enable CUDA-event tracing of forward/adjoint calls (hoe_set_timing)."""
+        _lib.check(_lib.load().hoe_set_timing(self._handle(), int(bool(enable))), self._h)
+
+    def timings(self) -> dict:
+        """Durations (ms) of the last traced calls and the launch count."""
+        t = _lib.HoeTimings()
+        _lib.check(_lib.load().hoe_get_timings(self._handle(), ctypes.byref(t)), self._h)
+        return {name: getattr(t, name) for name, _ in t._fields_}
+
+    def set_engine(self, engine: str) -> None:
+        if engine not in ENGINES:
+            raise ArgumentError(f"unknown engine {engine!r}")
+        _lib.check(_lib.load().hoe_set_engine(self._handle(), ENGINES[engine]), self._h)
+        self.engine = engine
+
+    def close(self) -> None:
+        """Release device resources; idempotent (explicit_gpu_operator.jl:435-446)."""
+        if self._h is not None:
+            _lib.load().hoe_close(self._h)
+
+    @property
+    def closed(self) -> bool:
+        return self._h is None or bool(_lib.load().hoe_is_closed(self._h))
+
+    # ------------------------------------------------------------ products
+    def prod_(self, out, x):
+        """In-place forward: out = E x (or B x in the kspha_dt mode)."""
+        fn = _lib.load().hoe_derivative if self.derivative_mode else _lib.load().hoe_forward
+        _lib.check(fn(self._handle(), x.data_ptr(), out.data_ptr(), self._stream()), self._h)
+        self.nprod += 1
+        return out
+
+    def ctprod_(self, out, y):
+        """In-place adjoint: out = E^H y (zeros outside the mask)."""
+        _lib.check(_lib.load().hoe_adjoint(self._handle(), y.data_ptr(), out.data_ptr(),
+                                           self._stream()), self._h)
+        self.nctprod += 1
+        return out
+
+    def forward(self, x):
+        v = _Vec(self, x, self.ncol, "x")
+        self._handle()
+        out = _torch().empty(self.nrow, dtype=_torch().complex64, device=self.torch_device)
+        return v.out_like(self.prod_(out, v.t))
+
+    def adjoint_apply(self, y):
+        v = _Vec(self, y, self.nrow, "y")
+        self._handle()
+        out = _torch().empty(self.ncol, dtype=_torch().complex64, device=self.torch_device)
+        return v.out_like(self.ctprod_(out, v.t))
+
+    def __mul__(self, x):
+        return self.forward(x)
+
+    __matmul__ = __mul__
+
+    @property
+    def H(self):
+        return AdjointOp(self)
+
+    def backward(self, x, r, *, kspha=True, fieldmap=True, t0_b0=True, t0_coef=False):
+        """Gradient of L = 0.5*||E x - y||^2 given the residual r = E x - y.
+
+        Returns (dL/dkspha (nTermEff, nSam) float32 tensor, dL/dfieldmap
+        (nFull,) float32 tensor zero outside the mask, dL/dt0 float64 tensor of
+        one element); unrequested outputs are None.  ``t0_coef`` needs
+        ``kspha_dt`` or ``kdot`` at construction.
+        """
+        torch = _torch()
+        xv = _Vec(self, x, self.ncol, "x")
+        rv = _Vec(self, r, self.nrow, "r")
+        flags = ((_lib.HOE_GRAD_KSPHA if kspha else 0) | (_lib.HOE_GRAD_FIELDMAP if fieldmap else 0)
+                 | (_lib.HOE_GRAD_T0_B0 if t0_b0 else 0) | (_lib.HOE_GRAD_T0_COEF if t0_coef else 0))
+        dk = torch.empty((self.nSam, self.nTermEff), dtype=torch.float32, device=self.torch_device) if kspha else None
+        ddf = torch.empty(self.ncol, dtype=torch.float32, device=self.torch_device) if fieldmap else None
+        dt0 = torch.zeros(1, dtype=torch.float64, device=self.torch_device) if (t0_b0 or t0_coef) else None
+        p = lambda t: t.data_ptr() if t is not None else None
+        _lib.check(_lib.load().hoe_backward(self._handle(), xv.t.data_ptr(), rv.t.data_ptr(),
+                                            p(dk), p(ddf), p(dt0), flags, self._stream()), self._h)
+        return (dk.t() if dk is not None else None), ddf, dt0
+
+
+class AdjointOp:
+    """``adjoint(op)``: prod and ctprod swapped (explicit_gpu_operator.jl:394-397)."""
+
+    def __init__(self, op: ExplicitGB300Op):
+        self.op = op
+        self.nrow, self.ncol = op.ncol, op.nrow
+        self.shape = (self.nrow, self.ncol)
+
+    def __mul__(self, y):
+        return self.op.adjoint_apply(y)
+
+    __matmul__ = __mul__
+
+    def prod_(self, out, y):
+        return self.op.ctprod_(out, y)
+
+    def ctprod_(self, out, x):
+        return self.op.prod_(out, x)
+
+    @property
+    def H(self):
+        return self.op
+
+
+class WeightingOp:
+    """Diagonal weighting W with raw complex sample weights repeated ``rep``
+    times (LinearOperatorCollection WeightingOp as used by recon_HOOp.jl:77)."""
+
+    def __init__(self, weights, rep: int = 1):
+        self.weights = np.tile(np.asarray(weights).reshape(-1), rep)
+        self.rep = rep
+
+
+class WeightedOp:
+    """``W ∘ op`` (recon_HOOp.jl:78)."""
+
+    def __init__(self, W: WeightingOp, op: ExplicitGB300Op):
+        if W.weights.size != op.nrow:
+            raise DimensionMismatch("weights and operator rows")
+        self.W, self.op = W, op
+        self.nrow, self.ncol = op.nrow, op.ncol
+
+
+def compose(W: WeightingOp, op: ExplicitGB300Op) -> WeightedOp:
+    return WeightedOp(W, op)
+
+
+class NormalOp:
+    """``E^H D E`` sharing its parent's workspace and lifetime."""
+
+    hermitian = True
+
+    def __init__(self, op: ExplicitGB300Op, D: np.ndarray):
+        torch = _torch()
+        self.op = op
+        self.nrow = self.ncol = op.ncol
+        self.shape = (self.ncol, self.ncol)
+        self.D = torch.from_numpy(np.ascontiguousarray(D, dtype=np.float32)).to(op.torch_device)
+
+    def prod_(self, out, x):
+        op = self.op
+        _lib.check(_lib.load().hoe_normal(op._handle(), self.D.data_ptr(), x.data_ptr(),
+                                          out.data_ptr(), op._stream()), op._h)
+        return out
+
+    def __mul__(self, x):
+        v = _Vec(self.op, x, self.ncol, "x")
+        self.op._handle()
+        out = _torch().empty(self.ncol, dtype=_torch().complex64, device=self.op.torch_device)
+        return v.out_like(self.prod_(out, v.t))
+
+    __matmul__ = __mul__
+
+
+def normal_diagonal(weights, nSam: int, nCha: int) -> np.ndarray:
+    """Validate and expand normal weights to the real diagonal D (length
+    nSam*nCha), with the rules of explicit_gpu_operator.jl:402-412."""
+    if isinstance(weights, WeightingOp):
+        weights = np.abs(weights.weights) ** 2
+    if weights is None:
+        D = np.ones(nSam * nCha)
+    else:
+        if hasattr(weights, "detach"):
+            weights = weights.detach().cpu().numpy()
+        D = np.asarray(weights).reshape(-1)
+    if D.size == nSam:
+        D = np.tile(D, nCha)
+    if D.size != nSam * nCha:
+        raise DimensionMismatch("normal weights")
+    if not np.all(np.isfinite(D)):
+        raise ArgumentError("normal weights must be finite")
+    eps = float(np.finfo(np.float32).eps)
+    if np.iscomplexobj(D):
+        if np.max(np.abs(D.imag)) > 10 * eps * max(1.0, float(np.max(np.abs(D)))):
+            raise ArgumentError("normal weights must already be real nonnegative WᴴW")
+        D = D.real
+    if np.min(D) < 0:
+        raise ArgumentError("normal weights must be nonnegative")
+    return D.astype(np.float64)
+
+
+def normalOperator(op, weights=None):
+    """Data normal ``A^H D A``; ``weights`` is the already squared real
+    non-negative diagonal D (length nSam or nSam*nCha), a WeightingOp (whose
+    raw weights are squared once), or None for unit weights.  A ``W ∘ op``
+    argument supplies W^H W (explicit_gpu_operator.jl:399-416)."""
+    if isinstance(op, WeightedOp):
+        return normalOperator(op.op, np.abs(op.W.weights) ** 2)
+    if not isinstance(op, ExplicitGB300Op):
+        raise ArgumentError("normalOperator expects the :gb300 operator")
+    op._handle()
+    return NormalOp(op, normal_diagonal(weights, op.nSam, op.nCha))
+
+
+def explicit_gpu_normal(op, weights=None):
+    """``A^H D A`` with ``D = abs2.(weights)`` from raw sample weights
+    (explicit_gpu_operator.jl:431-433)."""
+    if weights is None:
+        return normalOperator(op, None)
+    if hasattr(weights, "detach"):
+        weights = weights.detach().cpu().numpy()
+    return normalOperator(op, np.abs(np.asarray(weights)) ** 2)
+
+
+def HighOrderExplicitOp(grid: Grid, kspha, times, *, implementation: str = "gb300", **kwargs):
+    """Construct the explicit encoding operator (HighOrderExplicitOp.jl:44-51).
+
+    This package provides the ``:gb300`` implementation only; the reference's
+    ``:array`` and ``:kernel`` implementations are not part of it.
+    """
+    impl = str(implementation).lstrip(":")
+    if impl != "gb300":
+        raise ArgumentError("implementation must be :gb300 (this package has no :array or :kernel backend)")
+    kwargs.pop("arrayType", None)
+    kwargs.pop("nBlock", None)
+    kwargs.pop("verbose", None)
+    return ExplicitGB300Op(grid, kspha, times, **kwargs)
+
+
+def close(op) -> None:
+    op.close()

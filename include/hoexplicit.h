@@ -1,0 +1,169 @@
+/*
+ * hoexplicit.h — C ABI of libhoexplicit.so, the GB300 (sm_103a) explicit
+ * higher-order MRI encoding operator.
+ *
+ * The operator is
+ *
+ *   y[s,c] = (1/sqrt(nVox)) * sum_{v in mask} exp(+i*2*pi*phi[s,v]) * x[v] * csm[v,c]
+ *   phi[s,v] = sum_l bf[v,l] * kspha[l,s] + times[s] * fieldmap[v]      (cycles)
+ *
+ * with the adjoint writing zeros outside the mask.  Units follow the
+ * reference: coefficients in cycles/m^p, coordinates in metres, times in
+ * seconds, fieldmap in Hz.  Layouts follow the reference's Julia arrays
+ * (column-major):
+ *   image x   : complex64 [prod(matrixSize)], x index fastest
+ *   data  y   : complex64 [nSam*nCha], samples fastest, then coils
+ *   bf        : float64 [nVox x nTermEff]      element (v,l) at v + l*nVox
+ *   kspha     : float64 [nTermEff x nSam]      element (l,s) at l + s*nTermEff
+ *   csm       : complex128 [nVox x nCha]       element (v,c) at 2*(v + c*nVox)
+ *
+ * Reference interfaces each entry point replaces (paths inside the
+ * HighOrderMRI.jl tree):
+ *   hoe_create        ExplicitGPUOp constructor,
+ *                     src/EncodingOperator/Explicit/explicit_gpu_operator.jl:299-392
+ *                     (model preparation by prep_kspha / basisfunc_spha /
+ *                     prep_concomitant stays on the caller's side, as in
+ *                     array_operator.jl:124-139)
+ *   hoe_forward       explicit_gpu_forward!, explicit_gpu_operator.jl:226-246
+ *                     (math of explicit_array_forward, array_operator.jl:241-288)
+ *   hoe_adjoint       explicit_gpu_adjoint!, explicit_gpu_operator.jl:248-270
+ *                     (math of explicit_array_adjoint, array_operator.jl:294-348)
+ *   hoe_normal        explicit_gpu_normal!, explicit_gpu_operator.jl:272-297, with the
+ *                     weight checks of normalOperator, explicit_gpu_operator.jl:399-416
+ *   hoe_derivative    explicit_array_derivative, array_operator.jl:187-235
+ *                     (the kspha_dt mode used by FindDelay, FindDelay.jl:195-200)
+ *   hoe_backward      no reference counterpart: gradient of 0.5*||E x - y||^2 with
+ *                     respect to kspha, fieldmap and a time origin t0
+ *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
+ *   hoe_free          releases the host handle (Julia finalizer)
+ *   hoe_set_timing / hoe_get_timings
+ *                     CUDA-event tracing; replaces the reference's ad-hoc @elapsed
+ *                     timing of the legacy path, kernel_operator.jl:333-349
+ *
+ * Conventions: every entry point returns HOE_OK (0) or a negative HOE_ERR_*
+ * code; nothing throws across the ABI.  The message of the last failure is
+ * kept per handle (hoe_last_error) or per thread for failures without a
+ * handle (hoe_last_error(NULL)).  Device pointers are caller-owned, on the
+ * handle's device, and are never freed by the library.  Calls are ordered on
+ * the stream argument (a cudaStream_t; NULL = legacy default stream).  A handle
+ * owns scratch space and is not reentrant: one call at a time per handle.
+ */
+#ifndef HOEXPLICIT_H
+#define HOEXPLICIT_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HOE_API __attribute__((visibility("default")))
+#else
+#define HOE_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HOE_ABI_VERSION 1
+
+/* status codes */
+#define HOE_OK               0
+#define HOE_ERR_ARG         -1   /* invalid argument (Julia ArgumentError)        */
+#define HOE_ERR_DIM         -2   /* inconsistent sizes (Julia DimensionMismatch)  */
+#define HOE_ERR_OOM         -3   /* device allocation failed (OutOfMemoryError)   */
+#define HOE_ERR_CUDA        -4   /* CUDA runtime error                            */
+#define HOE_ERR_TIMEOUT     -5   /* a bounded device wait ran out                 */
+#define HOE_ERR_CLOSED      -6   /* handle was closed (Julia ArgumentError)       */
+#define HOE_ERR_UNSUPPORTED -7   /* mode not available on this device/build       */
+
+/* contraction engines (hoe_desc.engine, hoe_set_engine) */
+#define HOE_ENGINE_FP32_SIMT  0  /* plain FP32 CUDA-core direct kernel              */
+#define HOE_ENGINE_TC_BF16X3  1  /* tcgen05 tensor cores, split-BF16 3-product, FP32 accumulate */
+
+/* hoe_backward flags */
+#define HOE_GRAD_KSPHA     1     /* write dL/dkspha                                   */
+#define HOE_GRAD_FIELDMAP  2     /* write dL/dfieldmap                                */
+#define HOE_GRAD_T0_B0     4     /* dL/dt0 includes the fieldmap part  -fieldmap[v]   */
+#define HOE_GRAD_T0_COEF   8     /* dL/dt0 includes the coefficient part -bf.kspha_dt */
+
+typedef struct hoe_handle hoe_handle;
+
+typedef struct hoe_desc {
+    int32_t abi_version;      /* = HOE_ABI_VERSION                                     */
+    int32_t nX, nY, nZ;       /* grid matrix size                                      */
+    int32_t nSam;             /* samples                                               */
+    int32_t nCha;             /* coils                                                 */
+    int32_t nTerm;            /* spherical-harmonic terms: 9 or 16                     */
+    int32_t has_concomitant;  /* 1: bf/kspha carry 4 appended concomitant terms        */
+    int32_t nVox;             /* masked voxels (count(mask)) > 0                        */
+    int32_t engine;           /* HOE_ENGINE_*                                          */
+    int32_t device;           /* CUDA device ordinal; -1 = current device              */
+    int32_t tile_samples;     /* 0 = default (128); autotuner override                 */
+    int32_t tile_voxels;      /* 0 = default (128); autotuner override                 */
+    int32_t split_hint;       /* 0 = automatic split-K                                 */
+    const int32_t *mask_idx;  /* host [nVox], 0-based linear grid indices, ascending   */
+    const double  *bf;        /* host [nVox x nTermEff], nTermEff = nTerm + 4*has_conc */
+    const double  *kspha;     /* host [nTermEff x nSam], prepared (prep_kspha applied) */
+    const double  *times;     /* host [nSam] seconds                                   */
+    const double  *fieldmap;  /* host [nVox] Hz, masked; NULL = zeros                  */
+    const double  *csm;       /* host complex [nVox x nCha], masked; NULL = ones (nCha must be 1) */
+    const double  *kspha_dt;  /* host [nTerm x nSam] or NULL: dkspha/dt (derivative & t0 gradient) */
+} hoe_desc;
+
+typedef struct hoe_timings {
+    float   forward_kernel_ms;     /* main contraction kernel of the last forward   */
+    float   adjoint_kernel_ms;     /* main contraction kernel of the last adjoint   */
+    float   forward_total_ms;      /* whole last forward (prologue..epilogue)       */
+    float   adjoint_total_ms;      /* whole last adjoint                            */
+    int64_t launches;              /* kernels launched by this handle so far        */
+} hoe_timings;
+
+typedef struct hoe_info {
+    int32_t nSam, nCha, nVox, nTermEff, nFull;
+    int32_t engine;
+    int32_t tile_samples, tile_voxels;
+    int32_t n_sample_tiles, n_voxel_tiles;
+    int32_t split_forward, split_adjoint;
+    double  residual_phase_bound;  /* max |sum_l dbeta*kappa| in cycles over all tiles */
+    int64_t device_bytes;          /* device memory owned by the handle */
+} hoe_info;
+
+/* Library */
+HOE_API const char *hoe_version(void);
+HOE_API int  hoe_abi_version(void);
+
+/* Handle lifetime */
+HOE_API int  hoe_create(hoe_handle **out, const hoe_desc *desc);
+HOE_API int  hoe_close(hoe_handle *h);     /* idempotent; later calls return HOE_ERR_CLOSED */
+HOE_API void hoe_free(hoe_handle *h);      /* closes if needed and frees the host object   */
+HOE_API int  hoe_is_closed(const hoe_handle *h);
+HOE_API const char *hoe_last_error(const hoe_handle *h);
+HOE_API int  hoe_get_info(const hoe_handle *h, hoe_info *out);
+HOE_API int  hoe_set_engine(hoe_handle *h, int32_t engine);
+/* Tracing: with timing enabled, CUDA events are recorded on the call's stream
+ * around each forward/adjoint and its main kernel; hoe_get_timings waits for
+ * the last recorded events and reports their durations and the launch count. */
+HOE_API int  hoe_set_timing(hoe_handle *h, int32_t enable);
+HOE_API int  hoe_get_timings(hoe_handle *h, hoe_timings *out);
+
+/* Operator applications (complex64 device vectors) */
+HOE_API int  hoe_forward(hoe_handle *h, const void *x_dev, void *y_dev, void *stream);
+HOE_API int  hoe_adjoint(hoe_handle *h, const void *y_dev, void *x_dev, void *stream);
+/* D_dev: float [nSam*nCha] real >= 0 (W^H W, samples fastest) or NULL for ones.
+ * Weight validation (finite, non-negative, real) is done by the host caller,
+ * as in normalOperator; the device diagonal is used as given. */
+HOE_API int  hoe_normal(hoe_handle *h, const float *D_dev, const void *x_dev, void *out_dev, void *stream);
+/* B x of the kspha_dt mode: requires desc.kspha_dt. */
+HOE_API int  hoe_derivative(hoe_handle *h, const void *x_dev, void *y_dev, void *stream);
+/* Gradient of L = 0.5*||E x - y||^2 given the residual r = E x - y.
+ *   dk_dev   float [nTermEff x nSam] (same layout as kspha) or NULL
+ *   ddf_dev  float [prod(matrixSize)], zero outside the mask, or NULL
+ *   dt0_dev  double [1] or NULL
+ * flags: HOE_GRAD_* bits. */
+HOE_API int  hoe_backward(hoe_handle *h, const void *x_dev, const void *r_dev,
+                  float *dk_dev, float *ddf_dev, double *dt0_dev,
+                  int32_t flags, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HOEXPLICIT_H */

@@ -1,0 +1,85 @@
+"""The C-ABI library loads and exports every symbol include/hoexplicit.h
+declares; argument validation that happens before any CUDA call."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from hoexplicit import _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "hoexplicit.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"HOE_API[^;(]*?\b(hoe_\w+)\s*\(", text)))
+
+
+def test_header_declares_expected_entry_points():
+    syms = declared_symbols()
+    assert set(_lib.EXPORTED) == set(syms), syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(str(_lib.LIB_PATH))
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_version_and_abi():
+    lib = _lib.load()
+    assert lib.hoe_abi_version() == _lib.HOE_ABI_VERSION
+    assert b"sm_103a" in lib.hoe_version()
+
+
+def test_struct_layouts_match_header():
+    # two int32 blocks followed by pointers / doubles, natural alignment
+    assert ctypes.sizeof(_lib.HoeDesc) == 14 * 4 + 7 * 8
+    assert ctypes.sizeof(_lib.HoeInfo) == 12 * 4 + 8 + 8
+
+
+def _desc(**over):
+    d = _lib.HoeDesc()
+    d.abi_version = _lib.HOE_ABI_VERSION
+    d.nX, d.nY, d.nZ, d.nSam, d.nCha, d.nTerm, d.nVox = 2, 2, 1, 3, 1, 9, 4
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+@pytest.mark.parametrize("over,code", [
+    (dict(abi_version=99), _lib.HOE_ERR_ARG),
+    (dict(nTerm=10), _lib.HOE_ERR_ARG),
+    (dict(nVox=0), _lib.HOE_ERR_ARG),
+    (dict(nSam=0), _lib.HOE_ERR_ARG),
+    (dict(nX=0), _lib.HOE_ERR_DIM),
+    (dict(nVox=5), _lib.HOE_ERR_DIM),
+    (dict(engine=7), _lib.HOE_ERR_ARG),
+])
+def test_create_rejects_bad_descriptors_before_any_device_call(over, code):
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    d = _desc(**over)
+    assert lib.hoe_create(ctypes.byref(h), ctypes.byref(d)) == code
+    assert not h.value
+    assert lib.hoe_last_error(None)
+
+
+def test_null_arguments():
+    lib = _lib.load()
+    assert lib.hoe_create(None, None) == _lib.HOE_ERR_ARG
+    h = ctypes.c_void_p()
+    assert lib.hoe_create(ctypes.byref(h), None) == _lib.HOE_ERR_ARG
+    assert lib.hoe_forward(None, None, None, None) == _lib.HOE_ERR_ARG
+    assert lib.hoe_is_closed(None) == 1
+    lib.hoe_free(None)  # no-op
+
+
+def test_error_mapping():
+    with pytest.raises(_lib.ArgumentError):
+        _lib.check(_lib.HOE_ERR_CLOSED)
+    with pytest.raises(_lib.DimensionMismatch):
+        _lib.check(_lib.HOE_ERR_DIM)
+    with pytest.raises(_lib.OutOfMemoryError):
+        _lib.check(_lib.HOE_ERR_OOM)

@@ -1,0 +1,301 @@
+"""GPU parity of libhoexplicit.so against the FP64 oracle (through the C ABI).
+
+Mirrors the reference's explicit-operator tests (test/test_HighOrderExplicit.jl,
+test/test_explicit_gpu.jl, test/test_explicit_interface.jl,
+test/test_Concomitant.jl) on the committed golden fixtures and on seeded
+problems at sizes that are not multiples of the tiles.
+
+Tolerances (relative L2 vs FP64): 1e-5 for the plain FP32 engine, 1e-4 for
+the tensor-core engine.
+"""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from hoexplicit import (ArgumentError, Grid, HighOrderExplicitOp, OutOfMemoryError, WeightingOp,  # noqa: E402
+                        compose, explicit_gpu_normal, normalOperator, workloads)
+from hoexplicit.operator import ENGINES  # noqa: E402
+from oracle import dense, oracle  # noqa: E402
+from tests.golden_util import load, model_from_golden  # noqa: E402
+
+TOL = {"fp32": 1e-5, "tc": 1e-4}
+
+
+def engines():
+    out = ["fp32"]
+    try:
+        import hoexplicit._lib as L
+        L.load()
+        out.append("tc")
+    except Exception:
+        pass
+    return out
+
+
+def have_tc():
+    g = load("zero_phase")
+    try:
+        op = op_from_golden(g, "tc")
+        op.close()
+        return True
+    except Exception:
+        return False
+
+
+ENGINE_PARAMS = [pytest.param("fp32", id="fp32"), pytest.param("tc", id="tc")]
+
+
+def maybe_skip(engine):
+    if engine == "tc" and not have_tc():
+        pytest.skip("tensor-core engine not available in this build")
+
+
+def op_from_golden(g, engine, **kw):
+    nx, ny, nz = (int(v) for v in g["shape"])
+    dx, dy, dz = (float(v) for v in g["spacing"])
+    grid = Grid(nx, ny, nz, dx, dy, dz, x=g["x"], y=g["y"], z=g["z"])
+    sh = (nx, ny, nz)
+    nc = g["csm"].shape[1]
+    extra = {}
+    if "concomitant" in g:
+        extra["concomitant"] = g["concomitant"]
+    return HighOrderExplicitOp(grid, g["kspha"], g["times"],
+                               fieldmap=g["fieldmap"].reshape(sh, order="F"),
+                               csm=g["csm"].reshape(sh + (nc,), order="F"),
+                               mask=g["mask"].reshape(sh, order="F"), engine=engine, **extra, **kw)
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex64)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy().astype(np.complex128)
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_zero_phase_known_answer(engine):
+    maybe_skip(engine)
+    # test/test_explicit_gpu.jl:109-113 and test/test_explicit_multi_gpu.jl:72-77
+    g = load("zero_phase")
+    op = op_from_golden(g, engine)
+    y = host(op * dev(np.ones(4)))
+    assert np.allclose(y, 2.0, rtol=1e-6, atol=1e-6)
+    n = host(normalOperator(op) * dev(np.ones(4)))
+    assert np.allclose(n, 3.0, rtol=1e-6, atol=1e-6)
+    op.close()
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_fixture_highorder(engine):
+    maybe_skip(engine)
+    # test/test_HighOrderExplicit.jl:94-128
+    g = load("fixture_highorder")
+    op = op_from_golden(g, engine)
+    tol = TOL[engine]
+    y = host(op * dev(g["image"]))
+    xa = host(op.H * dev(g["probe"]))
+    assert dense.rel(y, g["forward"]) < tol
+    assert dense.rel(xa, g["adjoint"]) < tol
+    assert np.all(xa[~g["mask"]] == 0)
+    lhs, rhs = np.vdot(g["probe"], y), np.vdot(xa, g["image"])
+    assert abs(lhs - rhs) / (np.linalg.norm(y) * np.linalg.norm(g["probe"])) < tol
+    op.close()
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+@pytest.mark.parametrize("case", range(4))
+def test_reference_gpu_cases(engine, case):
+    maybe_skip(engine)
+    # test/test_explicit_gpu.jl:37-96 (forward, adjoint, weighted normal, RHS,
+    # adjoint identity, mask zeros, linearity, zero input, non-negativity,
+    # repeatability, invalid weights, close semantics)
+    g = load(f"gpu_case_{case}")
+    tol = TOL[engine]
+    op = op_from_golden(g, engine)
+    x, y, w = dev(g["image"]), dev(g["probe"]), g["weights"]
+    nc = g["csm"].shape[1]
+    fwd, bwd = host(op * x), host(op.H * y)
+    assert dense.rel(fwd, g["forward"]) < tol
+    assert dense.rel(bwd, g["adjoint"]) < tol
+    assert abs(np.vdot(g["probe"], fwd) - np.vdot(bwd, g["image"])) / max(
+        np.linalg.norm(fwd) * np.linalg.norm(g["probe"]), 1) < tol
+    assert np.all(bwd[~g["mask"]] == 0)
+    W = WeightingOp(w, nc)
+    normal = normalOperator(compose(W, op))
+    res = host(normal * x)
+    assert dense.rel(res, g["normal"]) < tol
+    assert dense.rel(host(explicit_gpu_normal(op, w) * x), g["normal"]) < tol
+    D = np.tile(np.abs(w) ** 2, nc)
+    assert dense.rel(host(normalOperator(op, D) * x), g["normal"]) < tol
+    rhs = host(op.H * dev(np.tile(np.abs(w) ** 2, nc) * g["probe"]))
+    assert dense.rel(rhs, g["rhs"]) < tol
+    assert np.real(np.vdot(g["image"], res)) >= 0
+    assert dense.rel(host(normal * (2 * x)), 2 * res) < 2 * tol
+    assert np.linalg.norm(host(normal * torch.zeros_like(x))) == 0
+    assert np.array_equal(host(normal * x), res)  # deterministic reductions
+    with pytest.raises(ArgumentError):
+        normalOperator(op, np.full(len(w), 1 + 1j))
+    with pytest.raises(ArgumentError):
+        normalOperator(op, np.full(len(w), -1.0))
+    op.close()
+    op.close()
+    with pytest.raises(ArgumentError):
+        normalOperator(op)
+    with pytest.raises(ArgumentError):
+        normal * x
+    with pytest.raises(ArgumentError):
+        op * x
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_concomitant_fixture(engine):
+    maybe_skip(engine)
+    # test/test_Concomitant.jl:93-107
+    g = load("concomitant")
+    op = op_from_golden(g, engine)
+    tol = TOL[engine]
+    assert dense.rel(host(op * dev(g["image"])), g["forward"]) < tol
+    assert dense.rel(host(op.H * dev(g["probe"])), g["adjoint"]) < tol
+
+
+def test_recon_terms_nominal_substitution():
+    # test/test_explicit_interface.jl:24-30: "0011" with k_nominal equals the
+    # operator built from the effective coefficients
+    g = load("gpu_case_1")
+    rng = np.random.default_rng(731)
+    kn = rng.standard_normal((3, g["kspha"].shape[1]))
+    eff = dict(g)
+    eff["kspha"] = g["kspha"].copy()
+    eff["kspha"][0] = 0
+    eff["kspha"][1:4] = kn
+    a = op_from_golden(g, "fp32", recon_terms="0011", k_nominal=kn)
+    b = op_from_golden(eff, "fp32")
+    x = dev(g["image"])
+    assert np.array_equal(host(a * x), host(b * x))
+
+
+SMALL = [
+    dict(shape=(9, 7, 1), nSam=300, nCha=3, nTerm=16),
+    dict(shape=(5, 6, 4), nSam=129, nCha=5, nTerm=9),
+    dict(shape=(13, 11, 1), nSam=257, nCha=16, nTerm=16, conc=True),
+    dict(shape=(17, 9, 2), nSam=200, nCha=1, nTerm=9),
+    dict(shape=(12, 12, 1), nSam=131, nCha=33, nTerm=16),
+    dict(shape=(16, 16, 1), nSam=640, nCha=8, nTerm=16, masked=False),
+]
+
+
+def run_small(engine, params, seed=11):
+    w = workloads.small(seed=seed, **params)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine=engine, **w.op_kwargs())
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    mask = np.zeros(w.x.size, dtype=bool)
+    mask[idx] = True
+    rng = np.random.default_rng(seed + 1)
+    y0 = rng.standard_normal(w.nSam * w.nCha) + 1j * rng.standard_normal(w.nSam * w.nCha)
+    return op, m, mask, w, y0
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+@pytest.mark.parametrize("params", SMALL, ids=lambda p: "x".join(map(str, p["shape"])) + f"-{p['nSam']}s-{p['nCha']}c")
+def test_small_problems_vs_oracle(engine, params):
+    maybe_skip(engine)
+    op, m, mask, w, y0 = run_small(engine, params)
+    tol = TOL[engine]
+    x = w.x.copy()
+    x[~mask] = 0
+    yo = oracle.forward(m, w.x[mask])
+    xo = oracle.scatter(oracle.adjoint(m, y0), mask)
+    yg = host(op * dev(w.x))
+    xg = host(op.H * dev(y0))
+    assert dense.rel(yg, yo) < tol
+    assert dense.rel(xg, xo) < tol
+    assert np.all(xg[~mask] == 0)
+    no = oracle.scatter(oracle.adjoint(m, oracle.forward(m, w.x[mask])), mask)
+    assert dense.rel(host(normalOperator(op) * dev(w.x)), no) < tol
+    op.close()
+
+
+def test_config1_full_size_vs_oracle():
+    w = workloads.config1()
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c)
+    yo = oracle.forward(m, w.x[idx])
+    yg = host(op * dev(w.x))
+    assert dense.rel(yg, yo) < 1e-5
+    rng = np.random.default_rng(5)
+    y = yo + 0.01 * np.linalg.norm(yo) / np.sqrt(yo.size) * (rng.standard_normal(yo.size) + 1j * rng.standard_normal(yo.size))
+    xo = oracle.adjoint(m, y)
+    xg = host(op.H * dev(y))
+    assert dense.rel(xg[idx], xo) < 1e-5
+    info = op.info()
+    assert info["residual_phase_bound"] < 16.0  # worst-case bound of the FP32 residual phase (cycles)
+
+
+def test_derivative_mode_vs_oracle():
+    # array_operator.jl:153-166 / 187-235: kspha_dt switches prod to B x
+    w = workloads.small(seed=3, shape=(11, 10, 1), nSam=260, nCha=4, nTerm=16, conc=True)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kspha_dt=w.kspha_dt, engine="fp32", **w.op_kwargs())
+    bf, k, t, f, c, idx = workloads.prepared_model(w, derivative=True)
+    m = oracle.Model(bf, k, t, f, c)
+    bo = oracle.derivative(m, w.kspha_dt, w.x[idx])
+    bg = host(op * dev(w.x))
+    assert dense.rel(bg, bo) < 1e-5
+
+
+def test_backward_vs_oracle_and_fd():
+    w = workloads.small(seed=4, shape=(10, 9, 1), nSam=300, nCha=4, nTerm=16)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=w.kspha_dt, engine="fp32", **w.op_kwargs())
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c)
+    rng = np.random.default_rng(9)
+    y = oracle.forward(m, w.x[idx]) * 0.9 + 0.05 * (rng.standard_normal(w.nSam * w.nCha) + 1j * rng.standard_normal(w.nSam * w.nCha))
+    r = oracle.forward(m, w.x[idx]) - y
+    dk_o, ddf_o, t0b, t0c = oracle.backward(m, w.x[idx], r, w.kspha_dt)
+    dk, ddf, dt0 = op.backward(dev(w.x), dev(r), t0_coef=True)
+    dk = dk.cpu().numpy().astype(np.float64)
+    ddf = ddf.cpu().numpy().astype(np.float64)
+    assert dense.rel(dk, dk_o) < 1e-4
+    assert dense.rel(ddf[idx], ddf_o) < 1e-4
+    assert np.all(ddf[np.setdiff1d(np.arange(ddf.size), idx)] == 0)
+    assert abs(dt0.item() - (t0b + t0c)) <= 1e-4 * abs(t0b + t0c)
+
+
+def test_failure_injection_cleans_up():
+    # host-side fault injection: the 3rd device allocation of create fails
+    g = load("gpu_case_0")
+    os.environ["HOE_INJECT_ALLOC_FAIL"] = "3"
+    try:
+        with pytest.raises(OutOfMemoryError):
+            op_from_golden(g, "fp32")
+    finally:
+        del os.environ["HOE_INJECT_ALLOC_FAIL"]
+    op = op_from_golden(g, "fp32")  # the next construction succeeds
+    assert dense.rel(host(op * dev(g["image"])), g["forward"]) < 1e-5
+    op.close()
+
+
+def test_host_round_trip_numpy():
+    g = load("gpu_case_2")
+    op = op_from_golden(g, "fp32")
+    y = op * g["image"].astype(np.complex64)
+    assert isinstance(y, np.ndarray)
+    assert dense.rel(y, g["forward"]) < 1e-5
+
+
+def test_timing_trace():
+    w = workloads.small(seed=2, shape=(16, 16, 1), nSam=512, nCha=8)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    op.set_timing(True)
+    y = op * dev(w.x)
+    op.H * y
+    t = op.timings()
+    assert t["forward_kernel_ms"] > 0 and t["adjoint_kernel_ms"] > 0
+    assert t["forward_total_ms"] >= t["forward_kernel_ms"]
+    assert t["launches"] >= 6

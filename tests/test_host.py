@@ -1,0 +1,93 @@
+"""Host-side logic of the product package (no GPU): grid, basis, order
+selection, concomitant terms, normal-weight validation, workloads."""
+import numpy as np
+import pytest
+
+from hoexplicit import ArgumentError, DimensionMismatch, Grid, basisfunc_spha, prep_concomitant, prep_kspha
+from hoexplicit.operator import WeightingOp, normal_diagonal
+from hoexplicit import workloads
+from oracle import dense, oracle
+
+
+def test_grid_matches_oracle_and_roundtrips():
+    g = Grid(5, 4, 3, 0.7, 0.9, 1.2)
+    x, y, z = oracle.grid(5, 4, 3, 0.7, 0.9, 1.2)
+    assert np.allclose(g.x, x) and np.allclose(g.y, y) and np.allclose(g.z, z)
+    g2 = Grid.from_dict(g.struct_to_dict())
+    assert g2.matrixSize == g.matrixSize and np.array_equal(g2.x, g.x)
+
+
+def test_basis_matches_oracle():
+    rng = np.random.default_rng(1)
+    x, y, z = rng.standard_normal((3, 40))
+    assert np.allclose(basisfunc_spha(x, y, z, list(range(1, 17))),
+                       oracle.basis(x, y, z, list(range(1, 17))), rtol=1e-14, atol=1e-14)
+    assert np.allclose(basisfunc_spha(x, y, z, [4, 2]), oracle.basis(x, y, z, [4, 2]))
+    with pytest.raises(ArgumentError):
+        basisfunc_spha(x, y, z, [37])
+
+
+def test_prep_kspha_flags_and_copy():
+    # prep_kspha.jl:1-56 and test/test_explicit_interface.jl:24-30 ("0011" + k_nominal)
+    rng = np.random.default_rng(2)
+    k = rng.standard_normal((16, 13))
+    kn = rng.standard_normal((3, 13))
+    kc = k.copy()
+    e = prep_kspha(k, kn, 16, "0011")
+    assert np.array_equal(k, kc)  # never mutates its input
+    assert np.all(e[0] == 0) and np.array_equal(e[1:4], kn) and np.array_equal(e[4:], k[4:])
+    e = prep_kspha(k, kn, 16, "1100")
+    assert np.all(e[4:] == 0) and np.array_equal(e[:4], k[:4])
+    e9 = prep_kspha(k[:9], kn, 9, None)
+    assert np.array_equal(e9, k[:9])
+    for bad in ("111", "11111", "11a1"):
+        with pytest.raises(ArgumentError):
+            prep_kspha(k, kn, 16, bad)
+    with pytest.raises(ArgumentError):
+        prep_kspha(k[:10], kn, 10, None)
+
+
+def test_prep_concomitant():
+    rng = np.random.default_rng(3)
+    x, y, z = rng.standard_normal((3, 7))
+    bf = rng.standard_normal((7, 16))
+    k = rng.standard_normal((16, 5))
+    c = rng.standard_normal((4, 5))
+    b2, k2 = prep_concomitant(bf, k, x, y, z, c)
+    assert b2.shape == (7, 20) and k2.shape == (20, 5)
+    assert np.allclose(b2[:, 16:], np.stack([z * z, x * x + y * y, x * z, y * z], 1))
+    assert prep_concomitant(bf, k, x, y, z, None)[0] is bf
+    with pytest.raises(DimensionMismatch):
+        prep_concomitant(bf, k, x, y, z, c[:3])
+    with pytest.raises(ArgumentError):
+        prep_concomitant(bf, k, x, y, z, c.astype(complex))
+
+
+def test_normal_weight_rules():
+    # explicit_gpu_operator.jl:402-412
+    ns, nc = 11, 3
+    D = normal_diagonal(None, ns, nc)
+    assert D.shape == (33,) and np.all(D == 1)
+    D = normal_diagonal(np.arange(ns, dtype=float), ns, nc)
+    assert D.shape == (33,) and np.array_equal(D[11:22], np.arange(ns))
+    w = np.arange(1, ns + 1) * (1 + 1j)
+    D = normal_diagonal(WeightingOp(w, nc), ns, nc)
+    assert np.allclose(D, np.tile(2 * np.arange(1, ns + 1) ** 2, nc))
+    with pytest.raises(ArgumentError):
+        normal_diagonal(np.full(ns, 1 + 1j), ns, nc)
+    with pytest.raises(ArgumentError):
+        normal_diagonal(np.full(ns, -1.0), ns, nc)
+    with pytest.raises(ArgumentError):
+        normal_diagonal(np.full(ns, np.nan), ns, nc)
+    with pytest.raises(DimensionMismatch):
+        normal_diagonal(np.ones(ns + 1), ns, nc)
+
+
+def test_workload_shapes():
+    w = workloads.config1()
+    assert w.kspha.shape == (16, 4096) and w.nCha == 8 and w.nVox == 64 * 64
+    assert abs(w.times[1] - 2e-6) < 1e-15
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    assert bf.shape == (4096, 16) and c.shape == (4096, 8)
+    w3 = workloads.config3()
+    assert w3.kspha.shape[1] == 12000 and w3.nCha == 16
