@@ -162,6 +162,10 @@ int finish(hoe_handle *h, cudaError_t e, const char *what) {
 
 }  // namespace
 
+namespace hoe {
+void record_error(const char *msg) { g_err = msg; }
+}  // namespace hoe
+
 extern "C" {
 
 const char *hoe_version(void) { return HOE_VERSION_STRING; }

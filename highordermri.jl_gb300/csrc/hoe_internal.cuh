@@ -100,6 +100,9 @@ cudaError_t prep_Yt(const hoe_handle *h, const float2 *y, const float *D, cudaSt
 cudaError_t simt_backward(const hoe_handle *h, const float2 *x, const float2 *r,
                           float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
 
+// Sets the thread's handle-less error message (hoe_last_error(NULL)).
+void record_error(const char *msg);
+
 // Records trace event i on stream st when tracing is enabled.
 inline void trace(const hoe_handle *h, int i, cudaStream_t st) {
   if (h->timing && h->ev[i]) cudaEventRecord(h->ev[i], st);

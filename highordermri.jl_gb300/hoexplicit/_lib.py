@@ -34,6 +34,7 @@ EXPORTED = (
     "hoe_version", "hoe_abi_version", "hoe_create", "hoe_close", "hoe_free", "hoe_is_closed",
     "hoe_last_error", "hoe_get_info", "hoe_set_engine", "hoe_forward", "hoe_adjoint",
     "hoe_normal", "hoe_derivative", "hoe_backward", "hoe_set_timing", "hoe_get_timings",
+    "hoe_forward_noalloc",
 )
 
 
@@ -69,6 +70,15 @@ class HoeDesc(ctypes.Structure):
         ("fieldmap", ctypes.POINTER(ctypes.c_double)),
         ("csm", ctypes.POINTER(ctypes.c_double)),
         ("kspha_dt", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+class HoeRawModel(ctypes.Structure):
+    _fields_ = [
+        ("nVox", ctypes.c_int32), ("nSam", ctypes.c_int32), ("nCha", ctypes.c_int32),
+        ("nTermEff", ctypes.c_int32),
+        ("mask_idx", ctypes.c_void_p), ("bf", ctypes.c_void_p), ("kspha", ctypes.c_void_p),
+        ("times", ctypes.c_void_p), ("fieldmap", ctypes.c_void_p), ("csm", ctypes.c_void_p),
     ]
 
 
@@ -124,6 +134,7 @@ def load():
     lib.hoe_backward.argtypes = [H, vp, vp, vp, vp, vp, ctypes.c_int32, vp]
     lib.hoe_set_timing.argtypes = [H, ctypes.c_int32]
     lib.hoe_get_timings.argtypes = [H, ctypes.POINTER(HoeTimings)]
+    lib.hoe_forward_noalloc.argtypes = [ctypes.POINTER(HoeRawModel), vp, vp, vp]
     for name in EXPORTED:
         if name not in ("hoe_free",):
             getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int

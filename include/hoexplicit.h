@@ -163,6 +163,56 @@ HOE_API int  hoe_backward(hoe_handle *h, const void *x_dev, const void *r_dev,
                   float *dk_dev, float *ddf_dev, double *dt0_dev,
                   int32_t flags, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free forward.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory: code where cudaMalloc is
+ * forbidden or unavailable, such as a reconstruction pipeline that
+ * pre-allocates everything up front, or a host framework that owns every
+ * device byte through its own pool.  Those callers cannot use hoe_create,
+ * which allocates.  hoe_forward_noalloc computes y = E x (same result
+ * convention and the plain FP32 arithmetic of hoe_forward) from a model
+ * the caller already holds in device memory, and allocates nothing: no
+ * cudaMalloc, no cudaFree, no allocating library call.
+ *
+ * Its scratch, the split-K partial sums, is one static device array of
+ * 2^21 complex64 values (16 MiB).  It exists on every GPU where this
+ * library's device code is loaded and stays there until the process exits.
+ * Sizes are limited by it: ceil(nSam/128)*128 * nChaPad must not exceed
+ * 2^21, where nChaPad is nCha rounded up to 4, 8 or a multiple of 16 (for
+ * example nSam*nCha <= 2,097,152 when nCha is a multiple of 16).  Larger
+ * problems are rejected with HOE_ERR_DIM and a message in
+ * hoe_last_error(NULL).  nTermEff is at most 20.
+ *
+ * The first call on a device, with that device current, looks up the
+ * scratch's device address (cudaGetSymbolAddress) and sets the kernels'
+ * shared-memory limit.  Make that first call before any stream capture.
+ * All calls share the one scratch array, and each call overwrites every
+ * slot it reads, so nothing has to be cleared between calls.  Calls whose
+ * work overlaps on the GPU (other streams, other threads) race on the
+ * scratch: serialise them.
+ *
+ * Arrays (device, caller-owned, reference layout):
+ *   mask_idx int32 [nVox]                  0-based linear grid indices of the mask
+ *   bf       float64 [nVox x nTermEff]     element (v,l) at v + l*nVox
+ *   kspha    float64 [nTermEff x nSam]     element (l,s) at l + s*nTermEff
+ *   times    float64 [nSam]
+ *   fieldmap float64 [nVox] or NULL
+ *   csm      complex64 [nVox x nCha]       element (v,c) at v + c*nVox
+ *   x        complex64 [nFull], y complex64 [nSam*nCha] (samples fastest)
+ * ------------------------------------------------------------------------- */
+typedef struct hoe_raw_model {
+    int32_t nVox, nSam, nCha, nTermEff;
+    const int32_t *mask_idx;
+    const double  *bf;
+    const double  *kspha;
+    const double  *times;
+    const double  *fieldmap;
+    const void    *csm;
+} hoe_raw_model;
+
+HOE_API int  hoe_forward_noalloc(const hoe_raw_model *m, const void *x_dev, void *y_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
