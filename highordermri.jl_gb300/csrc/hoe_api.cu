@@ -518,6 +518,25 @@ int hoe_get_timings(hoe_handle *h, hoe_timings *o) {
   return HOE_OK;
 }
 
+int hoe_check(hoe_handle *h, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  DeviceGuard guard(h->device);
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(h, e, "hoe_check");
+  int *word = hoe::tc_error_word(h);
+  if (word) {
+    int v = 0;
+    e = cudaMemcpy(&v, word, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(h, e, "hoe_check");
+    if (v != 0) {
+      cudaMemset(word, 0, sizeof(int));
+      return fail(h, HOE_ERR_TIMEOUT, "a bounded device wait ran out (tensor-core pipeline)");
+    }
+  }
+  return HOE_OK;
+}
+
 int hoe_forward(hoe_handle *h, const void *x, void *y, void *stream) {
   int rc = check_usable(h);
   if (rc) return rc;

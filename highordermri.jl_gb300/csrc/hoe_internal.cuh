@@ -87,6 +87,7 @@ struct hoe_handle {
   hoe::Tables t;
   hoe::Scratch s;
   hoe::TcState tc;
+  void *tc_host = nullptr;   // tensor-core buffer table (hoe_tc.cu)
 };
 
 namespace hoe {
@@ -97,6 +98,13 @@ cudaError_t simt_forward(const hoe_handle *h, const float2 *x, float2 *y,
 cudaError_t simt_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
 cudaError_t prep_Z(const hoe_handle *h, const float2 *x, cudaStream_t st);
 cudaError_t prep_Yt(const hoe_handle *h, const float2 *y, const float *D, cudaStream_t st);
+// Split-K reductions shared by both engines: sum `splits` partial slices of
+// `part` and write y (FWD_TO_Y / FWD_DERIV_TO_Y) or the weighted Yt, resp. the
+// coil-combined, scaled, scattered image.
+cudaError_t simt_reduce_forward(const hoe_handle *h, const float2 *part, int splits, float2 *y,
+                                const float *D, int mode, cudaStream_t st);
+cudaError_t simt_reduce_adjoint(const hoe_handle *h, const float2 *part, int splits, float2 *x,
+                                cudaStream_t st);
 cudaError_t simt_backward(const hoe_handle *h, const float2 *x, const float2 *r,
                           float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
 
@@ -119,5 +127,6 @@ cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y,
                        const float *D, int mode, cudaStream_t st);
 cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
 bool tc_supported(const hoe_handle *h, std::string *why);
+int *tc_error_word(const hoe_handle *h);   // device word set by a timed-out wait
 
 }  // namespace hoe

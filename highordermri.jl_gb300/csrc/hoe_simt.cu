@@ -521,15 +521,22 @@ cudaError_t simt_forward(const hoe_handle *h, const float2 *, float2 *y, const f
     deriv ? dispatch_fwd_rp<16, true>(h, nCC, st) : dispatch_fwd_rp<16, false>(h, nCC, st);
   }
   trace(h, EV_FK1, st);
-  h->launches += 2;
+  h->launches += 1;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  return simt_reduce_forward(h, h->s.part, h->splitF, y, D, mode, st);
+}
+
+cudaError_t simt_reduce_forward(const hoe_handle *h, const float2 *part, int splits, float2 *y,
+                                const float *D, int mode, cudaStream_t st) {
+  const auto &t = h->t;
   int64_t n = (int64_t)t.nSamPad * t.nChaPad;
   float scale = (float)(1.0 / sqrt((double)t.nVox));
   bool toY = (mode == FWD_TO_Y || mode == FWD_DERIV_TO_Y);
-  k_fwd_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.part, h->splitF, t.nSamPad, t.nChaPad,
+  k_fwd_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, splits, t.nSamPad, t.nChaPad,
                                                           t.nSam, t.nCha, scale, D,
                                                           toY ? y : nullptr, toY ? nullptr : h->s.Yt);
+  h->launches += 1;
   return cudaGetLastError();
 }
 
@@ -540,14 +547,21 @@ cudaError_t simt_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st
   else if (t.nChaPad == 8) dispatch_adj_rp<8>(h, 1, st);
   else dispatch_adj_rp<16>(h, t.nChaPad / 16, st);
   trace(h, EV_AK1, st);
-  h->launches += 2;
+  h->launches += 1;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(x, 0, (size_t)t.nFull * sizeof(float2), st);
+  return simt_reduce_adjoint(h, h->s.part, h->splitA, x, st);
+}
+
+cudaError_t simt_reduce_adjoint(const hoe_handle *h, const float2 *part, int splits, float2 *x,
+                                cudaStream_t st) {
+  const auto &t = h->t;
+  cudaError_t e = cudaMemsetAsync(x, 0, (size_t)t.nFull * sizeof(float2), st);
   if (e != cudaSuccess) return e;
   float scale = (float)(1.0 / sqrt((double)t.nVox));
-  k_adj_reduce<<<(t.nVoxPad + 255) / 256, 256, 0, st>>>(h->s.part, h->splitA, t.nVoxPad, t.nChaPad,
-                                                       t.nCha, t.csm, t.perm, scale, x);
+  k_adj_reduce<<<(t.nVoxPad + 255) / 256, 256, 0, st>>>(part, splits, t.nVoxPad, t.nChaPad, t.nCha,
+                                                       t.csm, t.perm, scale, x);
+  h->launches += 1;
   return cudaGetLastError();
 }
 

@@ -1,20 +1,622 @@
-// Tensor-core engine (tcgen05).  Placeholder until the UMMA kernels land:
-// reports itself unavailable so that hoe_create/hoe_set_engine fail loudly.
+// Tensor-core engine: the complex contraction on tcgen05 (UMMA) with
+// split-BF16 operands (3 products: hi*hi + hi*lo + lo*hi) accumulated in
+// FP32 in tensor memory.
+//
+// Both directions are the same real GEMM shape, D[M=128 rows, N=2*nChaTC] +=
+// A[rows, K] * B[K, N], with re/im interleaved along K and along N:
+//   forward  rows = samples, columns = voxels:
+//            A[s,2v+0] = Re P[s,v], A[s,2v+1] = Im P[s,v]
+//            B[2v+0,2c] = Re Z, B[2v+0,2c+1] = Im Z, B[2v+1,2c] = -Im Z, B[2v+1,2c+1] = Re Z
+//            so D[s,2c..2c+1] = (Re, Im) of sum_v P[s,v] Z[v,c]
+//   adjoint  rows = voxels, columns = samples:
+//            A[v,2s+0] = Re P[s,v], A[v,2s+1] = Im P[s,v]
+//            B[2s+0,2c] = Re Y, B[2s+0,2c+1] = Im Y, B[2s+1,2c] = Im Y, B[2s+1,2c+1] = -Re Y
+//            so D[v,2c..2c+1] = (Re, Im) of sum_s conj(P[s,v]) Y[s,c]
+//
+// The A operand (the phase tile) never touches global memory: 8 "phase"
+// warps form it in registers with the anchored FP32 phase of the plain
+// engine (identical arithmetic, see hoe_internal.cuh), split it into BF16
+// hi/lo and store it in shared memory in the no-swizzle K-major canonical
+// layout.  A loader warp streams the pre-tiled B operand and the per-stage
+// phase inputs with cp.async.bulk (TMA bulk copies) onto mbarriers; one
+// thread of the MMA warp issues tcgen05.mma and commits stage completion
+// back to the producers.  Every mbarrier wait is bounded in time: on
+// timeout the kernel records HOE_ERR_TIMEOUT in a device word, stops
+// issuing work, waits (bounded) for its own copies and MMAs and frees TMEM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+
 #include "hoe_internal.cuh"
 
 namespace hoe {
+namespace {
 
-bool tc_supported(const hoe_handle *, std::string *why) {
-  if (why) *why = "tensor-core kernels not built";
-  return false;
+constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel tile)
+constexpr int TV = 32;              // complex columns per pipeline stage
+constexpr int TK = 2 * TV;          // real K per stage (64 BF16 = 4 UMMA k-steps)
+constexpr int PHASE_WARPS = 8;      // two per TMEM lane quarter, half the stage's columns each
+constexpr int MMA_WARP = PHASE_WARPS;
+constexpr int LOAD_WARP = PHASE_WARPS + 1;
+constexpr int THREADS = (PHASE_WARPS + 2) * 32;
+constexpr float kTwoPi = 6.28318530717958647692f;
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
+
+constexpr int A_TILE_BYTES = TM * TK * 2;    // one BF16 A tile (hi or lo): 16 KB
+
+// byte offset of element (r, k) in a no-swizzle K-major tile with K = TK:
+// core matrices of 8 rows x 16 B; cores adjacent in K are 128 B apart (LBO),
+// 8-row groups are (TK/8)*128 B apart (SBO)
+__host__ __device__ constexpr uint32_t kmajor_off(int r, int k) {
+  return (uint32_t)((r / 8) * (TK / 8) * 128 + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2);
 }
-cudaError_t tc_prepare(hoe_handle *) { return cudaErrorNotSupported; }
-void tc_release(hoe_handle *h) { h->tc = TcState(); }
-cudaError_t tc_forward(const hoe_handle *, const float2 *, float2 *, const float *, int, cudaStream_t) {
-  return cudaErrorNotSupported;
+constexpr uint32_t LBO = 128;
+constexpr uint32_t SBO = (TK / 8) * 128;
+
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  // D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12), K-major, N>>3 at 17, M>>4 at 24
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
-cudaError_t tc_adjoint_from_Yt(const hoe_handle *, float2 *, cudaStream_t) {
-  return cudaErrorNotSupported;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(LBO >> 4) << 16) |
+         ((uint64_t)(SBO >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false on timeout or when another role aborted.
+__device__ __noinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                      int *gerr) {
+  uint64_t t0 = 0;
+  for (uint32_t n = 0;; ++n) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if ((n & 255) == 255) {
+      uint64_t t = globaltimer();
+      if (t0 == 0) t0 = t;
+      else if (t - t0 > kWaitNs) {
+        *abort = 1;
+        atomicExch(gerr, HOE_ERR_TIMEOUT);
+        return false;
+      }
+    }
+  }
+}
+
+// Bounded wait that ignores the abort flag (used to drain in-flight work).
+__device__ __noinline__ bool drain_bar(uint64_t *bar, uint32_t parity) {
+  uint64_t t0 = globaltimer();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer() - t0 > kWaitNs) return false;
+  return true;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                     uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x (low half) = lo_elem
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+struct TcParams {
+  const float *rowvec;     // [nRowPad][RP]: kappa (forward) / dbeta (adjoint)
+  const float *rowAnchor;  // [colTile][rowAnchorStride]: Atab (forward) / Btab (adjoint)
+  const float *colvec;     // [nColPad][RP]: dbeta (forward) / kappa (adjoint)
+  const float *colAnchor;  // [rowTile][colAnchorStride]: Btab (forward) / Atab (adjoint)
+  const uint16_t *Bop;     // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
+  float2 *part;            // [split][nRowPad][nChaPad] partial sums
+  int *err;
+  int rowAnchorStride, colAnchorStride;
+  int nRowPad, nChaPad, nChaTC;
+  int nColChunks, chunksPerSplit;
+};
+
+// Shared-memory plan (dynamic, 1024-byte aligned base):
+//   A    [NS][2][A_TILE_BYTES]        phase tile hi / lo
+//   B    [NS][2][N*TK*2]              B operand hi / lo
+//   CV   [NS][TV][RP] float           column phase vectors
+//   CA   [NS][TV] float               column anchors
+//   bars full[NS], afull[NS], empty[NS], done; tmem base; abort flag
+template <int N, int RP, int NS>
+struct Smem {
+  static constexpr int B_TILE = N * TK * 2;
+  static constexpr size_t A_OFF = 0;
+  static constexpr size_t B_OFF = A_OFF + (size_t)NS * 2 * A_TILE_BYTES;
+  static constexpr size_t CV_OFF = B_OFF + (size_t)NS * 2 * B_TILE;
+  static constexpr size_t CA_OFF = CV_OFF + (size_t)NS * TV * RP * 4;
+  static constexpr size_t BAR_OFF = (CA_OFF + (size_t)NS * TV * 4 + 7) / 8 * 8;
+  static constexpr size_t MISC_OFF = BAR_OFF + (size_t)(3 * NS + 1) * 8;
+  static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
+};
+
+template <int N, int RP, int NS>
+__global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
+  using S = Smem<N, RP, NS>;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char *sA = smem + S::A_OFF;
+  unsigned char *sB = smem + S::B_OFF;
+  float *sCV = reinterpret_cast<float *>(smem + S::CV_OFF);
+  float *sCA = reinterpret_cast<float *>(smem + S::CA_OFF);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
+  uint64_t *afull = full + NS;
+  uint64_t *empty = afull + NS;
+  uint64_t *done = empty + NS;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::MISC_OFF);
+  volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
+  constexpr uint32_t TMEM_COLS = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int rowTile = blockIdx.x, split = blockIdx.y;
+  const int ch0 = split * p.chunksPerSplit;
+  const int ch1 = min(p.nColChunks, ch0 + p.chunksPerSplit);
+  const int nIter = max(0, ch1 - ch0);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NS; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&afull[i], PHASE_WARPS);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(done, 1);
+    *abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == MMA_WARP) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < PHASE_WARPS) {
+    // ---------------- phase generator: rows x (half of the stage's columns)
+    const int row = (warp & 3) * 32 + lane;
+    const int half = warp >> 2;
+    const int grow = rowTile * TM + row;
+    float rv[RP];
+#pragma unroll
+    for (int l = 0; l < RP; l += 4) {
+      float4 v = *reinterpret_cast<const float4 *>(p.rowvec + (int64_t)grow * RP + l);
+      rv[l] = v.x; rv[l + 1] = v.y; rv[l + 2] = v.z; rv[l + 3] = v.w;
+    }
+    int curTile = -1;
+    float a = 0.f;
+    bool ok = true;
+    for (int it = 0; it < nIter && ok; ++it) {
+      const int slot = it % NS, round = it / NS;
+      const int col0 = (ch0 + it) * TV;
+      const int colTile = col0 / 128;
+      if (colTile != curTile) {
+        a = p.rowAnchor[(int64_t)colTile * p.rowAnchorStride + grow];
+        curTile = colTile;
+      }
+      if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) { ok = false; break; }
+      if (!wait_bar(&full[slot], round & 1, abort, p.err)) { ok = false; break; }
+      const float *cv = sCV + slot * TV * RP;
+      const float *ca = sCA + slot * TV;
+      unsigned char *aHi = sA + (size_t)slot * 2 * A_TILE_BYTES;
+      unsigned char *aLo = aHi + A_TILE_BYTES;
+#pragma unroll 1
+      for (int cc = 0; cc < 4; ++cc) {
+        const int v0 = half * 16 + cc * 4;
+        float ph[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ph[j] = a + ca[v0 + j];
+#pragma unroll
+        for (int q = 0; q < RP / 4; ++q) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            float4 d = reinterpret_cast<const float4 *>(cv + (v0 + j) * RP)[q];
+            ph[j] = fmaf(rv[4 * q], d.x, ph[j]);
+            ph[j] = fmaf(rv[4 * q + 1], d.y, ph[j]);
+            ph[j] = fmaf(rv[4 * q + 2], d.z, ph[j]);
+            ph[j] = fmaf(rv[4 * q + 3], d.w, ph[j]);
+          }
+        }
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float f = ph[j] - rintf(ph[j]);
+          float sn, cs;
+          __sincosf(kTwoPi * f, &sn, &cs);
+          __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
+          float2 hf = __bfloat1622float2(h);
+          hi[j] = *reinterpret_cast<uint32_t *>(&h);
+          lo[j] = pack_bf16(cs - hf.x, sn - hf.y);
+        }
+        const uint32_t off = kmajor_off(row, 2 * v0);
+        *reinterpret_cast<uint4 *>(aHi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4 *>(aLo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&afull[slot]);
+    }
+    // ---------------- epilogue: warps 0-3 read their TMEM lane quarter
+    if (warp < 4) {
+      float2 *dst = p.part + ((int64_t)split * p.nRowPad + grow) * p.nChaPad;
+      const int nOut = min(p.nChaTC, p.nChaPad);
+      if (nIter == 0) {
+        for (int c = 0; c < nOut; ++c) dst[c] = make_float2(0.f, 0.f);
+      } else {
+        bool got = ok && wait_bar(done, 0, abort, p.err);
+        tc_fence_after();
+        if (got) {
+#pragma unroll 1
+          for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) {
+              int c = (c0 + i) / 2;
+              if (c < nOut) dst[c] = make_float2(v[i], v[i + 1]);
+            }
+          }
+        }
+      }
+    }
+  } else if (warp == MMA_WARP) {
+    // ---------------- MMA issuer (one thread)
+    if (lane == 0 && nIter > 0) {
+      constexpr uint32_t idesc = idesc_bf16(TM, N);
+      int issued = 0;
+      for (int it = 0; it < nIter; ++it) {
+        const int slot = it % NS, round = it / NS;
+        if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
+        if (!wait_bar(&afull[slot], round & 1, abort, p.err)) break;
+        tc_fence_after();
+        const uint32_t aHi = smem_u32(sA + (size_t)slot * 2 * A_TILE_BYTES);
+        const uint32_t aLo = aHi + A_TILE_BYTES;
+        const uint32_t bHi = smem_u32(sB + (size_t)slot * 2 * S::B_TILE);
+        const uint32_t bLo = bHi + S::B_TILE;
+#pragma unroll
+        for (int ks = 0; ks < TK / 16; ++ks) {
+          const uint32_t ko = ks * 2 * LBO;  // 16 BF16 = two core matrices along K
+          umma(tmem, umma_desc(aHi + ko), umma_desc(bHi + ko), idesc, (it | ks) ? 1u : 0u);
+          umma(tmem, umma_desc(aHi + ko), umma_desc(bLo + ko), idesc, 1u);
+          umma(tmem, umma_desc(aLo + ko), umma_desc(bHi + ko), idesc, 1u);
+        }
+        umma_commit(&empty[slot]);
+        issued = it + 1;
+      }
+      if (issued == nIter) {
+        umma_commit(done);
+      } else if (issued > 0) {
+        // aborted: let the MMAs already issued finish before TMEM is freed
+        const int last = issued - 1;
+        drain_bar(&empty[last % NS], (last / NS) & 1);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ---------------- loader (one thread): B tiles + column phase inputs
+    if (lane == 0) {
+      const uint32_t bBytes = 2 * S::B_TILE, cvBytes = TV * RP * 4, caBytes = TV * 4;
+      int issued = 0;
+      for (int it = 0; it < nIter; ++it) {
+        const int slot = it % NS, round = it / NS;
+        if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
+        const int ch = ch0 + it;
+        const int col0 = ch * TV;
+        mbar_expect_tx(&full[slot], bBytes + cvBytes + caBytes);
+        bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, p.Bop + (size_t)ch * 2 * (N * TK), bBytes, &full[slot]);
+        bulk_g2s(sCV + slot * TV * RP, p.colvec + (size_t)col0 * RP, cvBytes, &full[slot]);
+        bulk_g2s(sCA + slot * TV, p.colAnchor + (int64_t)rowTile * p.colAnchorStride + col0, caBytes,
+                 &full[slot]);
+        issued = it + 1;
+      }
+      if (*abort) {
+        // drain the copies still in flight into this CTA's shared memory
+        for (int it = max(0, issued - NS); it < issued; ++it)
+          drain_bar(&full[it % NS], (it / NS) & 1);
+      }
+    }
+    __syncwarp();
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == MMA_WARP) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+  }
+}
+
+// B operand of the forward: chunk i covers voxels [i*TV, (i+1)*TV); element
+// (n, k) with k = 2*v_local + r and n = 2*c + q.
+__global__ void k_tc_bop_forward(const float2 *__restrict__ Z, uint16_t *__restrict__ Bop,
+                                 int nChunks, int N, int nChaPad) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t per = (int64_t)N * TK;
+  if (i >= (int64_t)nChunks * per) return;
+  int ch = (int)(i / per), e = (int)(i % per);
+  int n = e / TK, k = e % TK;
+  int v = ch * TV + k / 2, r = k & 1, c = n / 2, q = n & 1;
+  float2 z = c < nChaPad ? Z[(int64_t)v * nChaPad + c] : make_float2(0.f, 0.f);
+  float val = r == 0 ? (q == 0 ? z.x : z.y) : (q == 0 ? -z.y : z.x);
+  __nv_bfloat16 h = __float2bfloat16_rn(val);
+  __nv_bfloat16 l = __float2bfloat16_rn(val - __bfloat162float(h));
+  uint16_t *tile = Bop + (size_t)ch * 2 * per;
+  uint32_t o = kmajor_off(n, k) / 2;
+  tile[o] = *reinterpret_cast<uint16_t *>(&h);
+  tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+}
+
+// B operand of the adjoint from Yt [nSamPad][nChaPad]: chunk i covers
+// samples [i*TV, (i+1)*TV).
+__global__ void k_tc_bop_adjoint(const float2 *__restrict__ Yt, uint16_t *__restrict__ Bop,
+                                 int nChunks, int N, int nChaPad) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t per = (int64_t)N * TK;
+  if (i >= (int64_t)nChunks * per) return;
+  int ch = (int)(i / per), e = (int)(i % per);
+  int n = e / TK, k = e % TK;
+  int s = ch * TV + k / 2, r = k & 1, c = n / 2, q = n & 1;
+  float2 y = c < nChaPad ? Yt[(int64_t)s * nChaPad + c] : make_float2(0.f, 0.f);
+  float val = r == 0 ? (q == 0 ? y.x : y.y) : (q == 0 ? y.y : -y.x);
+  __nv_bfloat16 h = __float2bfloat16_rn(val);
+  __nv_bfloat16 l = __float2bfloat16_rn(val - __bfloat162float(h));
+  uint16_t *tile = Bop + (size_t)ch * 2 * per;
+  uint32_t o = kmajor_off(n, k) / 2;
+  tile[o] = *reinterpret_cast<uint16_t *>(&h);
+  tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+}
+
+int tc_ncha(int nCha) { return std::max(8, (nCha + 7) / 8 * 8); }
+
+template <int N, int RP>
+cudaError_t launch_contract(const hoe_handle *h, const TcParams &p, int gridX, int gridY, cudaStream_t st) {
+  constexpr int NS = N <= 64 ? 4 : 3;
+  using S = Smem<N, RP, NS>;
+  static_assert(S::BYTES <= 227 * 1024, "shared memory plan exceeds 227 KB");
+  auto kern = k_tc_contract<N, RP, NS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES);
+  if (e != cudaSuccess) return e;
+  kern<<<dim3(gridX, gridY), THREADS, S::BYTES, st>>>(p);
+  h->launches += 1;
+  return cudaGetLastError();
+}
+
+template <int RP>
+cudaError_t dispatch_n(const hoe_handle *h, const TcParams &p, int N, int gx, int gy, cudaStream_t st) {
+  switch (N) {
+    case 16: return launch_contract<16, RP>(h, p, gx, gy, st);
+    case 32: return launch_contract<32, RP>(h, p, gx, gy, st);
+    case 48: return launch_contract<48, RP>(h, p, gx, gy, st);
+    case 64: return launch_contract<64, RP>(h, p, gx, gy, st);
+    case 80: return launch_contract<80, RP>(h, p, gx, gy, st);
+    case 96: return launch_contract<96, RP>(h, p, gx, gy, st);
+    case 112: return launch_contract<112, RP>(h, p, gx, gy, st);
+    case 128: return launch_contract<128, RP>(h, p, gx, gy, st);
+    default: return cudaErrorNotSupported;
+  }
+}
+
+cudaError_t dispatch(const hoe_handle *h, const TcParams &p, int N, int gx, int gy, cudaStream_t st) {
+  switch (h->t.Rp) {
+    case 12: return dispatch_n<12>(h, p, N, gx, gy, st);
+    case 16: return dispatch_n<16>(h, p, N, gx, gy, st);
+    case 20: return dispatch_n<20>(h, p, N, gx, gy, st);
+    default: return dispatch_n<24>(h, p, N, gx, gy, st);
+  }
+}
+
+// split-K so that the grid covers the SMs in whole waves as far as possible
+int choose_split(int rowTiles, int chunks, int numSMs) {
+  int best = 1;
+  double bestCost = 1e300;
+  for (int s = 1; s <= std::min(chunks, 64); ++s) {
+    int cps = (chunks + s - 1) / s;
+    int sp = (chunks + cps - 1) / cps;
+    long ctas = (long)rowTiles * sp;
+    long waves = (ctas + numSMs - 1) / numSMs;
+    double cost = (double)waves * cps + 0.02 * sp * rowTiles / numSMs;  // wave time + reduce
+    if (cost < bestCost) { bestCost = cost; best = sp; }
+  }
+  return best;
+}
+
+struct TcBuffers {
+  uint16_t *bopF = nullptr, *bopA = nullptr;
+  float2 *part = nullptr;
+  int *err = nullptr;
+  int N = 0, nChaTC = 0, splitF = 1, splitA = 1;
+  size_t bopFElems = 0, bopAElems = 0, partElems = 0;
+};
+
+}  // namespace
+
+bool tc_supported(const hoe_handle *h, std::string *why) {
+  int dev = h->device, major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+  if (major != 10 || minor != 3) {
+    if (why) *why = "tcgen05 kernels are built for sm_103a (GB300) only";
+    return false;
+  }
+  if (tc_ncha(h->t.nCha) > 64) {
+    if (why) *why = "the tensor-core engine supports up to 64 coils";
+    return false;
+  }
+  return true;
+}
+
+cudaError_t tc_prepare(hoe_handle *h) {
+  if (h->tc.ready) return cudaSuccess;
+  const auto &t = h->t;
+  TcBuffers b;
+  b.nChaTC = tc_ncha(t.nCha);
+  b.N = 2 * b.nChaTC;
+  const int chunksF = t.nVoxPad / TV, chunksA = t.nSamPad / TV;
+  b.splitF = choose_split(t.nSt, chunksF, h->numSMs);
+  b.splitA = choose_split(t.nVt, chunksA, h->numSMs);
+  b.bopFElems = (size_t)chunksF * 2 * b.N * TK;
+  b.bopAElems = (size_t)chunksA * 2 * b.N * TK;
+  b.partElems = std::max((size_t)b.splitF * t.nSamPad, (size_t)b.splitA * t.nVoxPad) * t.nChaPad;
+  size_t bytes = b.bopFElems * 2 + 256 + b.bopAElems * 2 + 256 + b.partElems * sizeof(float2) + 256 + 256;
+  unsigned char *buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, bytes);
+  if (e != cudaSuccess) return e;
+  size_t off = 0;
+  auto take = [&](size_t n) { unsigned char *p = buf + off; off = (off + n + 255) / 256 * 256; return p; };
+  b.bopF = (uint16_t *)take(b.bopFElems * 2);
+  b.bopA = (uint16_t *)take(b.bopAElems * 2);
+  b.part = (float2 *)take(b.partElems * sizeof(float2));
+  b.err = (int *)take(sizeof(int));
+  e = cudaMemset(b.err, 0, sizeof(int));
+  if (e != cudaSuccess) { cudaFree(buf); return e; }
+  h->tc.buf = buf;
+  h->tc.bytes = bytes;
+  h->tc.ready = true;
+  h->tc_host = new TcBuffers(b);
+  return cudaSuccess;
+}
+
+void tc_release(hoe_handle *h) {
+  if (h->tc.buf) cudaFree(h->tc.buf);
+  delete (TcBuffers *)h->tc_host;
+  h->tc_host = nullptr;
+  h->tc = TcState();
+}
+
+static TcParams base_params(const hoe_handle *h, const TcBuffers &b) {
+  TcParams p{};
+  p.part = b.part;
+  p.err = b.err;
+  p.nChaPad = h->t.nChaPad;
+  p.nChaTC = b.nChaTC;
+  return p;
+}
+
+cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const float *D, int mode,
+                       cudaStream_t st) {
+  const auto &t = h->t;
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  const int chunks = t.nVoxPad / TV;
+  int64_t n = (int64_t)chunks * b.N * TK;
+  k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Z, b.bopF, chunks, b.N, t.nChaPad);
+  h->launches += 1;
+  TcParams p = base_params(h, b);
+  p.rowvec = t.kappa;
+  p.rowAnchor = t.Atab;
+  p.rowAnchorStride = t.nSamPad;
+  p.colvec = t.dbeta;
+  p.colAnchor = t.Btab;
+  p.colAnchorStride = t.nVoxPad;
+  p.Bop = b.bopF;
+  p.nRowPad = t.nSamPad;
+  p.nColChunks = chunks;
+  p.chunksPerSplit = (chunks + b.splitF - 1) / b.splitF;
+  const int splits = (chunks + p.chunksPerSplit - 1) / p.chunksPerSplit;
+  trace(h, EV_FK0, st);
+  cudaError_t e = dispatch(h, p, b.N, t.nSt, splits, st);
+  trace(h, EV_FK1, st);
+  if (e != cudaSuccess) return e;
+  return simt_reduce_forward(h, b.part, splits, y, D, mode, st);
+}
+
+cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) {
+  const auto &t = h->t;
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  const int chunks = t.nSamPad / TV;
+  int64_t n = (int64_t)chunks * b.N * TK;
+  k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Yt, b.bopA, chunks, b.N, t.nChaPad);
+  h->launches += 1;
+  TcParams p = base_params(h, b);
+  p.rowvec = t.dbeta;
+  p.rowAnchor = t.Btab;
+  p.rowAnchorStride = t.nVoxPad;
+  p.colvec = t.kappa;
+  p.colAnchor = t.Atab;
+  p.colAnchorStride = t.nSamPad;
+  p.Bop = b.bopA;
+  p.nRowPad = t.nVoxPad;
+  p.nColChunks = chunks;
+  p.chunksPerSplit = (chunks + b.splitA - 1) / b.splitA;
+  const int splits = (chunks + p.chunksPerSplit - 1) / p.chunksPerSplit;
+  trace(h, EV_AK0, st);
+  cudaError_t e = dispatch(h, p, b.N, t.nVt, splits, st);
+  trace(h, EV_AK1, st);
+  if (e != cudaSuccess) return e;
+  return simt_reduce_adjoint(h, b.part, splits, x, st);
+}
+
+int *tc_error_word(const hoe_handle *h) {
+  return h->tc_host ? ((const TcBuffers *)h->tc_host)->err : nullptr;
 }
 
 }  // namespace hoe

@@ -34,7 +34,7 @@ EXPORTED = (
     "hoe_version", "hoe_abi_version", "hoe_create", "hoe_close", "hoe_free", "hoe_is_closed",
     "hoe_last_error", "hoe_get_info", "hoe_set_engine", "hoe_forward", "hoe_adjoint",
     "hoe_normal", "hoe_derivative", "hoe_backward", "hoe_set_timing", "hoe_get_timings",
-    "hoe_forward_noalloc",
+    "hoe_forward_noalloc", "hoe_check",
 )
 
 
@@ -134,6 +134,7 @@ def load():
     lib.hoe_backward.argtypes = [H, vp, vp, vp, vp, vp, ctypes.c_int32, vp]
     lib.hoe_set_timing.argtypes = [H, ctypes.c_int32]
     lib.hoe_get_timings.argtypes = [H, ctypes.POINTER(HoeTimings)]
+    lib.hoe_check.argtypes = [H, vp]
     lib.hoe_forward_noalloc.argtypes = [ctypes.POINTER(HoeRawModel), vp, vp, vp]
     for name in EXPORTED:
         if name not in ("hoe_free",):

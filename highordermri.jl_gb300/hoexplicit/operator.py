@@ -224,6 +224,11 @@ class ExplicitGB300Op:
         _lib.check(_lib.load().hoe_get_timings(self._handle(), ctypes.byref(t)), self._h)
         return {name: getattr(t, name) for name, _ in t._fields_}
 
+    def check(self) -> None:
+        """Wait for the operator's stream and raise if a kernel reported a
+        bounded-wait timeout (hoe_check)."""
+        _lib.check(_lib.load().hoe_check(self._handle(), self._stream()), self._h)
+
     def set_engine(self, engine: str) -> None:
         if engine not in ENGINES:
             raise ArgumentError(f"unknown engine {engine!r}")

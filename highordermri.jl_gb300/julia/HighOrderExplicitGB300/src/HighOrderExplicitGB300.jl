@@ -1,0 +1,268 @@
+"""
+    HighOrderExplicitGB300
+
+Julia front end of libhoexplicit.so: the GB300 (sm_103a) explicit
+higher-order encoding operator as a third `HighOrderExplicitOp`
+implementation beside HighOrderMRI's `:array` and `:kernel`.
+
+`GB300ExplicitOp(grid, kspha, times; ...)` takes the constructor keywords of
+`HighOrderExplicitOp` (fieldmap, csm, mask, concomitant, recon_terms,
+k_nominal, kspha_dt, gpus).  Model preparation reuses HighOrderMRI's own
+`prep_kspha`, `basisfunc_spha` and `prep_concomitant`, so both packages see
+the same model.  Solver vectors are `CuVector{ComplexF32}` on the operator's
+device; calls are ordered on `CUDA.stream()`.
+"""
+module HighOrderExplicitGB300
+
+using CUDA
+using LinearAlgebra
+using LinearOperators
+using LinearOperatorCollection
+using ChainRulesCore
+import HighOrderMRI
+import HighOrderMRI: Grid, HighOrderExplicitOp, prep_kspha, basisfunc_spha, prep_concomitant
+
+export GB300ExplicitOp, explicit_backward, encode
+
+const libhoe = get(ENV, "HOE_LIBRARY",
+    normpath(joinpath(@__DIR__, "..", "..", "..", "libhoexplicit.so")))
+
+const HOE_ABI_VERSION = Int32(1)
+const HOE_ENGINE_FP32_SIMT = Int32(0)
+const HOE_ENGINE_TC_BF16X3 = Int32(1)
+const HOE_GRAD_KSPHA = Int32(1)
+const HOE_GRAD_FIELDMAP = Int32(2)
+const HOE_GRAD_T0_B0 = Int32(4)
+const HOE_GRAD_T0_COEF = Int32(8)
+
+# Field order and types match `hoe_desc` in include/hoexplicit.h.
+struct HoeDesc
+    abi_version::Int32
+    nX::Int32; nY::Int32; nZ::Int32
+    nSam::Int32; nCha::Int32; nTerm::Int32; has_concomitant::Int32; nVox::Int32
+    engine::Int32; device::Int32; tile_samples::Int32; tile_voxels::Int32; split_hint::Int32
+    mask_idx::Ptr{Int32}
+    bf::Ptr{Float64}
+    kspha::Ptr{Float64}
+    times::Ptr{Float64}
+    fieldmap::Ptr{Float64}
+    csm::Ptr{Float64}
+    kspha_dt::Ptr{Float64}
+end
+
+last_error(h) = unsafe_string(ccall((:hoe_last_error, libhoe), Cstring, (Ptr{Cvoid},), h))
+
+# Status codes -> the exception types the reference raises.
+function check(rc::Cint, h=C_NULL)
+    rc == 0 && return nothing
+    msg = last_error(h)
+    rc in (-1, -6, -7) && throw(ArgumentError(msg))
+    rc == -2 && throw(DimensionMismatch(msg))
+    rc == -3 && throw(OutOfMemoryError())
+    error("libhoexplicit: [$rc] $msg")
+end
+
+mutable struct GB300ExplicitOp{T,F,G} <: HighOrderExplicitOp{Complex{T}}
+    nrow::Int
+    ncol::Int
+    symmetric::Bool
+    hermitian::Bool
+    prod!::F
+    tprod!::Nothing
+    ctprod!::G
+    nprod::Int
+    ntprod::Int
+    nctprod::Int
+    Mv::CuVector{Complex{T}}
+    Mtu::CuVector{Complex{T}}
+    handle::Ptr{Cvoid}
+    device::CuDevice
+    nSam::Int
+    nCha::Int
+    nTermEff::Int
+    derivative::Bool
+end
+
+LinearOperators.storage_type(op::GB300ExplicitOp) = typeof(op.Mv)
+
+function activate(op::GB300ExplicitOp)
+    (op.handle == C_NULL || ccall((:hoe_is_closed, libhoe), Cint, (Ptr{Cvoid},), op.handle) != 0) &&
+        throw(ArgumentError("operator is closed"))
+    CUDA.device!(op.device)
+    return op.handle
+end
+
+stream_handle() = CUDA.stream().handle
+
+function forward!(op::GB300ExplicitOp, res, x)
+    h = activate(op)
+    rc = op.derivative ?
+        ccall((:hoe_derivative, libhoe), Cint, (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CUDA.CUstream),
+              h, x, res, stream_handle()) :
+        ccall((:hoe_forward, libhoe), Cint, (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CUDA.CUstream),
+              h, x, res, stream_handle())
+    check(rc, h)
+    return res
+end
+
+function adjoint!(op::GB300ExplicitOp, res, y)
+    h = activate(op)
+    check(ccall((:hoe_adjoint, libhoe), Cint, (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CUDA.CUstream),
+                h, y, res, stream_handle()), h)
+    return res
+end
+
+"""
+    GB300ExplicitOp(grid, kspha, times; fieldmap, csm, mask, concomitant=nothing,
+        recon_terms=nothing, k_nominal=kspha[2:4,:], kspha_dt=nothing, gpus=nothing,
+        engine=:tc)
+
+The `:gb300` implementation of `HighOrderExplicitOp` (see
+HighOrderExplicitOp.jl:44-51).  `engine=:tc` uses the tcgen05 tensor-core
+contraction (split-BF16, FP32 accumulation), `engine=:fp32` the plain FP32
+CUDA-core kernel.  With `kspha_dt` the forward product evaluates the
+derivative `B x` of the reference's kspha_dt mode and concomitant terms are
+ignored (array_operator.jl:139, 159-166).
+"""
+function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::AbstractVector{T};
+    fieldmap=zeros(T, grid.matrixSize...), csm=ones(Complex{T}, grid.matrixSize..., 1),
+    mask=trues(grid.matrixSize...), concomitant=nothing, recon_terms=nothing,
+    k_nominal=kspha[2:4, :], kspha_dt=nothing, gpus=nothing, engine::Symbol=:tc,
+) where {T<:AbstractFloat}
+    if gpus !== nothing
+        ids = Int.(collect(gpus))
+        length(ids) == 1 || throw(ArgumentError("the :gb300 operator uses exactly one GPU"))
+        0 <= only(ids) < length(collect(CUDA.devices())) || throw(ArgumentError("invalid visible GPU ID"))
+        CUDA.device!(only(ids))
+    end
+    engine in (:tc, :fp32) || throw(ArgumentError("engine must be :tc or :fp32"))
+    nTerm, nSam = size(kspha)
+    nTerm in (9, 16) || throw(ArgumentError("kspha requires 9 or 16 terms"))
+    length(times) == nSam || throw(DimensionMismatch("times and kspha"))
+    length(mask) == prod(grid.matrixSize) || throw(DimensionMismatch("mask and grid"))
+    length(fieldmap) == length(mask) || throw(DimensionMismatch("fieldmap and mask"))
+    nCha = size(csm, ndims(csm))
+    length(csm) == length(mask) * nCha || throw(DimensionMismatch("csm and grid"))
+    indices = findall(vec(mask))
+    nVox = length(indices)
+    nVox > 0 || throw(ArgumentError("mask must contain voxels"))
+    derivative = kspha_dt !== nothing
+    derivative && size(kspha_dt) != size(kspha) && throw(ArgumentError("kspha_dt must have same size as kspha"))
+
+    prepared = prep_kspha(kspha, k_nominal, nTerm; recon_terms)
+    bf = basisfunc_spha(grid.x[indices], grid.y[indices], grid.z[indices], collect(1:nTerm))
+    bf, prepared = prep_concomitant(bf, prepared, grid, vec(mask);
+                                    concomitant=derivative ? nothing : concomitant)
+    bf64 = Matrix{Float64}(bf)
+    k64 = Matrix{Float64}(prepared)
+    t64 = Vector{Float64}(times)
+    f64 = Vector{Float64}(vec(fieldmap)[indices])
+    c128 = Matrix{ComplexF64}(reshape(csm, :, nCha)[indices, :])
+    idx32 = Int32.(indices .- 1)
+    kd64 = derivative ? Matrix{Float64}(kspha_dt) : nothing
+    dev = CUDA.device()
+    handle = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve bf64 k64 t64 f64 c128 idx32 kd64 begin
+        desc = Ref(HoeDesc(HOE_ABI_VERSION, grid.nX, grid.nY, grid.nZ, nSam, nCha, nTerm,
+            Int32(size(k64, 1) != nTerm), nVox,
+            engine === :tc ? HOE_ENGINE_TC_BF16X3 : HOE_ENGINE_FP32_SIMT,
+            Int32(CUDA.deviceid(dev)), Int32(0), Int32(0), Int32(0),
+            pointer(idx32), pointer(bf64), pointer(k64), pointer(t64), pointer(f64),
+            Ptr{Float64}(pointer(c128)), kd64 === nothing ? Ptr{Float64}(C_NULL) : pointer(kd64)))
+        check(ccall((:hoe_create, libhoe), Cint, (Ref{Ptr{Cvoid}}, Ref{HoeDesc}), handle, desc))
+    end
+    op = nothing
+    prodf = (res, x) -> forward!(op, res, x)
+    ctprodf = (res, y) -> adjoint!(op, res, y)
+    op = GB300ExplicitOp{Float32,typeof(prodf),typeof(ctprodf)}(
+        nSam * nCha, prod(grid.matrixSize), false, false, prodf, nothing, ctprodf, 0, 0, 0,
+        CUDA.zeros(ComplexF32, 0), CUDA.zeros(ComplexF32, 0), handle[], dev, nSam, nCha,
+        size(k64, 1), derivative)
+    finalizer(o -> ccall((:hoe_free, libhoe), Cvoid, (Ptr{Cvoid},), o.handle), op)
+    return op
+end
+
+function Base.adjoint(op::GB300ExplicitOp{T}) where {T}
+    return LinearOperator{Complex{T}}(op.ncol, op.nrow, false, false,
+        op.ctprod!, nothing, op.prod!; S=CuVector{Complex{T}})
+end
+
+# normalOperator(op, D) with the validation of explicit_gpu_operator.jl:399-416:
+# D = W^H W (real, non-negative, finite), one entry per sample or per sample and coil.
+function LinearOperatorCollection.normalOperator(op::GB300ExplicitOp{T}, weights=nothing; kwargs...) where {T}
+    activate(op)
+    raw = weights isa LinearOperatorCollection.WeightingOp ? weights.weights : weights
+    D = raw === nothing ? ones(T, op.nSam * op.nCha) : vec(Array(raw))
+    length(D) == op.nSam && (D = repeat(D, op.nCha))
+    length(D) == op.nrow || throw(DimensionMismatch("normal weights"))
+    all(isfinite, D) || throw(ArgumentError("normal weights must be finite"))
+    maximum(abs, imag.(D)) <= 10eps(T) * max(one(T), maximum(abs, D)) ||
+        throw(ArgumentError("normal weights must already be real nonnegative WᴴW"))
+    minimum(real.(D)) >= zero(T) || throw(ArgumentError("normal weights must be nonnegative"))
+    diagonal = CuArray(Float32.(real.(D)))
+    normal = (out, x) -> begin
+        h = activate(op)
+        check(ccall((:hoe_normal, libhoe), Cint,
+                    (Ptr{Cvoid}, CuPtr{Float32}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CUDA.CUstream),
+                    h, diagonal, x, out, stream_handle()), h)
+        out
+    end
+    return LinearOperator{Complex{T}}(op.ncol, op.ncol, false, true, normal, nothing, normal;
+                                      S=CuVector{Complex{T}})
+end
+
+# W ∘ op from recon_HOOp: normalOperator receives W^H W from LinearOperatorCollection.
+HighOrderMRI.explicit_gpu_normal(op::GB300ExplicitOp; weights=nothing) =
+    LinearOperatorCollection.normalOperator(op, weights === nothing ? nothing : abs2.(weights))
+
+function Base.close(op::GB300ExplicitOp)
+    op.handle == C_NULL && return nothing
+    CUDA.device!(op.device)
+    ccall((:hoe_close, libhoe), Cint, (Ptr{Cvoid},), op.handle)
+    return nothing
+end
+
+"""
+    explicit_backward(op, x, r; kspha=true, fieldmap=true, t0_b0=true, t0_coef=false)
+
+Gradient of `0.5*norm(op*x - y)^2` given the residual `r = op*x - y`
+(`CuVector{ComplexF32}` each): returns `(dkspha::CuMatrix{Float32}
+(nTermEff, nSam), dfieldmap::CuVector{Float32} (full grid, zero outside the
+mask), dt0::Float64)`.  The same call is the pullback of `x -> op*x` for the
+phase parameters when `r` is the output cotangent.  `t0_coef` needs
+`kspha_dt` at construction.
+"""
+function explicit_backward(op::GB300ExplicitOp, x, r; kspha=true, fieldmap=true, t0_b0=true, t0_coef=false)
+    h = activate(op)
+    flags = Int32((kspha ? HOE_GRAD_KSPHA : 0) | (fieldmap ? HOE_GRAD_FIELDMAP : 0) |
+                  (t0_b0 ? HOE_GRAD_T0_B0 : 0) | (t0_coef ? HOE_GRAD_T0_COEF : 0))
+    dk = CUDA.zeros(Float32, op.nTermEff, op.nSam)
+    ddf = CUDA.zeros(Float32, op.ncol)
+    dt0 = CUDA.zeros(Float64, 1)
+    check(ccall((:hoe_backward, libhoe), Cint,
+                (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{Float32}, CuPtr{Float32},
+                 CuPtr{Float64}, Int32, CUDA.CUstream),
+                h, x, r, dk, ddf, dt0, flags, stream_handle()), h)
+    return dk, ddf, Array(dt0)[1]
+end
+
+"""
+    encode(op, x) = op * x
+
+Differentiable application: the `rrule` returns the cotangents of the phase
+model (kspha, fieldmap, t0) computed by the backward kernel, and `op' * ȳ`
+for `x`.
+"""
+encode(op::GB300ExplicitOp, x) = op * x
+
+function ChainRulesCore.rrule(::typeof(encode), op::GB300ExplicitOp, x)
+    y = op * x
+    function encode_pullback(ȳ)
+        ybar = CuArray{ComplexF32}(unthunk(ȳ))
+        dk, ddf, dt0 = explicit_backward(op, x, ybar)
+        return NoTangent(), Tangent{typeof(op)}(; kspha=dk, fieldmap=ddf, t0=dt0), op' * ybar
+    end
+    return y, encode_pullback
+end
+
+end # module

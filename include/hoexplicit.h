@@ -144,6 +144,10 @@ HOE_API int  hoe_set_engine(hoe_handle *h, int32_t engine);
  * the last recorded events and reports their durations and the launch count. */
 HOE_API int  hoe_set_timing(hoe_handle *h, int32_t enable);
 HOE_API int  hoe_get_timings(hoe_handle *h, hoe_timings *out);
+/* Waits for the stream and reports a device-side failure of an earlier call:
+ * HOE_ERR_TIMEOUT when a bounded wait inside a kernel ran out (the kernel
+ * then skipped its remaining work).  The word is cleared after reporting. */
+HOE_API int  hoe_check(hoe_handle *h, void *stream);
 
 /* Operator applications (complex64 device vectors) */
 HOE_API int  hoe_forward(hoe_handle *h, const void *x_dev, void *y_dev, void *stream);

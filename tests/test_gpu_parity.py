@@ -18,22 +18,10 @@ pytestmark = pytest.mark.gpu
 
 from hoexplicit import (ArgumentError, Grid, HighOrderExplicitOp, OutOfMemoryError, WeightingOp,  # noqa: E402
                         compose, explicit_gpu_normal, normalOperator, workloads)
-from hoexplicit.operator import ENGINES  # noqa: E402
 from oracle import dense, oracle  # noqa: E402
 from tests.golden_util import load, model_from_golden  # noqa: E402
 
 TOL = {"fp32": 1e-5, "tc": 1e-4}
-
-
-def engines():
-    out = ["fp32"]
-    try:
-        import hoexplicit._lib as L
-        L.load()
-        out.append("tc")
-    except Exception:
-        pass
-    return out
 
 
 def have_tc():
@@ -207,8 +195,6 @@ def test_small_problems_vs_oracle(engine, params):
     maybe_skip(engine)
     op, m, mask, w, y0 = run_small(engine, params)
     tol = TOL[engine]
-    x = w.x.copy()
-    x[~mask] = 0
     yo = oracle.forward(m, w.x[mask])
     xo = oracle.scatter(oracle.adjoint(m, y0), mask)
     yg = host(op * dev(w.x))
@@ -218,22 +204,27 @@ def test_small_problems_vs_oracle(engine, params):
     assert np.all(xg[~mask] == 0)
     no = oracle.scatter(oracle.adjoint(m, oracle.forward(m, w.x[mask])), mask)
     assert dense.rel(host(normalOperator(op) * dev(w.x)), no) < tol
+    op.check()
     op.close()
 
 
-def test_config1_full_size_vs_oracle():
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_config1_full_size_vs_oracle(engine):
+    maybe_skip(engine)
+    tol = TOL[engine]
     w = workloads.config1()
-    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine=engine, **w.op_kwargs())
     bf, k, t, f, c, idx = workloads.prepared_model(w)
     m = oracle.Model(bf, k, t, f, c)
     yo = oracle.forward(m, w.x[idx])
     yg = host(op * dev(w.x))
-    assert dense.rel(yg, yo) < 1e-5
+    assert dense.rel(yg, yo) < tol
     rng = np.random.default_rng(5)
     y = yo + 0.01 * np.linalg.norm(yo) / np.sqrt(yo.size) * (rng.standard_normal(yo.size) + 1j * rng.standard_normal(yo.size))
     xo = oracle.adjoint(m, y)
     xg = host(op.H * dev(y))
-    assert dense.rel(xg[idx], xo) < 1e-5
+    assert dense.rel(xg[idx], xo) < tol
+    op.check()  # no bounded device wait ran out
     info = op.info()
     assert info["residual_phase_bound"] < 16.0  # worst-case bound of the FP32 residual phase (cycles)
 
