@@ -284,7 +284,8 @@ def run_gb300(a):
            "config": {"workload": w.name, "nVox": w.nVox, "nSam": w.nSam, "nCha": w.nCha,
                       "nTermEff": info["nTermEff"], "engine": engine, "parallelism": f"replicas x{ws}",
                       "l2": "flushed between timed steps (256 MiB write)",
-                      "residual_phase_bound_cycles": info["residual_phase_bound"]},
+                      "residual_phase_bound_cycles": info["residual_phase_bound"],
+                      "residual_rank": info["residual_rank"]},
            "roofline": roofline, "clocks": clk.summary(),
            "gpu_launches": int(r["launches"]),
            "kernel_ms": {"forward": fk, "adjoint": ak}}

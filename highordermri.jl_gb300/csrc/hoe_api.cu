@@ -178,9 +178,21 @@ const char *hoe_last_error(const hoe_handle *h) {
 
 int hoe_is_closed(const hoe_handle *h) { return valid_handle(h) ? h->closed : 1; }
 
-int hoe_create(hoe_handle **out, const hoe_desc *d) {
-  if (!out) return fail(nullptr, HOE_ERR_ARG, "out must not be NULL");
-  *out = nullptr;
+}  // extern "C"
+
+namespace {
+
+// Host-side plan of an operator: tiling, anchors and the tables uploaded by
+// hoe_create.  Built without touching the device (also used by hoe_plan).
+struct Plan {
+  hoe::Tables t;                                   // sizes (device pointers unused)
+  std::vector<int> order, perm;
+  std::vector<double> beta64, gam64, betabar, gambar, kap64;
+  std::vector<float> dbeta, kappa, bfraw, kdot, times_f;
+  std::vector<float2> csm;
+};
+
+int make_plan(const hoe_desc *d, Plan &P) {
   if (!d) return fail(nullptr, HOE_ERR_ARG, "descriptor must not be NULL");
   if (d->abi_version != HOE_ABI_VERSION)
     return fail(nullptr, HOE_ERR_ARG, "descriptor ABI version %d, library %d", d->abi_version,
@@ -216,6 +228,283 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   if (d->tile_voxels != 0 && d->tile_voxels != hoe::kTileV)
     return fail(nullptr, HOE_ERR_ARG, "tile_voxels must be 0 or %d", hoe::kTileV);
 
+  auto &t = P.t;
+  t.nX = d->nX; t.nY = d->nY; t.nZ = d->nZ; t.nFull = (int)nFull;
+  t.nSam = d->nSam; t.nCha = d->nCha; t.nTerm = d->nTerm;
+  t.R0 = d->nTerm + 4 * d->has_concomitant;
+  t.R = t.R0 + 1;
+  t.nVox = d->nVox;
+  t.nSt = (t.nSam + t.ST - 1) / t.ST;
+  t.nVt = (t.nVox + t.VT - 1) / t.VT;
+  t.nSamPad = t.nSt * t.ST;
+  t.nVoxPad = t.nVt * t.VT;
+  t.nChaPad = t.nCha <= 4 ? 4 : (t.nCha <= 8 ? 8 : (t.nCha + 15) / 16 * 16);
+  t.hasKdot = d->kspha_dt != nullptr;
+  const int R = t.R, R0 = t.R0;
+  const int nVox = t.nVox, nSam = t.nSam;
+
+  // ---- voxel order: Morton order of grid indices, chunks of VT voxels ----
+  auto &order = P.order;
+  order.assign(nVox, 0);
+  {
+    std::vector<uint64_t> code(nVox);
+    for (int m = 0; m < nVox; ++m) {
+      int64_t lin = d->mask_idx[m];
+      uint64_t i = lin % t.nX, j = (lin / t.nX) % t.nY, k = lin / ((int64_t)t.nX * t.nY);
+      code[m] = (t.nZ == 1) ? (spread2(i) | (spread2(j) << 1))
+                            : (spread3(i) | (spread3(j) << 1) | (spread3(k) << 2));
+    }
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return code[a] < code[b]; });
+  }
+
+  // ---- beta / gamma in FP64, tile anchors (component midrange) ----
+  auto &beta64 = P.beta64, &gam64 = P.gam64;
+  auto &perm = P.perm;
+  beta64.assign((size_t)t.nVoxPad * R, 0.0);
+  gam64.assign((size_t)t.nSamPad * R, 0.0);
+  perm.assign(t.nVoxPad, -1);
+  for (int p = 0; p < nVox; ++p) {
+    int m = order[p];
+    perm[p] = d->mask_idx[m];
+    for (int l = 0; l < R0; ++l) beta64[(size_t)p * R + l] = d->bf[(size_t)m + (size_t)l * nVox];
+    beta64[(size_t)p * R + R0] = d->fieldmap ? d->fieldmap[m] : 0.0;
+  }
+  for (int s = 0; s < nSam; ++s) {
+    for (int l = 0; l < R0; ++l) gam64[(size_t)s * R + l] = d->kspha[(size_t)l + (size_t)s * R0];
+    gam64[(size_t)s * R + R0] = d->times[s];
+  }
+  for (size_t i = 0; i < beta64.size(); ++i)
+    if (!std::isfinite(beta64[i])) return fail(nullptr, HOE_ERR_ARG, "bf/fieldmap must be finite");
+  for (size_t i = 0; i < gam64.size(); ++i)
+    if (!std::isfinite(gam64[i])) return fail(nullptr, HOE_ERR_ARG, "kspha/times must be finite");
+
+  // ---- tile anchors ----
+  // voxel tiles: the basis of the voxel nearest the tile's bounding-box centre
+  // (grid index space) for the basis components, the midrange for the fieldmap
+  auto &betabar = P.betabar, &gambar = P.gambar;
+  betabar.assign((size_t)t.nVt * R, 0.0);
+  gambar.assign((size_t)t.nSt * R, 0.0);
+  for (int vt = 0; vt < t.nVt; ++vt) {
+    int p0 = vt * t.VT, p1 = std::min(nVox, p0 + t.VT);
+    int64_t lo[3] = {INT64_MAX, INT64_MAX, INT64_MAX}, hi[3] = {INT64_MIN, INT64_MIN, INT64_MIN};
+    auto ijk = [&](int p, int64_t *c) {
+      int64_t lin = perm[p];
+      c[0] = lin % t.nX; c[1] = (lin / t.nX) % t.nY; c[2] = lin / ((int64_t)t.nX * t.nY);
+    };
+    for (int p = p0; p < p1; ++p) {
+      int64_t c[3];
+      ijk(p, c);
+      for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], c[a]); hi[a] = std::max(hi[a], c[a]); }
+    }
+    int best = p0;
+    double bestd = INFINITY;
+    for (int p = p0; p < p1; ++p) {
+      int64_t c[3];
+      ijk(p, c);
+      double dd = 0;
+      for (int a = 0; a < 3; ++a) { double e = 2.0 * c[a] - (double)(lo[a] + hi[a]); dd += e * e; }
+      if (dd < bestd) { bestd = dd; best = p; }
+    }
+    for (int l = 0; l < R0; ++l) betabar[(size_t)vt * R + l] = beta64[(size_t)best * R + l];
+    double flo = INFINITY, fhi = -INFINITY;
+    for (int p = p0; p < p1; ++p) { double v = beta64[(size_t)p * R + R0]; flo = std::min(flo, v); fhi = std::max(fhi, v); }
+    betabar[(size_t)vt * R + R0] = 0.5 * (flo + fhi);
+  }
+  // sample tiles: component midrange
+  for (int st = 0; st < t.nSt; ++st) {
+    int s0 = st * t.ST, s1 = std::min(nSam, s0 + t.ST);
+    for (int l = 0; l < R; ++l) {
+      double lo = INFINITY, hi = -INFINITY;
+      for (int s = s0; s < s1; ++s) { double v = gam64[(size_t)s * R + l]; lo = std::min(lo, v); hi = std::max(hi, v); }
+      gambar[(size_t)st * R + l] = 0.5 * (lo + hi);
+    }
+  }
+
+  // ---- residual vectors in FP64, balanced per component ----
+  std::vector<double> db64((size_t)nVox * R);
+  auto &kap64 = P.kap64;
+  kap64.assign((size_t)t.nSamPad * R, 0.0);
+  for (int p = 0; p < nVox; ++p)
+    for (int l = 0; l < R; ++l)
+      db64[(size_t)p * R + l] = beta64[(size_t)p * R + l] - betabar[(size_t)(p / t.VT) * R + l];
+  for (int s = 0; s < nSam; ++s)
+    for (int l = 0; l < R; ++l)
+      kap64[(size_t)s * R + l] = gam64[(size_t)s * R + l] - gambar[(size_t)(s / t.ST) * R + l];
+  std::vector<double> bal(R, 1.0);
+  for (int l = 0; l < R; ++l) {
+    double a = 0, b = 0;
+    for (int p = 0; p < nVox; ++p) a = std::max(a, std::fabs(db64[(size_t)p * R + l]));
+    for (int s = 0; s < nSam; ++s) b = std::max(b, std::fabs(kap64[(size_t)s * R + l]));
+    if (a > 0 && b > 0) bal[l] = std::sqrt(b / a);
+  }
+  // ---- reduced basis: Householder QR of the balanced dbeta, Jacobi SVD of R ----
+  std::vector<double> Vr;  // [R][r] right singular vectors kept
+  int rank = 0;
+  {
+    std::vector<double> A((size_t)nVox * R);  // column-major nVox x R
+    for (int p = 0; p < nVox; ++p)
+      for (int l = 0; l < R; ++l) A[(size_t)p + (size_t)l * nVox] = db64[(size_t)p * R + l] * bal[l];
+    const int kmax = std::min(R, nVox);
+    std::vector<double> v(nVox);
+    for (int j = 0; j < kmax; ++j) {
+      double *cj = &A[(size_t)j * nVox];
+      double nrm = 0;
+      for (int i = j; i < nVox; ++i) nrm += cj[i] * cj[i];
+      nrm = std::sqrt(nrm);
+      if (nrm == 0) continue;
+      double alpha = cj[j] >= 0 ? -nrm : nrm;
+      double vn = 0;
+      for (int i = j; i < nVox; ++i) { v[i] = cj[i]; }
+      v[j] -= alpha;
+      for (int i = j; i < nVox; ++i) vn += v[i] * v[i];
+      if (vn == 0) continue;
+      for (int k = j + 1; k < R; ++k) {
+        double *ck = &A[(size_t)k * nVox];
+        double d = 0;
+        for (int i = j; i < nVox; ++i) d += v[i] * ck[i];
+        double tau = 2.0 * d / vn;
+        for (int i = j; i < nVox; ++i) ck[i] -= tau * v[i];
+      }
+      cj[j] = alpha;
+    }
+    std::vector<double> W((size_t)R * R, 0.0), V((size_t)R * R, 0.0);  // row-major R x R
+    for (int i = 0; i < kmax; ++i)
+      for (int k = i; k < R; ++k) W[(size_t)i * R + k] = A[(size_t)i + (size_t)k * nVox];
+    for (int i = 0; i < R; ++i) V[(size_t)i * R + i] = 1.0;
+    for (int sweep = 0; sweep < 80; ++sweep) {
+      double off = 0;
+      for (int pp = 0; pp < R - 1; ++pp)
+        for (int qq = pp + 1; qq < R; ++qq) {
+          double al = 0, be = 0, ga = 0;
+          for (int i = 0; i < R; ++i) {
+            double wp = W[(size_t)i * R + pp], wq = W[(size_t)i * R + qq];
+            al += wp * wp; be += wq * wq; ga += wp * wq;
+          }
+          if (ga == 0 || std::fabs(ga) <= 1e-15 * std::sqrt(al * be)) continue;
+          off = std::max(off, std::fabs(ga) / std::sqrt(al * be));
+          double zeta = (be - al) / (2 * ga);
+          double tt = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1 + zeta * zeta));
+          double c = 1 / std::sqrt(1 + tt * tt), sn = c * tt;
+          for (int i = 0; i < R; ++i) {
+            double wp = W[(size_t)i * R + pp], wq = W[(size_t)i * R + qq];
+            W[(size_t)i * R + pp] = c * wp - sn * wq;
+            W[(size_t)i * R + qq] = sn * wp + c * wq;
+            double vp = V[(size_t)i * R + pp], vq = V[(size_t)i * R + qq];
+            V[(size_t)i * R + pp] = c * vp - sn * vq;
+            V[(size_t)i * R + qq] = sn * vp + c * vq;
+          }
+        }
+      if (off < 1e-15) break;
+    }
+    std::vector<std::pair<double, int>> sig(R);
+    for (int k = 0; k < R; ++k) {
+      double n2 = 0;
+      for (int i = 0; i < R; ++i) n2 += W[(size_t)i * R + k] * W[(size_t)i * R + k];
+      sig[k] = {std::sqrt(n2), k};
+    }
+    std::sort(sig.begin(), sig.end(), [](auto a, auto b) { return a.first > b.first; });
+    double kmaxn = 0;
+    for (int s = 0; s < nSam; ++s) {
+      double n2 = 0;
+      for (int l = 0; l < R; ++l) { double e = kap64[(size_t)s * R + l] / bal[l]; n2 += e * e; }
+      kmaxn = std::max(kmaxn, std::sqrt(n2));
+    }
+    // keep every direction whose largest possible contribution exceeds 1e-9 cycles
+    std::vector<int> keep;
+    for (int k = 0; k < R; ++k)
+      if (sig[k].first * kmaxn >= 1e-9 || keep.empty()) keep.push_back(sig[k].second);
+    rank = (int)keep.size();
+    Vr.assign((size_t)R * rank, 0.0);
+    for (int l = 0; l < R; ++l)
+      for (int k = 0; k < rank; ++k) Vr[(size_t)l * rank + k] = V[(size_t)l * R + keep[k]];
+  }
+  t.rank = rank;
+  t.Rp = rank <= 8 ? 8 : (rank <= 12 ? 12 : (rank <= 16 ? 16 : 24));
+  const int Rp = t.Rp;
+
+  auto &dbeta = P.dbeta, &kappa = P.kappa;
+  dbeta.assign((size_t)t.nVoxPad * Rp, 0.f);
+  kappa.assign((size_t)t.nSamPad * Rp, 0.f);
+  std::vector<double> dbr((size_t)nVox * rank), kpr((size_t)nSam * rank);
+  for (int p = 0; p < nVox; ++p)
+    for (int k = 0; k < rank; ++k) {
+      double acc = 0;
+      for (int l = 0; l < R; ++l) acc += db64[(size_t)p * R + l] * bal[l] * Vr[(size_t)l * rank + k];
+      dbr[(size_t)p * rank + k] = acc;
+      dbeta[(size_t)p * Rp + k] = (float)acc;
+    }
+  for (int s = 0; s < nSam; ++s)
+    for (int k = 0; k < rank; ++k) {
+      double acc = 0;
+      for (int l = 0; l < R; ++l) acc += kap64[(size_t)s * R + l] / bal[l] * Vr[(size_t)l * rank + k];
+      kpr[(size_t)s * rank + k] = acc;
+      kappa[(size_t)s * Rp + k] = (float)acc;
+    }
+  // worst-case residual magnitude over tile pairs (reported)
+  {
+    std::vector<double> dmx((size_t)t.nVt * rank, 0.0), kmx((size_t)t.nSt * rank, 0.0);
+    for (int p = 0; p < nVox; ++p)
+      for (int k = 0; k < rank; ++k) {
+        double &m = dmx[(size_t)(p / t.VT) * rank + k];
+        m = std::max(m, std::fabs(dbr[(size_t)p * rank + k]));
+      }
+    for (int s = 0; s < nSam; ++s)
+      for (int k = 0; k < rank; ++k) {
+        double &m = kmx[(size_t)(s / t.ST) * rank + k];
+        m = std::max(m, std::fabs(kpr[(size_t)s * rank + k]));
+      }
+    double bound = 0.0;
+    for (int vt = 0; vt < t.nVt; ++vt)
+      for (int st = 0; st < t.nSt; ++st) {
+        double b = 0.0;
+        for (int k = 0; k < rank; ++k) b += dmx[(size_t)vt * rank + k] * kmx[(size_t)st * rank + k];
+        bound = std::max(bound, b);
+      }
+    t.residBound = bound;
+  }
+
+  auto &bfraw = P.bfraw, &kdot = P.kdot, &times_f = P.times_f;
+  bfraw.assign((size_t)t.nVoxPad * hoe::kRF, 0.f);
+  kdot.assign((size_t)t.nSamPad * hoe::kRF, 0.f);
+  times_f.assign(t.nSamPad, 0.f);
+  for (int p = 0; p < nVox; ++p)
+    for (int l = 0; l < R; ++l) bfraw[(size_t)p * hoe::kRF + l] = (float)beta64[(size_t)p * R + l];
+  for (int s = 0; s < nSam; ++s) {
+    if (d->kspha_dt)
+      for (int l = 0; l < t.nTerm; ++l)
+        kdot[(size_t)s * hoe::kRF + l] = (float)d->kspha_dt[(size_t)l + (size_t)s * t.nTerm];
+    times_f[s] = (float)d->times[s];
+  }
+  auto &csm = P.csm;
+  csm.assign((size_t)t.nVoxPad * t.nChaPad, make_float2(0.f, 0.f));
+  for (int p = 0; p < nVox; ++p) {
+    int m = order[p];
+    for (int c = 0; c < t.nCha; ++c) {
+      float2 v = make_float2(1.f, 0.f);
+      if (d->csm) {
+        size_t o = 2 * ((size_t)m + (size_t)c * nVox);
+        v = make_float2((float)d->csm[o], (float)d->csm[o + 1]);
+      }
+      csm[(size_t)p * t.nChaPad + c] = v;
+    }
+  }
+
+  return HOE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hoe_create(hoe_handle **out, const hoe_desc *d) {
+  if (!out) return fail(nullptr, HOE_ERR_ARG, "out must not be NULL");
+  *out = nullptr;
+  Plan P;
+  int prc = make_plan(d, P);
+  if (prc != HOE_OK) return prc;
+
   int ndev = 0;
   cudaError_t ce = cudaGetDeviceCount(&ndev);
   if (ce != cudaSuccess || ndev == 0) return fail(nullptr, HOE_ERR_CUDA, "no CUDA device");
@@ -234,117 +523,13 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   if (h->numSMs <= 0) h->numSMs = 148;
 
   auto &t = h->t;
-  t.nX = d->nX; t.nY = d->nY; t.nZ = d->nZ; t.nFull = (int)nFull;
-  t.nSam = d->nSam; t.nCha = d->nCha; t.nTerm = d->nTerm;
-  t.R0 = d->nTerm + 4 * d->has_concomitant;
-  t.R = t.R0 + 1;
-  t.Rp = (t.R + 3) / 4 * 4;
-  t.nVox = d->nVox;
-  t.nSt = (t.nSam + t.ST - 1) / t.ST;
-  t.nVt = (t.nVox + t.VT - 1) / t.VT;
-  t.nSamPad = t.nSt * t.ST;
-  t.nVoxPad = t.nVt * t.VT;
-  t.nChaPad = t.nCha <= 4 ? 4 : (t.nCha <= 8 ? 8 : (t.nCha + 15) / 16 * 16);
-  t.hasKdot = d->kspha_dt != nullptr;
-  const int R = t.R, R0 = t.R0, Rp = t.Rp;
-  const int nVox = t.nVox, nSam = t.nSam;
-
-  // ---- voxel order: Morton order of grid indices, chunks of VT voxels ----
-  std::vector<int> order(nVox);
-  {
-    std::vector<uint64_t> code(nVox);
-    for (int m = 0; m < nVox; ++m) {
-      int64_t lin = d->mask_idx[m];
-      uint64_t i = lin % t.nX, j = (lin / t.nX) % t.nY, k = lin / ((int64_t)t.nX * t.nY);
-      code[m] = (t.nZ == 1) ? (spread2(i) | (spread2(j) << 1))
-                            : (spread3(i) | (spread3(j) << 1) | (spread3(k) << 2));
-    }
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int a, int b) { return code[a] < code[b]; });
-  }
-
-  // ---- beta / gamma in FP64, tile anchors (component midrange) ----
-  std::vector<double> beta64((size_t)t.nVoxPad * R, 0.0), gam64((size_t)t.nSamPad * R, 0.0);
-  std::vector<int> perm(t.nVoxPad, -1);
-  for (int p = 0; p < nVox; ++p) {
-    int m = order[p];
-    perm[p] = d->mask_idx[m];
-    for (int l = 0; l < R0; ++l) beta64[(size_t)p * R + l] = d->bf[(size_t)m + (size_t)l * nVox];
-    beta64[(size_t)p * R + R0] = d->fieldmap ? d->fieldmap[m] : 0.0;
-  }
-  for (int s = 0; s < nSam; ++s) {
-    for (int l = 0; l < R0; ++l) gam64[(size_t)s * R + l] = d->kspha[(size_t)l + (size_t)s * R0];
-    gam64[(size_t)s * R + R0] = d->times[s];
-  }
-  for (size_t i = 0; i < beta64.size(); ++i)
-    if (!std::isfinite(beta64[i])) { delete h; return fail(nullptr, HOE_ERR_ARG, "bf/fieldmap must be finite"); }
-  for (size_t i = 0; i < gam64.size(); ++i)
-    if (!std::isfinite(gam64[i])) { delete h; return fail(nullptr, HOE_ERR_ARG, "kspha/times must be finite"); }
-
-  std::vector<double> betabar((size_t)t.nVt * R, 0.0), gambar((size_t)t.nSt * R, 0.0);
-  std::vector<double> dbmax((size_t)t.nVt * R, 0.0), kpmax((size_t)t.nSt * R, 0.0);
-  for (int vt = 0; vt < t.nVt; ++vt) {
-    int p0 = vt * t.VT, p1 = std::min(nVox, p0 + t.VT);
-    for (int l = 0; l < R; ++l) {
-      double lo = INFINITY, hi = -INFINITY;
-      for (int p = p0; p < p1; ++p) { double v = beta64[(size_t)p * R + l]; lo = std::min(lo, v); hi = std::max(hi, v); }
-      betabar[(size_t)vt * R + l] = 0.5 * (lo + hi);
-      dbmax[(size_t)vt * R + l] = 0.5 * (hi - lo);
-    }
-  }
-  for (int st = 0; st < t.nSt; ++st) {
-    int s0 = st * t.ST, s1 = std::min(nSam, s0 + t.ST);
-    for (int l = 0; l < R; ++l) {
-      double lo = INFINITY, hi = -INFINITY;
-      for (int s = s0; s < s1; ++s) { double v = gam64[(size_t)s * R + l]; lo = std::min(lo, v); hi = std::max(hi, v); }
-      gambar[(size_t)st * R + l] = 0.5 * (lo + hi);
-      kpmax[(size_t)st * R + l] = 0.5 * (hi - lo);
-    }
-  }
-  double bound = 0.0;
-  for (int vt = 0; vt < t.nVt; ++vt)
-    for (int st = 0; st < t.nSt; ++st) {
-      double b = 0.0;
-      for (int l = 0; l < R; ++l) b += dbmax[(size_t)vt * R + l] * kpmax[(size_t)st * R + l];
-      bound = std::max(bound, b);
-    }
-  t.residBound = bound;
-
-  std::vector<float> dbeta((size_t)t.nVoxPad * Rp, 0.f), kappa((size_t)t.nSamPad * Rp, 0.f);
-  std::vector<float> bfraw((size_t)t.nVoxPad * Rp, 0.f), kdot((size_t)t.nSamPad * Rp, 0.f);
-  std::vector<float> times_f(t.nSamPad, 0.f);
-  std::vector<double> kap64((size_t)t.nSamPad * R, 0.0);
-  for (int p = 0; p < nVox; ++p) {
-    int vt = p / t.VT;
-    for (int l = 0; l < R; ++l) {
-      dbeta[(size_t)p * Rp + l] = (float)(beta64[(size_t)p * R + l] - betabar[(size_t)vt * R + l]);
-      bfraw[(size_t)p * Rp + l] = (float)beta64[(size_t)p * R + l];
-    }
-  }
-  for (int s = 0; s < nSam; ++s) {
-    int st = s / t.ST;
-    for (int l = 0; l < R; ++l) {
-      double kv = gam64[(size_t)s * R + l] - gambar[(size_t)st * R + l];
-      kap64[(size_t)s * R + l] = kv;
-      kappa[(size_t)s * Rp + l] = (float)kv;
-    }
-    if (d->kspha_dt)
-      for (int l = 0; l < t.nTerm; ++l) kdot[(size_t)s * Rp + l] = (float)d->kspha_dt[(size_t)l + (size_t)s * t.nTerm];
-    times_f[s] = (float)d->times[s];
-  }
-  std::vector<float2> csm((size_t)t.nVoxPad * t.nChaPad, make_float2(0.f, 0.f));
-  for (int p = 0; p < nVox; ++p) {
-    int m = order[p];
-    for (int c = 0; c < t.nCha; ++c) {
-      float2 v = make_float2(1.f, 0.f);
-      if (d->csm) {
-        size_t o = 2 * ((size_t)m + (size_t)c * nVox);
-        v = make_float2((float)d->csm[o], (float)d->csm[o + 1]);
-      }
-      csm[(size_t)p * t.nChaPad + c] = v;
-    }
-  }
+  t = P.t;
+  const int R = t.R;
+  const int nSam = t.nSam;
+  auto &dbeta = P.dbeta, &kappa = P.kappa, &bfraw = P.bfraw, &kdot = P.kdot, &times_f = P.times_f;
+  auto &beta64 = P.beta64, &kap64 = P.kap64, &betabar = P.betabar, &gambar = P.gambar;
+  auto &csm = P.csm;
+  auto &perm = P.perm;
 
   // ---- split-K choice for the SIMT engine ----
   {
@@ -436,6 +621,22 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   return HOE_OK;
 }
 
+int hoe_plan(const hoe_desc *d, hoe_info *o) {
+  if (!o) return fail(nullptr, HOE_ERR_ARG, "output must not be NULL");
+  Plan P;
+  int rc = make_plan(d, P);
+  if (rc != HOE_OK) return rc;
+  const auto &t = P.t;
+  memset(o, 0, sizeof(*o));
+  o->nSam = t.nSam; o->nCha = t.nCha; o->nVox = t.nVox; o->nTermEff = t.R0; o->nFull = t.nFull;
+  o->engine = d->engine;
+  o->tile_samples = t.ST; o->tile_voxels = t.VT;
+  o->n_sample_tiles = t.nSt; o->n_voxel_tiles = t.nVt;
+  o->residual_rank = t.rank; o->residual_width = t.Rp;
+  o->residual_phase_bound = t.residBound;
+  return HOE_OK;
+}
+
 int hoe_close(hoe_handle *h) {
   if (!valid_handle(h)) return fail(nullptr, HOE_ERR_ARG, "invalid handle");
   if (h->closed) return HOE_OK;
@@ -461,6 +662,7 @@ int hoe_get_info(const hoe_handle *h, hoe_info *o) {
   o->tile_samples = t.ST; o->tile_voxels = t.VT;
   o->n_sample_tiles = t.nSt; o->n_voxel_tiles = t.nVt;
   o->split_forward = h->splitF; o->split_adjoint = h->splitA;
+  o->residual_rank = t.rank; o->residual_width = t.Rp;
   o->residual_phase_bound = t.residBound;
   o->device_bytes = h->bytes + (int64_t)h->tc.bytes;
   return HOE_OK;

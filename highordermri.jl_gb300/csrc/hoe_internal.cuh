@@ -16,9 +16,21 @@
 // A and B are evaluated once per operator in FP64 and range-reduced to their
 // fractional cycle in [-1/2, 1/2] before being stored as FP32.  Only the
 // residual dbeta.kappa, whose magnitude is bounded by the tile extents (a
-// few cycles at most, reported as residual_phase_bound), is formed per
-// (sample, voxel) pair in FP32.  The sum is range-reduced again before the
-// FP32 sine/cosine, so the argument of every sincos is in [-pi, pi].
+// few cycles, reported as residual_phase_bound), is formed per (sample,
+// voxel) pair in FP32.  The sum is range-reduced again before the FP32
+// sine/cosine, so the argument of every sincos is in [-pi, pi].
+//
+// The voxel-tile anchor of the basis components is the basis of one voxel
+// of the tile (the one nearest the tile's centre), so every dbeta_v is a
+// difference of basis vectors.  On a 2-D slice the solid harmonics are
+// polynomials of degree <= 3 in (x, y) and those differences span at most
+// 9 directions (10 with the fieldmap).  The residual is therefore stored in
+// a reduced basis: with column balancing S (so dbeta and kappa have equal
+// scales per component) and the right singular vectors V_r of the balanced
+// dbeta matrix (FP64 Householder QR + one-sided Jacobi SVD),
+//   dbeta.kappa = (dbeta S V_r) . (kappa S^-1 V_r) + e,
+// where the dropped directions contribute |e| <= 1e-9 cycles per dropped
+// direction.  The stored width Rp is r rounded up to 8, 12, 16 or 24.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -31,6 +43,7 @@ namespace hoe {
 
 constexpr int kTileS = 128;   // samples per sample tile (phase anchors, SIMT CTA rows)
 constexpr int kTileV = 128;   // voxels per voxel tile
+constexpr int kRF = 24;       // stored width of the raw basis / kspha_dt rows
 
 struct Tables {
   // sizes
@@ -41,14 +54,15 @@ struct Tables {
   int hasKdot = 0;
   double residBound = 0.0;
   // model tables (device)
-  float  *dbeta = nullptr;   // [nVoxPad][Rp]  beta_v - betabar
-  float  *kappa = nullptr;   // [nSamPad][Rp]  gamma_s - gammabar
+  int    rank = 0;          // reduced residual dimension r (<= R)
+  float  *dbeta = nullptr;   // [nVoxPad][Rp]  reduced, balanced beta_v - betabar
+  float  *kappa = nullptr;   // [nSamPad][Rp]  reduced, balanced gamma_s - gammabar
   float  *Atab  = nullptr;   // [nVt][nSamPad] frac(betabar . kappa)
   float  *Btab  = nullptr;   // [nSt][nVoxPad] frac(beta . gammabar)
   float2 *csm   = nullptr;   // [nVoxPad][nChaPad]
   int    *perm  = nullptr;   // [nVoxPad] linear grid index, -1 for padding
-  float  *bfraw = nullptr;   // [nVoxPad][Rp]  bf (R0 terms) and fieldmap at slot R0
-  float  *kdot  = nullptr;   // [nSamPad][Rp]  kspha_dt (nTerm terms), zero elsewhere
+  float  *bfraw = nullptr;   // [nVoxPad][kRF] bf (R0 terms) and fieldmap at slot R0
+  float  *kdot  = nullptr;   // [nSamPad][kRF] kspha_dt (nTerm terms), zero elsewhere
   float  *times = nullptr;   // [nSamPad]
 };
 

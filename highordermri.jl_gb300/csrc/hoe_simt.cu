@@ -71,7 +71,7 @@ k_fwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
   __shared__ __align__(16) float sD[T * RP];
   __shared__ __align__(16) float2 sZ[T * NC];
   __shared__ float sB[T];
-  __shared__ __align__(16) float sR[DERIV ? T * RP : 4];
+  __shared__ __align__(16) float sR[DERIV ? T * kRF : 4];
   const int st = blockIdx.x, split = blockIdx.y, c0 = blockIdx.z * NC;
   const int tid = threadIdx.x;
   const int s = st * kTileS + tid;
@@ -82,10 +82,10 @@ k_fwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
     float4 v = *reinterpret_cast<const float4 *>(kappa + (int64_t)s * RP + l);
     kap[l] = v.x; kap[l + 1] = v.y; kap[l + 2] = v.z; kap[l + 3] = v.w;
   }
-  float kd[DERIV ? RP : 1];
+  float kd[DERIV ? kRF : 1];
   if (DERIV) {
 #pragma unroll
-    for (int l = 0; l < RP; ++l) kd[l] = kdot[(int64_t)s * RP + l];
+    for (int l = 0; l < kRF; ++l) kd[l] = kdot[(int64_t)s * kRF + l];
   }
   float accR[NC], accI[NC];
 #pragma unroll
@@ -100,9 +100,9 @@ k_fwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
       float4 *dst = reinterpret_cast<float4 *>(sD);
       for (int i = tid; i < T * RP / 4; i += 128) dst[i] = src[i];
       if (DERIV) {
-        const float4 *srcr = reinterpret_cast<const float4 *>(bfraw + (int64_t)vt * T * RP);
+        const float4 *srcr = reinterpret_cast<const float4 *>(bfraw + (int64_t)vt * T * kRF);
         float4 *dstr = reinterpret_cast<float4 *>(sR);
-        for (int i = tid; i < T * RP / 4; i += 128) dstr[i] = srcr[i];
+        for (int i = tid; i < T * kRF / 4; i += 128) dstr[i] = srcr[i];
       }
       for (int i = tid; i < T * NC; i += 128) {
         int j = i / NC, c = i % NC;
@@ -131,8 +131,8 @@ k_fwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
       if (DERIV) {
         float g = 0.f;
 #pragma unroll
-        for (int l = 0; l < RP; ++l)
-          if (l < nTerm) g = fmaf(kd[l], sR[j * RP + l], g);
+        for (int l = 0; l < kRF; ++l)
+          if (l < nTerm) g = fmaf(kd[l], sR[j * kRF + l], g);
         float w = kTwoPi * g;
         float ncs = -w * sn, nsn = w * cs;
         cs = ncs; sn = nsn;
@@ -292,7 +292,7 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
            int nSamPad, int nVoxPad, int nChaPad, int nVt, int tps, float scaleG) {
   constexpr int T = kTileV;
   __shared__ __align__(16) float sD[T * RP];
-  __shared__ __align__(16) float sF[T * RP];
+  __shared__ __align__(16) float sF[T * kRF];
   __shared__ __align__(16) float2 sZ[T * NC];
   __shared__ float sB[T];
   __shared__ float sW1[4][T];
@@ -311,9 +311,9 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
     rr[c] = v.x; ri[c] = v.y;
   }
   const float ts = times[s];
-  float dk[RP];
+  float dk[kRF];
 #pragma unroll
-  for (int l = 0; l < RP; ++l) dk[l] = 0.f;
+  for (int l = 0; l < kRF; ++l) dk[l] = 0.f;
 
   const int vt0 = split * tps, vt1 = min(nVt, vt0 + tps);
   for (int vt = vt0; vt < vt1; ++vt) {
@@ -321,11 +321,9 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
     __syncthreads();
     {
       const float4 *src = reinterpret_cast<const float4 *>(dbeta + (int64_t)vt * T * RP);
-      const float4 *srf = reinterpret_cast<const float4 *>(bfraw + (int64_t)vt * T * RP);
-      for (int i = tid; i < T * RP / 4; i += 128) {
-        reinterpret_cast<float4 *>(sD)[i] = src[i];
-        reinterpret_cast<float4 *>(sF)[i] = srf[i];
-      }
+      const float4 *srf = reinterpret_cast<const float4 *>(bfraw + (int64_t)vt * T * kRF);
+      for (int i = tid; i < T * RP / 4; i += 128) reinterpret_cast<float4 *>(sD)[i] = src[i];
+      for (int i = tid; i < T * kRF / 4; i += 128) reinterpret_cast<float4 *>(sF)[i] = srf[i];
       for (int i = tid; i < T * NC; i += 128) {
         int j = i / NC, c = i % NC;
         sZ[i] = Z[((int64_t)vt * T + j) * nChaPad + c];
@@ -348,7 +346,7 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
       }
       float G = -scaleG * (cs * wi + sn * wr);
 #pragma unroll
-      for (int l = 0; l < RP; ++l) dk[l] = fmaf(G, sF[j * RP + l], dk[l]);
+      for (int l = 0; l < kRF; ++l) dk[l] = fmaf(G, sF[j * kRF + l], dk[l]);
       float g1 = G, gt = G * ts;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -364,25 +362,25 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
       gtpart[o] = (sWt[0][tid] + sWt[1][tid]) + (sWt[2][tid] + sWt[3][tid]);
     }
   }
-  float *dst = dkpart + ((int64_t)split * nSamPad + s) * RP;
+  float *dst = dkpart + ((int64_t)split * nSamPad + s) * kRF;
 #pragma unroll
-  for (int l = 0; l < RP; ++l) dst[l] = dk[l];
+  for (int l = 0; l < kRF; ++l) dst[l] = dk[l];
 }
 
-__global__ void k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamPad, int RP, int R0,
+__global__ void k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamPad, int R0,
                          int nSam, float *__restrict__ dk) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)nSam * R0) return;
   int s = (int)(i / R0), l = (int)(i % R0);
   float acc = 0.f;
-  for (int k = 0; k < nSplit; ++k) acc += dkpart[((int64_t)k * nSamPad + s) * RP + l];
+  for (int k = 0; k < nSplit; ++k) acc += dkpart[((int64_t)k * nSamPad + s) * kRF + l];
   dk[(int64_t)s * R0 + l] = acc;  // [nTermEff x nSam] column-major
 }
 
 // Per voxel: dL/dfieldmap and the fieldmap part of dL/dt0 (block partials in FP64).
 __global__ void k_bwd_vox(const float *__restrict__ g1part, const float *__restrict__ gtpart,
                           int nSt, int nVoxPad, const int *__restrict__ perm,
-                          const float *__restrict__ bfraw, int RP, int R0, float *__restrict__ ddf,
+                          const float *__restrict__ bfraw, int R0, float *__restrict__ ddf,
                           double *__restrict__ blockAcc) {
   __shared__ double red[256];
   int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -394,7 +392,7 @@ __global__ void k_bwd_vox(const float *__restrict__ g1part, const float *__restr
       gt += gtpart[(int64_t)k * nVoxPad + p];
     }
     if (ddf) ddf[perm[p]] = (float)gt;
-    contrib = -(double)bfraw[(int64_t)p * RP + R0] * g1;
+    contrib = -(double)bfraw[(int64_t)p * kRF + R0] * g1;
   }
   red[threadIdx.x] = contrib;
   __syncthreads();
@@ -406,7 +404,7 @@ __global__ void k_bwd_vox(const float *__restrict__ g1part, const float *__restr
 }
 
 __global__ void k_bwd_t0(const double *__restrict__ blockAcc, int nBlocks, int useB0,
-                         const float *__restrict__ dkpart, int nSplit, int nSamPad, int RP,
+                         const float *__restrict__ dkpart, int nSplit, int nSamPad,
                          const float *__restrict__ kdot, int nSam, int nTerm, int useCoef,
                          double *__restrict__ dt0) {
   __shared__ double red[256];
@@ -417,8 +415,8 @@ __global__ void k_bwd_t0(const double *__restrict__ blockAcc, int nBlocks, int u
     for (int64_t i = threadIdx.x; i < (int64_t)nSam * nTerm; i += blockDim.x) {
       int s = (int)(i / nTerm), l = (int)(i % nTerm);
       double g = 0.0;
-      for (int k = 0; k < nSplit; ++k) g += dkpart[((int64_t)k * nSamPad + s) * RP + l];
-      acc -= (double)kdot[(int64_t)s * RP + l] * g;
+      for (int k = 0; k < nSplit; ++k) g += dkpart[((int64_t)k * nSamPad + s) * kRF + l];
+      acc -= (double)kdot[(int64_t)s * kRF + l] * g;
     }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -451,9 +449,9 @@ void launch_adj(const hoe_handle *h, int nCC, cudaStream_t st) {
 template <int NC, bool DERIV>
 void dispatch_fwd_rp(const hoe_handle *h, int nCC, cudaStream_t st) {
   switch (h->t.Rp) {
+    case 8: launch_fwd<NC, 8, DERIV>(h, nCC, st); break;
     case 12: launch_fwd<NC, 12, DERIV>(h, nCC, st); break;
     case 16: launch_fwd<NC, 16, DERIV>(h, nCC, st); break;
-    case 20: launch_fwd<NC, 20, DERIV>(h, nCC, st); break;
     default: launch_fwd<NC, 24, DERIV>(h, nCC, st); break;
   }
 }
@@ -461,9 +459,9 @@ void dispatch_fwd_rp(const hoe_handle *h, int nCC, cudaStream_t st) {
 template <int NC>
 void dispatch_adj_rp(const hoe_handle *h, int nCC, cudaStream_t st) {
   switch (h->t.Rp) {
+    case 8: launch_adj<NC, 8>(h, nCC, st); break;
     case 12: launch_adj<NC, 12>(h, nCC, st); break;
     case 16: launch_adj<NC, 16>(h, nCC, st); break;
-    case 20: launch_adj<NC, 20>(h, nCC, st); break;
     default: launch_adj<NC, 24>(h, nCC, st); break;
   }
 }
@@ -474,16 +472,16 @@ void launch_bwd(const hoe_handle *h, float scaleG, cudaStream_t st) {
   int tps = (t.nVt + h->splitF - 1) / h->splitF;
   dim3 grid(t.nSt, h->splitF, 1);
   float *dkpart = h->s.gpart;
-  float *g1 = dkpart + (size_t)h->splitF * t.nSamPad * t.Rp;
+  float *g1 = dkpart + (size_t)h->splitF * t.nSamPad * kRF;
   float *gt = g1 + (size_t)t.nSt * t.nVoxPad;
 #define HOE_BWD(RPV)                                                                          \
   k_bwd_simt<NC, RPV><<<grid, 128, 0, st>>>(t.kappa, t.dbeta, t.Atab, t.Btab, h->s.Z, h->s.Yt, \
                                             t.bfraw, t.times, dkpart, g1, gt, t.nSamPad,      \
                                             t.nVoxPad, t.nChaPad, t.nVt, tps, scaleG)
   switch (t.Rp) {
+    case 8: HOE_BWD(8); break;
     case 12: HOE_BWD(12); break;
     case 16: HOE_BWD(16); break;
-    case 20: HOE_BWD(20); break;
     default: HOE_BWD(24); break;
   }
 #undef HOE_BWD
@@ -571,7 +569,7 @@ cudaError_t simt_backward(const hoe_handle *hc, const float2 *, const float2 *r,
   const auto &t = h->t;
   if (t.nChaPad > 16) return cudaErrorNotSupported;
   // scratch for the gradient partials, allocated on first use
-  size_t need = (size_t)h->splitF * t.nSamPad * t.Rp + 2 * (size_t)t.nSt * t.nVoxPad;
+  size_t need = (size_t)h->splitF * t.nSamPad * kRF + 2 * (size_t)t.nSt * t.nVoxPad;
   int nVB = (t.nVoxPad + 255) / 256;
   if (h->s.gpartElems < need || !h->s.dred) {
     if (h->s.gpart) cudaFree(h->s.gpart);
@@ -595,21 +593,21 @@ cudaError_t simt_backward(const hoe_handle *hc, const float2 *, const float2 *r,
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   float *dkpart = h->s.gpart;
-  float *g1 = dkpart + (size_t)h->splitF * t.nSamPad * t.Rp;
+  float *g1 = dkpart + (size_t)h->splitF * t.nSamPad * kRF;
   float *gt = g1 + (size_t)t.nSt * t.nVoxPad;
   if (flags & HOE_GRAD_KSPHA) {
     int64_t n = (int64_t)t.nSam * t.R0;
-    k_bwd_dk<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dkpart, h->splitF, t.nSamPad, t.Rp, t.R0, t.nSam, dk);
+    k_bwd_dk<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dkpart, h->splitF, t.nSamPad, t.R0, t.nSam, dk);
   }
   if (flags & HOE_GRAD_FIELDMAP) {
     e = cudaMemsetAsync(ddf, 0, (size_t)t.nFull * sizeof(float), st);
     if (e != cudaSuccess) return e;
   }
-  k_bwd_vox<<<nVB, 256, 0, st>>>(g1, gt, t.nSt, t.nVoxPad, t.perm, t.bfraw, t.Rp, t.R0,
+  k_bwd_vox<<<nVB, 256, 0, st>>>(g1, gt, t.nSt, t.nVoxPad, t.perm, t.bfraw, t.R0,
                                  (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr, h->s.dred);
   if (flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF))
     k_bwd_t0<<<1, 256, 0, st>>>(h->s.dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0, dkpart, h->splitF,
-                                t.nSamPad, t.Rp, t.kdot, t.nSam, t.nTerm,
+                                t.nSamPad, t.kdot, t.nSam, t.nTerm,
                                 (flags & HOE_GRAD_T0_COEF) ? 1 : 0, dt0);
   return cudaGetLastError();
 }

@@ -44,6 +44,10 @@ constexpr float kTwoPi = 6.28318530717958647692f;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
 
 constexpr int A_TILE_BYTES = TM * TK * 2;    // one BF16 A tile (hi or lo): 16 KB
+// The tensor-core FP32 accumulator sums at most GROUP chunks (GROUP*12 MMAs)
+// before it is added, in round-to-nearest FP32, into register sums: long
+// accumulation chains in TMEM lose accuracy on coherent sums.
+constexpr int GROUP = 16;
 
 // byte offset of element (r, k) in a no-swizzle K-major tile with K = TK:
 // core matrices of 8 rows x 16 B; cores adjacent in K are 128 B apart (LBO),
@@ -86,8 +90,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 }
 
 // Bounded wait; returns false on timeout or when another role aborted.
-__device__ __noinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile int *abort,
-                                      int *gerr) {
+__device__ __noinline__ bool wait_bar_slow(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                           int *gerr) {
   uint64_t t0 = 0;
   for (uint32_t n = 0;; ++n) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -102,6 +106,12 @@ __device__ __noinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile i
       }
     }
   }
+}
+
+__device__ __forceinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                         int *gerr) {
+  if (mbar_try_wait(bar, parity)) return true;
+  return wait_bar_slow(bar, parity, abort, gerr);
 }
 
 // Bounded wait that ignores the abort flag (used to drain in-flight work).
@@ -162,6 +172,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x (low half) = lo_elem
   return *reinterpret_cast<uint32_t *>(&v);
@@ -173,19 +194,26 @@ struct TcParams {
   const float *colvec;     // [nColPad][RP]: dbeta (forward) / kappa (adjoint)
   const float *colAnchor;  // [rowTile][colAnchorStride]: Btab (forward) / Atab (adjoint)
   const uint16_t *Bop;     // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
-  float2 *part;            // [split][nRowPad][nChaPad] partial sums
+  float2 *part;            // [slot][nRowPad][nChaPad] partial sums (zeroed before launch)
   int *err;
   int rowAnchorStride, colAnchorStride;
   int nRowPad, nChaPad, nChaTC;
-  int nColChunks, chunksPerSplit;
+  int nColChunks;          // column chunks per row tile (C)
+  int64_t work;            // nRowTiles * C work items, split evenly over gridDim.x CTAs
 };
+
+// CTA that owns work item w when W items are split into G contiguous ranges
+// [b*W/G, (b+1)*W/G).
+__host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
+  return (int)(((w + 1) * (int64_t)G - 1) / W);
+}
 
 // Shared-memory plan (dynamic, 1024-byte aligned base):
 //   A    [NS][2][A_TILE_BYTES]        phase tile hi / lo
 //   B    [NS][2][N*TK*2]              B operand hi / lo
 //   CV   [NS][TV][RP] float           column phase vectors
 //   CA   [NS][TV] float               column anchors
-//   bars full[NS], afull[NS], empty[NS], done; tmem base; abort flag
+//   bars full[NS], afull[NS], empty[NS], segdone[2], tmemfree[2]; tmem base; abort flag
 template <int N, int RP, int NS>
 struct Smem {
   static constexpr int B_TILE = N * TK * 2;
@@ -194,7 +222,7 @@ struct Smem {
   static constexpr size_t CV_OFF = B_OFF + (size_t)NS * 2 * B_TILE;
   static constexpr size_t CA_OFF = CV_OFF + (size_t)NS * TV * RP * 4;
   static constexpr size_t BAR_OFF = (CA_OFF + (size_t)NS * TV * 4 + 7) / 8 * 8;
-  static constexpr size_t MISC_OFF = BAR_OFF + (size_t)(3 * NS + 1) * 8;
+  static constexpr size_t MISC_OFF = BAR_OFF + (size_t)(3 * NS + 4) * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
 
@@ -210,16 +238,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
   uint64_t *afull = full + NS;
   uint64_t *empty = afull + NS;
-  uint64_t *done = empty + NS;
+  uint64_t *segdone = empty + NS;   // [2]: accumulator buffer b complete (group of chunks)
+  uint64_t *tmemfree = segdone + 2; // [2]: accumulator buffer b read out
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::MISC_OFF);
   volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
-  constexpr uint32_t TMEM_COLS = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+  // two accumulator buffers of N FP32 columns
+  constexpr uint32_t TMEM_COLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int rowTile = blockIdx.x, split = blockIdx.y;
-  const int ch0 = split * p.chunksPerSplit;
-  const int ch1 = min(p.nColChunks, ch0 + p.chunksPerSplit);
-  const int nIter = max(0, ch1 - ch0);
+  const int C = p.nColChunks;
+  const int G = gridDim.x, b = blockIdx.x;
+  const int64_t wb = (int64_t)b * p.work / G, we = (int64_t)(b + 1) * p.work / G;
+  const int nIter = (int)(we - wb);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NS; ++i) {
@@ -227,7 +257,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       mbar_init(&afull[i], PHASE_WARPS);
       mbar_init(&empty[i], 1);
     }
-    mbar_init(done, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&segdone[i], 1);
+      mbar_init(&tmemfree[i], PHASE_WARPS);
+    }
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -242,27 +275,99 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
+  // Work item w = (row tile w / C, chunk w % C).  A "group" is a run of at
+  // most GROUP consecutive chunks of one row tile; group g accumulates into
+  // TMEM buffer g & 1.
+  // first (row tile, chunk) of this CTA; later items advance incrementally
+  const int rt0 = (int)(wb / C), ch0 = (int)(wb % C);
   if (warp < PHASE_WARPS) {
-    // ---------------- phase generator: rows x (half of the stage's columns)
+    // ---------------- phase generator: rows x (half of the stage's columns).
+    // After the first stage of group g+1 (or at the end) all 8 warps add
+    // group g's accumulator into register sums (columns split by warp half)
+    // and, at the end of a row tile, write the sums to the partial slot.
     const int row = (warp & 3) * 32 + lane;
     const int half = warp >> 2;
-    const int grow = rowTile * TM + row;
-    float rv[RP];
+    constexpr int NA = N / 2;  // accumulator columns owned by this thread
+    float acc[NA];
 #pragma unroll
-    for (int l = 0; l < RP; l += 4) {
-      float4 v = *reinterpret_cast<const float4 *>(p.rowvec + (int64_t)grow * RP + l);
-      rv[l] = v.x; rv[l + 1] = v.y; rv[l + 2] = v.z; rv[l + 3] = v.w;
-    }
-    int curTile = -1;
+    for (int i = 0; i < NA; ++i) acc[i] = 0.f;
+    float rv[RP];
+    int curRT = -1, curTile = -1, grp = -1, grow = 0;
+    int pendGrp = -1, pendRT = -1;
+    bool pendLast = false;
     float a = 0.f;
     bool ok = true;
-    for (int it = 0; it < nIter && ok; ++it) {
+    auto flush = [&]() {
+      // add group pendGrp into acc; write acc out if it closed its row tile
+      const int g = pendGrp;
+      bool got = ok && wait_bar(&segdone[g & 1], (g >> 1) & 1, abort, p.err);
+      tc_fence_after();
+      if (got) {
+        const uint32_t base = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((g & 1) * N + half * NA);
+        if constexpr (NA % 16 == 0) {
+#pragma unroll
+          for (int c0 = 0; c0 < NA; c0 += 16) {
+            float v[16];
+            tmem_ld16(base + c0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+          }
+        } else {
+          static_assert(NA == 8, "accumulator columns per thread");
+          float v[8];
+          tmem_ld8(base, v);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) acc[i] += v[i];
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tmemfree[g & 1]);
+      if (pendLast) {
+        const int slot = b - work_owner((int64_t)pendRT * C, p.work, G);
+        float2 *dst = p.part + ((int64_t)slot * p.nRowPad + (int64_t)pendRT * TM + row) * p.nChaPad;
+        const int nOut = min(p.nChaTC, p.nChaPad);
+        if (ok) {
+#pragma unroll
+          for (int i = 0; i < NA; i += 2) {
+            int c = (half * NA + i) / 2;
+            if (c < nOut) dst[c] = make_float2(acc[i], acc[i + 1]);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < NA; ++i) acc[i] = 0.f;
+      }
+      pendGrp = -1;
+    };
+    int rt = rt0, ch = ch0;
+    // anchor phase of the next anchor tile, loaded one stage ahead
+    float aNext = nIter > 0
+        ? p.rowAnchor[(int64_t)(ch0 * TV / 128) * p.rowAnchorStride + rt0 * TM + row] : 0.f;
+    for (int it = 0; it < nIter && ok; ++it, ++ch) {
+      if (ch == C) { ch = 0; ++rt; }
+      if (it == 0 || ch % GROUP == 0) ++grp;
+      if (rt != curRT) {
+        curRT = rt;
+        curTile = -1;
+        grow = rt * TM + row;
+#pragma unroll
+        for (int l = 0; l < RP; l += 4) {
+          float4 v = *reinterpret_cast<const float4 *>(p.rowvec + (int64_t)grow * RP + l);
+          rv[l] = v.x; rv[l + 1] = v.y; rv[l + 2] = v.z; rv[l + 3] = v.w;
+        }
+      }
       const int slot = it % NS, round = it / NS;
-      const int col0 = (ch0 + it) * TV;
+      const int col0 = ch * TV;
       const int colTile = col0 / 128;
       if (colTile != curTile) {
-        a = p.rowAnchor[(int64_t)colTile * p.rowAnchorStride + grow];
+        a = aNext;
         curTile = colTile;
+      }
+      {
+        int nch = ch + 1, nrt = rt;
+        if (nch == C) { nch = 0; ++nrt; }
+        if (it + 1 < nIter && (nrt != rt || nch * TV / 128 != colTile))
+          aNext = p.rowAnchor[(int64_t)(nch * TV / 128) * p.rowAnchorStride + nrt * TM + row];
       }
       if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) { ok = false; break; }
       if (!wait_bar(&full[slot], round & 1, abort, p.err)) { ok = false; break; }
@@ -305,40 +410,36 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&afull[slot]);
-    }
-    // ---------------- epilogue: warps 0-3 read their TMEM lane quarter
-    if (warp < 4) {
-      float2 *dst = p.part + ((int64_t)split * p.nRowPad + grow) * p.nChaPad;
-      const int nOut = min(p.nChaTC, p.nChaPad);
-      if (nIter == 0) {
-        for (int c = 0; c < nOut; ++c) dst[c] = make_float2(0.f, 0.f);
-      } else {
-        bool got = ok && wait_bar(done, 0, abort, p.err);
-        tc_fence_after();
-        if (got) {
-#pragma unroll 1
-          for (int c0 = 0; c0 < N; c0 += 16) {
-            float v[16];
-            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
-#pragma unroll
-            for (int i = 0; i < 16; i += 2) {
-              int c = (c0 + i) / 2;
-              if (c < nOut) dst[c] = make_float2(v[i], v[i + 1]);
-            }
-          }
-        }
+      // the previous group is flushed one stage late, so its MMAs are done by now
+      if (pendGrp >= 0) flush();
+      const bool endRT = (it == nIter - 1) || (ch + 1 == C);
+      if (endRT || (ch + 1) % GROUP == 0) {
+        pendGrp = grp;
+        pendRT = rt;
+        pendLast = endRT;
       }
     }
+    if (pendGrp >= 0) flush();
   } else if (warp == MMA_WARP) {
     // ---------------- MMA issuer (one thread)
     if (lane == 0 && nIter > 0) {
       constexpr uint32_t idesc = idesc_bf16(TM, N);
-      int issued = 0;
-      for (int it = 0; it < nIter; ++it) {
+      int issued = 0, grp = -1;
+      int ch = ch0;
+      for (int it = 0; it < nIter; ++it, ++ch) {
+        if (ch == C) ch = 0;
+        const bool first = (it == 0) || (ch % GROUP == 0);
+        if (first) {
+          ++grp;
+          // buffer grp&1 was last used by group grp-2: wait until it was read out
+          if (grp >= 2 && !wait_bar(&tmemfree[grp & 1], ((grp >> 1) - 1) & 1, abort, p.err)) break;
+        }
+        const bool last = (it == nIter - 1) || (ch + 1 == C) || ((ch + 1) % GROUP == 0);
         const int slot = it % NS, round = it / NS;
         if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
         if (!wait_bar(&afull[slot], round & 1, abort, p.err)) break;
         tc_fence_after();
+        const uint32_t dt = tmem + (uint32_t)((grp & 1) * N);
         const uint32_t aHi = smem_u32(sA + (size_t)slot * 2 * A_TILE_BYTES);
         const uint32_t aLo = aHi + A_TILE_BYTES;
         const uint32_t bHi = smem_u32(sB + (size_t)slot * 2 * S::B_TILE);
@@ -346,19 +447,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
 #pragma unroll
         for (int ks = 0; ks < TK / 16; ++ks) {
           const uint32_t ko = ks * 2 * LBO;  // 16 BF16 = two core matrices along K
-          umma(tmem, umma_desc(aHi + ko), umma_desc(bHi + ko), idesc, (it | ks) ? 1u : 0u);
-          umma(tmem, umma_desc(aHi + ko), umma_desc(bLo + ko), idesc, 1u);
-          umma(tmem, umma_desc(aLo + ko), umma_desc(bHi + ko), idesc, 1u);
+          umma(dt, umma_desc(aHi + ko), umma_desc(bHi + ko), idesc, (first && ks == 0) ? 0u : 1u);
+          umma(dt, umma_desc(aHi + ko), umma_desc(bLo + ko), idesc, 1u);
+          umma(dt, umma_desc(aLo + ko), umma_desc(bHi + ko), idesc, 1u);
         }
         umma_commit(&empty[slot]);
+        if (last) umma_commit(&segdone[grp & 1]);
         issued = it + 1;
       }
-      if (issued == nIter) {
-        umma_commit(done);
-      } else if (issued > 0) {
+      if (issued != nIter && issued > 0) {
         // aborted: let the MMAs already issued finish before TMEM is freed
-        const int last = issued - 1;
-        drain_bar(&empty[last % NS], (last / NS) & 1);
+        const int lastIt = issued - 1;
+        drain_bar(&empty[lastIt % NS], (lastIt / NS) & 1);
       }
     }
     __syncwarp();
@@ -367,15 +467,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
     if (lane == 0) {
       const uint32_t bBytes = 2 * S::B_TILE, cvBytes = TV * RP * 4, caBytes = TV * 4;
       int issued = 0;
-      for (int it = 0; it < nIter; ++it) {
+      int rt = rt0, ch = ch0;
+      for (int it = 0; it < nIter; ++it, ++ch) {
+        if (ch == C) { ch = 0; ++rt; }
         const int slot = it % NS, round = it / NS;
         if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
-        const int ch = ch0 + it;
         const int col0 = ch * TV;
         mbar_expect_tx(&full[slot], bBytes + cvBytes + caBytes);
         bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, p.Bop + (size_t)ch * 2 * (N * TK), bBytes, &full[slot]);
         bulk_g2s(sCV + slot * TV * RP, p.colvec + (size_t)col0 * RP, cvBytes, &full[slot]);
-        bulk_g2s(sCA + slot * TV, p.colAnchor + (int64_t)rowTile * p.colAnchorStride + col0, caBytes,
+        bulk_g2s(sCA + slot * TV, p.colAnchor + (int64_t)rt * p.colAnchorStride + col0, caBytes,
                  &full[slot]);
         issued = it + 1;
       }
@@ -436,65 +537,101 @@ __global__ void k_tc_bop_adjoint(const float2 *__restrict__ Yt, uint16_t *__rest
   tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
 }
 
-int tc_ncha(int nCha) { return std::max(8, (nCha + 7) / 8 * 8); }
+int tc_ncha(int nCha) {
+  int n = 8;
+  while (n < nCha) n *= 2;
+  return n;  // 8, 16, 32 or 64 coils per MMA: N = 16, 32, 64, 128
+}
 
 template <int N, int RP>
-cudaError_t launch_contract(const hoe_handle *h, const TcParams &p, int gridX, int gridY, cudaStream_t st) {
-  constexpr int NS = N <= 64 ? 4 : 3;
+struct Kern {
+  static constexpr int NS = N <= 64 ? 4 : 3;
   using S = Smem<N, RP, NS>;
   static_assert(S::BYTES <= 227 * 1024, "shared memory plan exceeds 227 KB");
-  auto kern = k_tc_contract<N, RP, NS>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES);
+  static void *fn() { return (void *)k_tc_contract<N, RP, NS>; }
+};
+
+template <int N, int RP>
+cudaError_t launch_contract(const hoe_handle *h, const TcParams &p, int G, cudaStream_t st) {
+  using K = Kern<N, RP>;
+  auto kern = k_tc_contract<N, RP, K::NS>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES);
   if (e != cudaSuccess) return e;
-  kern<<<dim3(gridX, gridY), THREADS, S::BYTES, st>>>(p);
+  kern<<<G, THREADS, K::S::BYTES, st>>>(p);
   h->launches += 1;
   return cudaGetLastError();
 }
 
+// resident CTAs per SM of the instantiation for (N, RP)
+template <int N, int RP>
+int blocks_per_sm() {
+  using K = Kern<N, RP>;
+  auto kern = k_tc_contract<N, RP, K::NS>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES) != cudaSuccess)
+    return 1;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, THREADS, K::S::BYTES) != cudaSuccess || nb < 1)
+    nb = 1;
+  return nb;
+}
+
+
 template <int RP>
-cudaError_t dispatch_n(const hoe_handle *h, const TcParams &p, int N, int gx, int gy, cudaStream_t st) {
+cudaError_t dispatch_n(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
   switch (N) {
-    case 16: return launch_contract<16, RP>(h, p, gx, gy, st);
-    case 32: return launch_contract<32, RP>(h, p, gx, gy, st);
-    case 48: return launch_contract<48, RP>(h, p, gx, gy, st);
-    case 64: return launch_contract<64, RP>(h, p, gx, gy, st);
-    case 80: return launch_contract<80, RP>(h, p, gx, gy, st);
-    case 96: return launch_contract<96, RP>(h, p, gx, gy, st);
-    case 112: return launch_contract<112, RP>(h, p, gx, gy, st);
-    case 128: return launch_contract<128, RP>(h, p, gx, gy, st);
-    default: return cudaErrorNotSupported;
+    case 16: return launch_contract<16, RP>(h, p, G, st);
+    case 32: return launch_contract<32, RP>(h, p, G, st);
+    case 64: return launch_contract<64, RP>(h, p, G, st);
+    default: return launch_contract<128, RP>(h, p, G, st);
   }
 }
 
-cudaError_t dispatch(const hoe_handle *h, const TcParams &p, int N, int gx, int gy, cudaStream_t st) {
+cudaError_t dispatch(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
   switch (h->t.Rp) {
-    case 12: return dispatch_n<12>(h, p, N, gx, gy, st);
-    case 16: return dispatch_n<16>(h, p, N, gx, gy, st);
-    case 20: return dispatch_n<20>(h, p, N, gx, gy, st);
-    default: return dispatch_n<24>(h, p, N, gx, gy, st);
+    case 8: return dispatch_n<8>(h, p, N, G, st);
+    case 12: return dispatch_n<12>(h, p, N, G, st);
+    case 16: return dispatch_n<16>(h, p, N, G, st);
+    default: return dispatch_n<24>(h, p, N, G, st);
   }
 }
 
-// split-K so that the grid covers the SMs in whole waves as far as possible
-int choose_split(int rowTiles, int chunks, int numSMs) {
-  int best = 1;
-  double bestCost = 1e300;
-  for (int s = 1; s <= std::min(chunks, 64); ++s) {
-    int cps = (chunks + s - 1) / s;
-    int sp = (chunks + cps - 1) / cps;
-    long ctas = (long)rowTiles * sp;
-    long waves = (ctas + numSMs - 1) / numSMs;
-    double cost = (double)waves * cps + 0.02 * sp * rowTiles / numSMs;  // wave time + reduce
-    if (cost < bestCost) { bestCost = cost; best = sp; }
+template <int RP>
+int bps_n(int N) {
+  switch (N) {
+    case 16: return blocks_per_sm<16, RP>();
+    case 32: return blocks_per_sm<32, RP>();
+    case 64: return blocks_per_sm<64, RP>();
+    default: return blocks_per_sm<128, RP>();
   }
-  return best;
+}
+
+int bps(int Rp, int N) {
+  switch (Rp) {
+    case 8: return bps_n<8>(N);
+    case 12: return bps_n<12>(N);
+    case 16: return bps_n<16>(N);
+    default: return bps_n<24>(N);
+  }
+}
+
+// Largest number of CTAs that share one row tile when rowTiles*C work items
+// are split evenly over G CTAs.
+int max_slots(int rowTiles, int C, int G) {
+  const int64_t W = (int64_t)rowTiles * C;
+  int J = 1;
+  for (int r = 0; r < rowTiles; ++r) {
+    int b0 = work_owner((int64_t)r * C, W, G), b1 = work_owner((int64_t)(r + 1) * C - 1, W, G);
+    J = std::max(J, b1 - b0 + 1);
+  }
+  return J;
 }
 
 struct TcBuffers {
   uint16_t *bopF = nullptr, *bopA = nullptr;
   float2 *part = nullptr;
   int *err = nullptr;
-  int N = 0, nChaTC = 0, splitF = 1, splitA = 1;
+  int N = 0, nChaTC = 0;
+  int gridF = 1, gridA = 1, slotsF = 1, slotsA = 1;
   size_t bopFElems = 0, bopAElems = 0, partElems = 0;
 };
 
@@ -522,11 +659,14 @@ cudaError_t tc_prepare(hoe_handle *h) {
   b.nChaTC = tc_ncha(t.nCha);
   b.N = 2 * b.nChaTC;
   const int chunksF = t.nVoxPad / TV, chunksA = t.nSamPad / TV;
-  b.splitF = choose_split(t.nSt, chunksF, h->numSMs);
-  b.splitA = choose_split(t.nVt, chunksA, h->numSMs);
+  const int G = h->numSMs * bps(t.Rp, b.N);
+  b.gridF = (int)std::min<int64_t>(G, (int64_t)t.nSt * chunksF);
+  b.gridA = (int)std::min<int64_t>(G, (int64_t)t.nVt * chunksA);
+  b.slotsF = max_slots(t.nSt, chunksF, b.gridF);
+  b.slotsA = max_slots(t.nVt, chunksA, b.gridA);
   b.bopFElems = (size_t)chunksF * 2 * b.N * TK;
   b.bopAElems = (size_t)chunksA * 2 * b.N * TK;
-  b.partElems = std::max((size_t)b.splitF * t.nSamPad, (size_t)b.splitA * t.nVoxPad) * t.nChaPad;
+  b.partElems = std::max((size_t)b.slotsF * t.nSamPad, (size_t)b.slotsA * t.nVoxPad) * t.nChaPad;
   size_t bytes = b.bopFElems * 2 + 256 + b.bopAElems * 2 + 256 + b.partElems * sizeof(float2) + 256 + 256;
   unsigned char *buf = nullptr;
   cudaError_t e = cudaMalloc(&buf, bytes);
@@ -580,13 +720,14 @@ cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const flo
   p.Bop = b.bopF;
   p.nRowPad = t.nSamPad;
   p.nColChunks = chunks;
-  p.chunksPerSplit = (chunks + b.splitF - 1) / b.splitF;
-  const int splits = (chunks + p.chunksPerSplit - 1) / p.chunksPerSplit;
+  p.work = (int64_t)t.nSt * chunks;
+  cudaError_t e = cudaMemsetAsync(b.part, 0, (size_t)b.slotsF * t.nSamPad * t.nChaPad * sizeof(float2), st);
+  if (e != cudaSuccess) return e;
   trace(h, EV_FK0, st);
-  cudaError_t e = dispatch(h, p, b.N, t.nSt, splits, st);
+  e = dispatch(h, p, b.N, b.gridF, st);
   trace(h, EV_FK1, st);
   if (e != cudaSuccess) return e;
-  return simt_reduce_forward(h, b.part, splits, y, D, mode, st);
+  return simt_reduce_forward(h, b.part, b.slotsF, y, D, mode, st);
 }
 
 cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) {
@@ -606,13 +747,14 @@ cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) 
   p.Bop = b.bopA;
   p.nRowPad = t.nVoxPad;
   p.nColChunks = chunks;
-  p.chunksPerSplit = (chunks + b.splitA - 1) / b.splitA;
-  const int splits = (chunks + p.chunksPerSplit - 1) / p.chunksPerSplit;
+  p.work = (int64_t)t.nVt * chunks;
+  cudaError_t e = cudaMemsetAsync(b.part, 0, (size_t)b.slotsA * t.nVoxPad * t.nChaPad * sizeof(float2), st);
+  if (e != cudaSuccess) return e;
   trace(h, EV_AK0, st);
-  cudaError_t e = dispatch(h, p, b.N, t.nVt, splits, st);
+  e = dispatch(h, p, b.N, b.gridA, st);
   trace(h, EV_AK1, st);
   if (e != cudaSuccess) return e;
-  return simt_reduce_adjoint(h, b.part, splits, x, st);
+  return simt_reduce_adjoint(h, b.part, b.slotsA, x, st);
 }
 
 int *tc_error_word(const hoe_handle *h) {

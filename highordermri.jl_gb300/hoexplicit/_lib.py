@@ -34,7 +34,7 @@ EXPORTED = (
     "hoe_version", "hoe_abi_version", "hoe_create", "hoe_close", "hoe_free", "hoe_is_closed",
     "hoe_last_error", "hoe_get_info", "hoe_set_engine", "hoe_forward", "hoe_adjoint",
     "hoe_normal", "hoe_derivative", "hoe_backward", "hoe_set_timing", "hoe_get_timings",
-    "hoe_forward_noalloc", "hoe_check",
+    "hoe_forward_noalloc", "hoe_check", "hoe_plan",
 )
 
 
@@ -97,6 +97,7 @@ class HoeInfo(ctypes.Structure):
         ("tile_samples", ctypes.c_int32), ("tile_voxels", ctypes.c_int32),
         ("n_sample_tiles", ctypes.c_int32), ("n_voxel_tiles", ctypes.c_int32),
         ("split_forward", ctypes.c_int32), ("split_adjoint", ctypes.c_int32),
+        ("residual_rank", ctypes.c_int32), ("residual_width", ctypes.c_int32),
         ("residual_phase_bound", ctypes.c_double), ("device_bytes", ctypes.c_int64),
     ]
 
@@ -135,6 +136,7 @@ def load():
     lib.hoe_set_timing.argtypes = [H, ctypes.c_int32]
     lib.hoe_get_timings.argtypes = [H, ctypes.POINTER(HoeTimings)]
     lib.hoe_check.argtypes = [H, vp]
+    lib.hoe_plan.argtypes = [ctypes.POINTER(HoeDesc), ctypes.POINTER(HoeInfo)]
     lib.hoe_forward_noalloc.argtypes = [ctypes.POINTER(HoeRawModel), vp, vp, vp]
     for name in EXPORTED:
         if name not in ("hoe_free",):

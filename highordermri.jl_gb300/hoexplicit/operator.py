@@ -75,6 +75,105 @@ class _Vec:
         return result
 
 
+def build_desc(grid: Grid, kspha, times, *, fieldmap=None, csm=None, mask=None, concomitant=None,
+               recon_terms=None, k_nominal=None, kspha_dt=None, kdot=None, engine=DEFAULT_ENGINE,
+               device=0, split_hint=0):
+    """Validate the constructor inputs (reference rules) and build the C
+    descriptor.  Returns (desc, keep, meta); ``keep`` holds the host arrays the
+    descriptor points to and must outlive every use of ``desc``."""
+    if engine not in ENGINES:
+        raise ArgumentError(f"unknown engine {engine!r}; choose one of {sorted(ENGINES)}")
+    kspha = np.asarray(kspha)
+    if kspha.ndim != 2:
+        raise DimensionMismatch("kspha must be (nTerm, nSam)")
+    nTerm, nSam = kspha.shape
+    if nTerm not in (9, 16):
+        raise ArgumentError("kspha requires 9 or 16 terms")
+    times = np.asarray(times, dtype=np.float64).reshape(-1)
+    if times.size != nSam:
+        raise DimensionMismatch("times and kspha")
+    nFull = grid.nX * grid.nY * grid.nZ
+    mask = np.ones(nFull, dtype=bool) if mask is None else _fortran_flat(mask).astype(bool)
+    if mask.size != nFull:
+        raise DimensionMismatch("mask and grid")
+    fieldmap = np.zeros(nFull) if fieldmap is None else _fortran_flat(fieldmap).astype(np.float64)
+    if fieldmap.size != nFull:
+        raise DimensionMismatch("fieldmap and mask")
+    if csm is None:
+        csm_flat = np.ones((nFull, 1), dtype=np.complex128)
+    else:
+        csm = np.asarray(csm)
+        nCha_ = csm.shape[-1]
+        if csm.size != nFull * nCha_:
+            raise DimensionMismatch("csm and grid")
+        csm_flat = csm.reshape(nFull, nCha_, order="F").astype(np.complex128)
+    nCha = csm_flat.shape[1]
+    idx = np.flatnonzero(mask)
+    nVox = idx.size
+    if nVox == 0:
+        raise ArgumentError("mask must contain voxels")
+    if nSam <= 0 or nCha <= 0:
+        raise ArgumentError("samples and coils must be positive")
+    if k_nominal is None:
+        k_nominal = kspha[1:4, :]
+    k_nominal = np.asarray(k_nominal, dtype=np.float64)
+    if k_nominal.shape[0] != 3:
+        raise ArgumentError("k_nominal must have 3 terms (row) for kx, ky, kz")
+
+    prepared = prep_kspha(kspha, k_nominal, nTerm, recon_terms)
+    xm, ym, zm = grid.x[idx], grid.y[idx], grid.z[idx]
+    bf = basisfunc_spha(xm, ym, zm, list(range(1, nTerm + 1)))
+    derivative_mode = kspha_dt is not None
+    # the derivative mode ignores concomitant terms (array_operator.jl:139)
+    bf, prepared = prep_concomitant(bf, prepared, xm, ym, zm,
+                                    None if derivative_mode else concomitant)
+    has_conc = int(prepared.shape[0] != nTerm)
+    kd = kspha_dt if kspha_dt is not None else kdot
+    if kd is not None:
+        kd = np.asfortranarray(kd, dtype=np.float64)
+        if kd.shape != (nTerm, nSam):
+            raise ArgumentError("kspha_dt must have same size as kspha")
+
+    keep = dict(
+        mask_idx=np.ascontiguousarray(idx, dtype=np.int32),
+        bf=np.asfortranarray(bf, dtype=np.float64),
+        kspha=np.asfortranarray(prepared, dtype=np.float64),
+        times=np.ascontiguousarray(times),
+        fieldmap=np.ascontiguousarray(fieldmap[idx]),
+        csm=np.asfortranarray(csm_flat[idx, :]),
+        kspha_dt=kd,
+    )
+    k = keep
+    desc = _lib.HoeDesc()
+    desc.abi_version = _lib.HOE_ABI_VERSION
+    desc.nX, desc.nY, desc.nZ = grid.nX, grid.nY, grid.nZ
+    desc.nSam, desc.nCha, desc.nTerm = nSam, nCha, nTerm
+    desc.has_concomitant = has_conc
+    desc.nVox = nVox
+    desc.engine = ENGINES[engine]
+    desc.device = device
+    desc.split_hint = int(split_hint)
+    desc.mask_idx = k["mask_idx"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    desc.bf = _dptr(k["bf"])
+    desc.kspha = _dptr(k["kspha"])
+    desc.times = _dptr(k["times"])
+    desc.fieldmap = _dptr(k["fieldmap"])
+    desc.csm = k["csm"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    desc.kspha_dt = _dptr(kd)
+    meta = dict(nSam=nSam, nCha=nCha, nVox=nVox, nTerm=nTerm, nTermEff=prepared.shape[0], nFull=nFull,
+                mask=mask, derivative_mode=derivative_mode)
+    return desc, keep, meta
+
+
+def plan(grid: Grid, kspha, times, **kwargs) -> dict:
+    """Host-side plan of the operator (hoe_plan): tiles, residual rank and
+    width, residual phase bound.  Needs no GPU."""
+    desc, keep, meta = build_desc(grid, kspha, times, **kwargs)
+    inf = _lib.HoeInfo()
+    _lib.check(_lib.load().hoe_plan(ctypes.byref(desc), ctypes.byref(inf)))
+    return {name: getattr(inf, name) for name, _ in inf._fields_}
+
+
 class ExplicitGB300Op:
     """Resident explicit encoding operator on one GB300 (the ``:gb300`` backend).
 
@@ -92,8 +191,6 @@ class ExplicitGB300Op:
         torch = _torch()
         if not torch.cuda.is_available():
             raise _lib.HoeError("the :gb300 explicit operator requires a CUDA device")
-        if engine not in ENGINES:
-            raise ArgumentError(f"unknown engine {engine!r}; choose one of {sorted(ENGINES)}")
         if gpus is not None:
             ids = [int(g) for g in gpus]
             if len(ids) != 1:
@@ -104,83 +201,13 @@ class ExplicitGB300Op:
         else:
             device = torch.cuda.current_device()
 
-        kspha = np.asarray(kspha)
-        if kspha.ndim != 2:
-            raise DimensionMismatch("kspha must be (nTerm, nSam)")
-        nTerm, nSam = kspha.shape
-        if nTerm not in (9, 16):
-            raise ArgumentError("kspha requires 9 or 16 terms")
-        times = np.asarray(times, dtype=np.float64).reshape(-1)
-        if times.size != nSam:
-            raise DimensionMismatch("times and kspha")
-        nFull = grid.nX * grid.nY * grid.nZ
-        mask = np.ones(nFull, dtype=bool) if mask is None else _fortran_flat(mask).astype(bool)
-        if mask.size != nFull:
-            raise DimensionMismatch("mask and grid")
-        fieldmap = np.zeros(nFull) if fieldmap is None else _fortran_flat(fieldmap).astype(np.float64)
-        if fieldmap.size != nFull:
-            raise DimensionMismatch("fieldmap and mask")
-        if csm is None:
-            csm_flat = np.ones((nFull, 1), dtype=np.complex128)
-        else:
-            csm = np.asarray(csm)
-            nCha_ = csm.shape[-1]
-            if csm.size != nFull * nCha_:
-                raise DimensionMismatch("csm and grid")
-            csm_flat = csm.reshape(nFull, nCha_, order="F").astype(np.complex128)
-        nCha = csm_flat.shape[1]
-        idx = np.flatnonzero(mask)
-        nVox = idx.size
-        if nVox == 0:
-            raise ArgumentError("mask must contain voxels")
-        if nSam <= 0 or nCha <= 0:
-            raise ArgumentError("samples and coils must be positive")
-        if k_nominal is None:
-            k_nominal = kspha[1:4, :]
-        k_nominal = np.asarray(k_nominal, dtype=np.float64)
-        if k_nominal.shape[0] != 3:
-            raise ArgumentError("k_nominal must have 3 terms (row) for kx, ky, kz")
-
-        prepared = prep_kspha(kspha, k_nominal, nTerm, recon_terms)
-        xm, ym, zm = grid.x[idx], grid.y[idx], grid.z[idx]
-        bf = basisfunc_spha(xm, ym, zm, list(range(1, nTerm + 1)))
-        self.derivative_mode = kspha_dt is not None
-        # the derivative mode ignores concomitant terms (array_operator.jl:139)
-        bf, prepared = prep_concomitant(bf, prepared, xm, ym, zm,
-                                        None if self.derivative_mode else concomitant)
-        has_conc = int(prepared.shape[0] != nTerm)
-        kd = kspha_dt if kspha_dt is not None else kdot
-        if kd is not None:
-            kd = np.asfortranarray(kd, dtype=np.float64)
-            if kd.shape != (nTerm, nSam):
-                raise ArgumentError("kspha_dt must have same size as kspha")
-
-        self._keep = dict(
-            mask_idx=np.ascontiguousarray(idx, dtype=np.int32),
-            bf=np.asfortranarray(bf, dtype=np.float64),
-            kspha=np.asfortranarray(prepared, dtype=np.float64),
-            times=np.ascontiguousarray(times),
-            fieldmap=np.ascontiguousarray(fieldmap[idx]),
-            csm=np.asfortranarray(csm_flat[idx, :]),
-            kspha_dt=kd,
-        )
-        k = self._keep
-        desc = _lib.HoeDesc()
-        desc.abi_version = _lib.HOE_ABI_VERSION
-        desc.nX, desc.nY, desc.nZ = grid.nX, grid.nY, grid.nZ
-        desc.nSam, desc.nCha, desc.nTerm = nSam, nCha, nTerm
-        desc.has_concomitant = has_conc
-        desc.nVox = nVox
-        desc.engine = ENGINES[engine]
-        desc.device = device
-        desc.split_hint = int(split_hint)
-        desc.mask_idx = k["mask_idx"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
-        desc.bf = _dptr(k["bf"])
-        desc.kspha = _dptr(k["kspha"])
-        desc.times = _dptr(k["times"])
-        desc.fieldmap = _dptr(k["fieldmap"])
-        desc.csm = k["csm"].ctypes.data_as(ctypes.POINTER(ctypes.c_double))
-        desc.kspha_dt = _dptr(kd)
+        desc, self._keep, meta = build_desc(
+            grid, kspha, times, fieldmap=fieldmap, csm=csm, mask=mask, concomitant=concomitant,
+            recon_terms=recon_terms, k_nominal=k_nominal, kspha_dt=kspha_dt, kdot=kdot,
+            engine=engine, device=device, split_hint=split_hint)
+        self.derivative_mode = meta["derivative_mode"]
+        nSam, nCha, nVox, nTerm = meta["nSam"], meta["nCha"], meta["nVox"], meta["nTerm"]
+        nFull, mask = meta["nFull"], meta["mask"]
         handle = ctypes.c_void_p()
         torch.cuda.init()
         _lib.check(lib.hoe_create(ctypes.byref(handle), ctypes.byref(desc)))
@@ -191,7 +218,7 @@ class ExplicitGB300Op:
         self.device = device
         self.torch_device = torch.device("cuda", device)
         self.nSam, self.nCha, self.nVox, self.nTerm = nSam, nCha, nVox, nTerm
-        self.nTermEff = prepared.shape[0]
+        self.nTermEff = meta["nTermEff"]
         self.nrow = nSam * nCha
         self.ncol = nFull
         self.shape = (self.nrow, self.ncol)

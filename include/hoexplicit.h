@@ -123,6 +123,8 @@ typedef struct hoe_info {
     int32_t tile_samples, tile_voxels;
     int32_t n_sample_tiles, n_voxel_tiles;
     int32_t split_forward, split_adjoint;
+    int32_t residual_rank;         /* dimension r of the reduced residual phase basis */
+    int32_t residual_width;        /* stored width (r rounded up to 8, 12, 16 or 24)  */
     double  residual_phase_bound;  /* max |sum_l dbeta*kappa| in cycles over all tiles */
     int64_t device_bytes;          /* device memory owned by the handle */
 } hoe_info;
@@ -133,6 +135,9 @@ HOE_API int  hoe_abi_version(void);
 
 /* Handle lifetime */
 HOE_API int  hoe_create(hoe_handle **out, const hoe_desc *desc);
+/* Validates a descriptor and reports the operator's host-side plan (tiles,
+ * residual rank/width, residual phase bound) without touching any device. */
+HOE_API int  hoe_plan(const hoe_desc *desc, hoe_info *out);
 HOE_API int  hoe_close(hoe_handle *h);     /* idempotent; later calls return HOE_ERR_CLOSED */
 HOE_API void hoe_free(hoe_handle *h);      /* closes if needed and frees the host object   */
 HOE_API int  hoe_is_closed(const hoe_handle *h);

@@ -36,7 +36,7 @@ def test_version_and_abi():
 def test_struct_layouts_match_header():
     # two int32 blocks followed by pointers / doubles, natural alignment
     assert ctypes.sizeof(_lib.HoeDesc) == 14 * 4 + 7 * 8
-    assert ctypes.sizeof(_lib.HoeInfo) == 12 * 4 + 8 + 8
+    assert ctypes.sizeof(_lib.HoeInfo) == 14 * 4 + 8 + 8
 
 
 def _desc(**over):

@@ -227,6 +227,8 @@ def test_config1_full_size_vs_oracle(engine):
     op.check()  # no bounded device wait ran out
     info = op.info()
     assert info["residual_phase_bound"] < 16.0  # worst-case bound of the FP32 residual phase (cycles)
+    # 2-D slice: solid harmonics through third order span 9 directions, +1 fieldmap
+    assert info["residual_rank"] <= 10 and info["residual_width"] == 12
 
 
 def test_derivative_mode_vs_oracle():
