@@ -13,7 +13,7 @@
 //            B[2s+0,2c] = Re Y, B[2s+0,2c+1] = Im Y, B[2s+1,2c] = Im Y, B[2s+1,2c+1] = -Re Y
 //            so D[v,2c..2c+1] = (Re, Im) of sum_s conj(P[s,v]) Y[s,c]
 //
-// The A operand (the phase tile) never touches global memory: 8 "phase"
+// The A operand (the phase tile) never touches global memory: 16 "phase"
 // warps form it in registers with the anchored FP32 phase of the plain
 // engine (identical arithmetic, see hoe_internal.cuh), split it into BF16
 // hi/lo and store it in shared memory in the no-swizzle K-major canonical
@@ -36,7 +36,7 @@ namespace {
 constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel tile)
 constexpr int TV = 32;              // complex columns per pipeline stage
 constexpr int TK = 2 * TV;          // real K per stage (64 BF16 = 4 UMMA k-steps)
-constexpr int PHASE_WARPS = 8;      // two per TMEM lane quarter, half the stage's columns each
+constexpr int PHASE_WARPS = 16;     // four per TMEM lane quarter, a quarter of the stage's columns each
 constexpr int MMA_WARP = PHASE_WARPS;
 constexpr int LOAD_WARP = PHASE_WARPS + 1;
 constexpr int THREADS = (PHASE_WARPS + 2) * 32;
@@ -172,6 +172,16 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -281,13 +291,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   // first (row tile, chunk) of this CTA; later items advance incrementally
   const int rt0 = (int)(wb / C), ch0 = (int)(wb % C);
   if (warp < PHASE_WARPS) {
-    // ---------------- phase generator: rows x (half of the stage's columns).
-    // After the first stage of group g+1 (or at the end) all 8 warps add
-    // group g's accumulator into register sums (columns split by warp half)
-    // and, at the end of a row tile, write the sums to the partial slot.
+    // ---------------- phase generator: rows x (a quarter of the stage's columns).
+    // After the first stage of group g+1 (or at the end) all 16 warps add
+    // group g's accumulator into register sums (columns split by warp
+    // quarter) and, at the end of a row tile, write the sums to the partial slot.
     const int row = (warp & 3) * 32 + lane;
-    const int half = warp >> 2;
-    constexpr int NA = N / 2;  // accumulator columns owned by this thread
+    const int qcol = warp >> 2;
+    constexpr int NA = N / 4;  // accumulator columns owned by this thread
     float acc[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) acc[i] = 0.f;
@@ -303,7 +313,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       bool got = ok && wait_bar(&segdone[g & 1], (g >> 1) & 1, abort, p.err);
       tc_fence_after();
       if (got) {
-        const uint32_t base = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((g & 1) * N + half * NA);
+        const uint32_t base = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((g & 1) * N + qcol * NA);
         if constexpr (NA % 16 == 0) {
 #pragma unroll
           for (int c0 = 0; c0 < NA; c0 += 16) {
@@ -312,12 +322,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
 #pragma unroll
             for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
           }
-        } else {
-          static_assert(NA == 8, "accumulator columns per thread");
+        } else if constexpr (NA == 8) {
           float v[8];
           tmem_ld8(base, v);
 #pragma unroll
           for (int i = 0; i < 8; ++i) acc[i] += v[i];
+        } else {
+          static_assert(NA == 4, "accumulator columns per thread");
+          float v[4];
+          tmem_ld4(base, v);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) acc[i] += v[i];
         }
       }
       tc_fence_before();
@@ -330,7 +345,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
         if (ok) {
 #pragma unroll
           for (int i = 0; i < NA; i += 2) {
-            int c = (half * NA + i) / 2;
+            int c = (qcol * NA + i) / 2;
             if (c < nOut) dst[c] = make_float2(acc[i], acc[i + 1]);
           }
         }
@@ -376,11 +391,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       unsigned char *aHi = sA + (size_t)slot * 2 * A_TILE_BYTES;
       unsigned char *aLo = aHi + A_TILE_BYTES;
 #pragma unroll 1
-      for (int cc = 0; cc < 4; ++cc) {
-        const int v0 = half * 16 + cc * 4;
-        float ph[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) ph[j] = a + ca[v0 + j];
+      for (int cc = 0; cc < 2; ++cc) {
+        const int v0 = qcol * 8 + cc * 4;
+        const float4 c4 = *reinterpret_cast<const float4 *>(ca + v0);
+        float ph[4] = {a + c4.x, a + c4.y, a + c4.z, a + c4.w};
 #pragma unroll
         for (int q = 0; q < RP / 4; ++q) {
 #pragma unroll
