@@ -95,6 +95,7 @@ void release_device(hoe_handle *h) {
   hoe::tc_release(h);
   auto &t = h->t;
   dfree(t.dbeta); dfree(t.kappa); dfree(t.Atab); dfree(t.Btab); dfree(t.csm);
+  dfree(t.dbHi); dfree(t.dbLo); dfree(t.kpHi); dfree(t.kpLo);
   dfree(t.perm);  dfree(t.bfraw); dfree(t.kdot); dfree(t.times);
   auto &s = h->s;
   dfree(s.Z); dfree(s.Yt); dfree(s.part); dfree(s.gpart); dfree(s.dred);
@@ -189,8 +190,42 @@ struct Plan {
   std::vector<int> order, perm;
   std::vector<double> beta64, gam64, betabar, gambar, kap64;
   std::vector<float> dbeta, kappa, bfraw, kdot, times_f;
+  std::vector<float> dbHi, dbLo, kpHi, kpLo;   // TF32 hi/lo, UMMA K-major tiles
   std::vector<float2> csm;
 };
+
+// Round to the nearest TF32 value (10 explicit mantissa bits, ties to even).
+float tf32_round(float f) {
+  uint32_t b;
+  memcpy(&b, &f, 4);
+  if ((b & 0x7f800000u) != 0x7f800000u) {
+    b += 0x00000fffu + ((b >> 13) & 1u);
+    b &= 0xffffe000u;
+  }
+  memcpy(&f, &b, 4);
+  return f;
+}
+
+// Index of element (row, k) in a K-major no-swizzle TF32 table with KP columns:
+// [row/8][k/4][row%8][k%4].
+inline size_t tf32_index(size_t row, int k, int KP) {
+  return ((row / 8) * (KP / 4) + (size_t)(k / 4)) * 32 + (row % 8) * 4 + (k % 4);
+}
+
+void split_tf32(const std::vector<double> &v, int n, int rank, int KP, size_t nPad,
+                std::vector<float> &hi, std::vector<float> &lo) {
+  hi.assign(nPad * KP, 0.f);
+  lo.assign(nPad * KP, 0.f);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < rank; ++k) {
+      double x = v[(size_t)i * rank + k];
+      float h = tf32_round((float)x);
+      float l = tf32_round((float)(x - (double)h));
+      size_t o = tf32_index((size_t)i, k, KP);
+      hi[o] = h;
+      lo[o] = l;
+    }
+}
 
 int make_plan(const hoe_desc *d, Plan &P) {
   if (!d) return fail(nullptr, HOE_ERR_ARG, "descriptor must not be NULL");
@@ -442,6 +477,9 @@ int make_plan(const hoe_desc *d, Plan &P) {
       kpr[(size_t)s * rank + k] = acc;
       kappa[(size_t)s * Rp + k] = (float)acc;
     }
+  t.KP = rank <= 8 ? 8 : (rank <= 16 ? 16 : 24);
+  split_tf32(dbr, nVox, rank, t.KP, t.nVoxPad, P.dbHi, P.dbLo);
+  split_tf32(kpr, nSam, rank, t.KP, t.nSamPad, P.kpHi, P.kpLo);
   // worst-case residual magnitude over tile pairs (reported)
   {
     std::vector<double> dmx((size_t)t.nVt * rank, 0.0), kmx((size_t)t.nSt * rank, 0.0);
@@ -554,6 +592,10 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
   A(al.alloc(&t.dbeta, dbeta.size()));
   A(al.alloc(&t.kappa, kappa.size()));
+  A(al.alloc(&t.dbHi, P.dbHi.size()));
+  A(al.alloc(&t.dbLo, P.dbLo.size()));
+  A(al.alloc(&t.kpHi, P.kpHi.size()));
+  A(al.alloc(&t.kpLo, P.kpLo.size()));
   A(al.alloc(&t.Atab, (size_t)t.nVt * t.nSamPad));
   A(al.alloc(&t.Btab, (size_t)t.nSt * t.nVoxPad));
   A(al.alloc(&t.csm, csm.size()));
@@ -579,6 +621,10 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   if (e == cudaSuccess) {
     H2D(t.dbeta, dbeta.data(), dbeta.size() * sizeof(float));
     H2D(t.kappa, kappa.data(), kappa.size() * sizeof(float));
+    H2D(t.dbHi, P.dbHi.data(), P.dbHi.size() * sizeof(float));
+    H2D(t.dbLo, P.dbLo.data(), P.dbLo.size() * sizeof(float));
+    H2D(t.kpHi, P.kpHi.data(), P.kpHi.size() * sizeof(float));
+    H2D(t.kpLo, P.kpLo.data(), P.kpLo.size() * sizeof(float));
     H2D(t.csm, csm.data(), csm.size() * sizeof(float2));
     H2D(t.perm, perm.data(), perm.size() * sizeof(int));
     H2D(t.bfraw, bfraw.data(), bfraw.size() * sizeof(float));

@@ -61,6 +61,12 @@ struct Tables {
   float  *Btab  = nullptr;   // [nSt][nVoxPad] frac(beta . gammabar)
   float2 *csm   = nullptr;   // [nVoxPad][nChaPad]
   int    *perm  = nullptr;   // [nVoxPad] linear grid index, -1 for padding
+  // TF32 hi/lo copies of the reduced residual vectors for the tensor-core
+  // phase MMA, in UMMA K-major no-swizzle layout: 8-row groups of KP/4 core
+  // matrices (8 rows x 4 TF32 each); width KP = rank rounded up to 8, 16 or 24
+  int    KP = 0;
+  float  *dbHi = nullptr, *dbLo = nullptr;  // [nVoxPad/8][KP/4][8][4]
+  float  *kpHi = nullptr, *kpLo = nullptr;  // [nSamPad/8][KP/4][8][4]
   float  *bfraw = nullptr;   // [nVoxPad][kRF] bf (R0 terms) and fieldmap at slot R0
   float  *kdot  = nullptr;   // [nSamPad][kRF] kspha_dt (nTerm terms), zero elsewhere
   float  *times = nullptr;   // [nSamPad]

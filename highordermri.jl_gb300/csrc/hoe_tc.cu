@@ -13,14 +13,19 @@
 //            B[2s+0,2c] = Re Y, B[2s+0,2c+1] = Im Y, B[2s+1,2c] = Im Y, B[2s+1,2c+1] = -Re Y
 //            so D[v,2c..2c+1] = (Re, Im) of sum_s conj(P[s,v]) Y[s,c]
 //
-// The A operand (the phase tile) never touches global memory: 16 "phase"
-// warps form it in registers with the anchored FP32 phase of the plain
-// engine (identical arithmetic, see hoe_internal.cuh), split it into BF16
-// hi/lo and store it in shared memory in the no-swizzle K-major canonical
-// layout.  A loader warp streams the pre-tiled B operand and the per-stage
-// phase inputs with cp.async.bulk (TMA bulk copies) onto mbarriers; one
-// thread of the MMA warp issues tcgen05.mma and commits stage completion
-// back to the producers.  Every mbarrier wait is bounded in time: on
+// The A operand (the phase tile) never touches global or shared memory.  Per
+// stage of 64 columns the MMA thread first computes the residual phase
+// dbeta.kappa of the 128 x 64 tile on the tensor cores (TF32, 3 products of
+// hi/lo splits made at create time, K = reduced rank) into a TMEM tile, a
+// few stages ahead; 16 "phase" warps read it, add the FP32 anchors (see
+// hoe_internal.cuh), range-reduce, take the FP32 sincos, split the result
+// into BF16 hi/lo and write both into a TMEM A tile with tcgen05.st (lane =
+// row, one 32-bit column = one (re, im) pair).  A loader warp streams the
+// pre-tiled B operand, the TF32 residual tiles and the anchors with
+// cp.async.bulk (TMA bulk copies) onto mbarriers; the MMA thread issues the
+// contraction with A from TMEM and B from shared memory (3 BF16 products)
+// into a double-buffered FP32 TMEM accumulator that is flushed every GROUP
+// stages into FP32 register sums.  Every mbarrier wait is bounded in time: on
 // timeout the kernel records HOE_ERR_TIMEOUT in a device word, stops
 // issuing work, waits (bounded) for its own copies and MMAs and frees TMEM.
 #include <cuda_bf16.h>
@@ -34,8 +39,8 @@ namespace hoe {
 namespace {
 
 constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel tile)
-constexpr int TV = 32;              // complex columns per pipeline stage
-constexpr int TK = 2 * TV;          // real K per stage (64 BF16 = 4 UMMA k-steps)
+constexpr int TV = 64;              // complex columns per pipeline stage
+constexpr int TK = 2 * TV;          // real K per stage (128 BF16 = 8 UMMA k-steps)
 constexpr int PHASE_WARPS = 16;     // four per TMEM lane quarter, a quarter of the stage's columns each
 constexpr int MMA_WARP = PHASE_WARPS;
 constexpr int LOAD_WARP = PHASE_WARPS + 1;
@@ -43,11 +48,10 @@ constexpr int THREADS = (PHASE_WARPS + 2) * 32;
 constexpr float kTwoPi = 6.28318530717958647692f;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
 
-constexpr int A_TILE_BYTES = TM * TK * 2;    // one BF16 A tile (hi or lo): 16 KB
-// The tensor-core FP32 accumulator sums at most GROUP chunks (GROUP*12 MMAs)
+// The tensor-core FP32 accumulator sums at most GROUP stages (GROUP*24 MMAs)
 // before it is added, in round-to-nearest FP32, into register sums: long
 // accumulation chains in TMEM lose accuracy on coherent sums.
-constexpr int GROUP = 16;
+constexpr int GROUP = 8;
 
 // byte offset of element (r, k) in a no-swizzle K-major tile with K = TK:
 // core matrices of 8 rows x 16 B; cores adjacent in K are 128 B apart (LBO),
@@ -55,8 +59,8 @@ constexpr int GROUP = 16;
 __host__ __device__ constexpr uint32_t kmajor_off(int r, int k) {
   return (uint32_t)((r / 8) * (TK / 8) * 128 + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2);
 }
-constexpr uint32_t LBO = 128;
-constexpr uint32_t SBO = (TK / 8) * 128;
+constexpr uint32_t LBO = 128;                 // K-direction core stride (all tiles)
+constexpr uint32_t SBO = (TK / 8) * 128;      // 8-row group stride of the BF16 tiles
 
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   // D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12), K-major, N>>3 at 17, M>>4 at 24
@@ -67,9 +71,16 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  // D = F32, A = B = TF32 (2 at bits 7-9, 10-12), K-major, N>>3 at 17, M>>4 at 24
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Shared-memory matrix descriptor, no swizzle: start address, LBO (K step of
+// core matrices), SBO (step of 8-row groups), descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo = SBO) {
   return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(LBO >> 4) << 16) |
-         ((uint64_t)(SBO >> 4) << 32) | (1ull << 46);
+         ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
 }
 
 __device__ __forceinline__ uint64_t globaltimer() {
@@ -89,21 +100,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// try_wait with a suspend-time hint: a waiting thread sleeps until the phase
+// completes (or the hint elapses) instead of spinning on issue slots.
+constexpr uint32_t kSuspendNs = 200000;
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait; returns false on timeout or when another role aborted.
 __device__ __noinline__ bool wait_bar_slow(uint64_t *bar, uint32_t parity, volatile int *abort,
                                            int *gerr) {
-  uint64_t t0 = 0;
-  for (uint32_t n = 0;; ++n) {
-    if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (;;) {
+    if (mbar_try_wait_sleep(bar, parity)) return true;
     if (*abort) return false;
-    if ((n & 255) == 255) {
-      uint64_t t = globaltimer();
-      if (t0 == 0) t0 = t;
-      else if (t - t0 > kWaitNs) {
-        *abort = 1;
-        atomicExch(gerr, HOE_ERR_TIMEOUT);
-        return false;
-      }
+    if (globaltimer() - t0 > kWaitNs) {
+      *abort = 1;
+      atomicExch(gerr, HOE_ERR_TIMEOUT);
+      return false;
     }
   }
 }
@@ -117,7 +138,7 @@ __device__ __forceinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatil
 // Bounded wait that ignores the abort flag (used to drain in-flight work).
 __device__ __noinline__ bool drain_bar(uint64_t *bar, uint32_t parity) {
   uint64_t t0 = globaltimer();
-  while (!mbar_try_wait(bar, parity))
+  while (!mbar_try_wait_sleep(bar, parity))
     if (globaltimer() - t0 > kWaitNs) return false;
   return true;
 }
@@ -146,6 +167,29 @@ __device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bd
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+// D += A(TMEM) * B(SMEM)^T, kind::f16
+__device__ __forceinline__ void umma_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(dtmem),
+      "r"(atmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t *w) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7]), "r"(w[8]),
+      "r"(w[9]), "r"(w[10]), "r"(w[11]), "r"(w[12]), "r"(w[13]), "r"(w[14]), "r"(w[15])
+      : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
   asm volatile(
@@ -199,17 +243,17 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
 }
 
 struct TcParams {
-  const float *rowvec;     // [nRowPad][RP]: kappa (forward) / dbeta (adjoint)
-  const float *rowAnchor;  // [colTile][rowAnchorStride]: Atab (forward) / Btab (adjoint)
-  const float *colvec;     // [nColPad][RP]: dbeta (forward) / kappa (adjoint)
-  const float *colAnchor;  // [rowTile][colAnchorStride]: Btab (forward) / Atab (adjoint)
-  const uint16_t *Bop;     // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
-  float2 *part;            // [slot][nRowPad][nChaPad] partial sums (zeroed before launch)
+  const float *rowHi, *rowLo;   // TF32 row-side residual tables: kappa (forward) / dbeta (adjoint)
+  const float *colHi, *colLo;   // TF32 column-side residual tables: dbeta (forward) / kappa (adjoint)
+  const float *rowAnchor;       // [colTile][rowAnchorStride]: Atab (forward) / Btab (adjoint)
+  const float *colAnchor;       // [rowTile][colAnchorStride]: Btab (forward) / Atab (adjoint)
+  const uint16_t *Bop;          // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
+  float2 *part;                 // [slot][nRowPad][nChaPad] partial sums (zeroed before launch)
   int *err;
   int rowAnchorStride, colAnchorStride;
   int nRowPad, nChaPad, nChaTC;
-  int nColChunks;          // column chunks per row tile (C)
-  int64_t work;            // nRowTiles * C work items, split evenly over gridDim.x CTAs
+  int nColChunks;               // column chunks per row tile (C)
+  int64_t work;                 // nRowTiles * C work items, split evenly over gridDim.x CTAs
 };
 
 // CTA that owns work item w when W items are split into G contiguous ranges
@@ -218,58 +262,106 @@ __host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
   return (int)(((w + 1) * (int64_t)G - 1) / W);
 }
 
+// Tensor-memory plan (512 columns): BF16 phase tiles ABUF x [hi TV | lo TV]
+// columns (one 32-bit column per complex element), residual-phase tiles
+// PD x TV FP32 columns, accumulators 2 x N FP32 columns.
+template <int N>
+struct Tmem {
+  static constexpr int ABUF = N <= 64 ? 2 : 1;
+  static constexpr int PD_MAX = (512 - 2 * N - ABUF * 2 * TV) / TV;
+  static constexpr uint32_t A_COL = 0;
+  static constexpr uint32_t P_COL = ABUF * 2 * TV;
+};
+
 // Shared-memory plan (dynamic, 1024-byte aligned base):
-//   A    [NS][2][A_TILE_BYTES]        phase tile hi / lo
-//   B    [NS][2][N*TK*2]              B operand hi / lo
-//   CV   [NS][TV][RP] float           column phase vectors
-//   CA   [NS][TV] float               column anchors
-//   bars full[NS], afull[NS], empty[NS], segdone[2], tmemfree[2]; tmem base; abort flag
-template <int N, int RP, int NS>
+//   B   [NS][hi,lo]   BF16 contraction operand, N x TK
+//   CV  [NS][hi,lo]   TF32 column residual tile, TV x KP
+//   RV  [2][hi,lo]    TF32 row residual tile, 128 x KP (one per row-tile parity)
+//   CA  [NS][TV]      column anchors
+//   barriers: full[NS] empty[NS] afull[ABUF] aempty[ABUF] segdone[2]
+//             tmemfree[2] pfull[PD] pfree[PD] rfull[2] rfree[2]
+// The residual-phase tile of stage i+PD is issued right after the
+// contraction of stage i, PD <= NS-1 stages ahead of its use (the loader ring
+// of NS stages allows no more without a dependency cycle).
+template <int N, int KP, int NS>
 struct Smem {
+  static constexpr int ABUF = Tmem<N>::ABUF;
+  static constexpr int PD = (NS - 1) < Tmem<N>::PD_MAX ? (NS - 1) : Tmem<N>::PD_MAX;
   static constexpr int B_TILE = N * TK * 2;
-  static constexpr size_t A_OFF = 0;
-  static constexpr size_t B_OFF = A_OFF + (size_t)NS * 2 * A_TILE_BYTES;
+  static constexpr int CV_TILE = TV * KP * 4;
+  static constexpr int RV_TILE = TM * KP * 4;
+  static constexpr size_t B_OFF = 0;
   static constexpr size_t CV_OFF = B_OFF + (size_t)NS * 2 * B_TILE;
-  static constexpr size_t CA_OFF = CV_OFF + (size_t)NS * TV * RP * 4;
+  static constexpr size_t RV_OFF = CV_OFF + (size_t)NS * 2 * CV_TILE;
+  static constexpr size_t CA_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
   static constexpr size_t BAR_OFF = (CA_OFF + (size_t)NS * TV * 4 + 7) / 8 * 8;
-  static constexpr size_t MISC_OFF = BAR_OFF + (size_t)(3 * NS + 4) * 8;
+  static constexpr int NBAR = 2 * NS + 2 * ABUF + 8 + 2 * PD;
+  static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
 
-template <int N, int RP, int NS>
+template <int N, int KP>
+constexpr int pick_stages() {
+  return Smem<N, KP, 6>::BYTES <= 227 * 1024 ? 6
+       : Smem<N, KP, 5>::BYTES <= 227 * 1024 ? 5
+       : Smem<N, KP, 4>::BYTES <= 227 * 1024 ? 4
+       : Smem<N, KP, 3>::BYTES <= 227 * 1024 ? 3 : 2;
+}
+
+template <int N, int KP, int NS>
 __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
-  using S = Smem<N, RP, NS>;
+  using S = Smem<N, KP, NS>;
+  constexpr int ABUF = S::ABUF, PD = S::PD;
+  static_assert(PD >= 1, "residual-phase look-ahead");
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char *sA = smem + S::A_OFF;
   unsigned char *sB = smem + S::B_OFF;
-  float *sCV = reinterpret_cast<float *>(smem + S::CV_OFF);
+  unsigned char *sCV = smem + S::CV_OFF;
+  unsigned char *sRV = smem + S::RV_OFF;
   float *sCA = reinterpret_cast<float *>(smem + S::CA_OFF);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
-  uint64_t *afull = full + NS;
-  uint64_t *empty = afull + NS;
-  uint64_t *segdone = empty + NS;   // [2]: accumulator buffer b complete (group of chunks)
-  uint64_t *tmemfree = segdone + 2; // [2]: accumulator buffer b read out
+  uint64_t *empty = full + NS;        // B-ring stage consumed by the contraction MMAs
+  uint64_t *afull = empty + NS;       // [ABUF] TMEM phase tile written (16 phase warps)
+  uint64_t *aempty = afull + ABUF;    // [ABUF] TMEM phase tile consumed by the MMAs
+  uint64_t *segdone = aempty + ABUF;  // [2] accumulator buffer complete (group of stages)
+  uint64_t *tmemfree = segdone + 2;   // [2] accumulator buffer read out
+  uint64_t *pfull = tmemfree + 2;     // [PD] residual-phase TMEM tile computed
+  uint64_t *pfree = pfull + PD;       // [PD] residual-phase TMEM tile read out
+  uint64_t *rfull = pfree + PD;       // [2] row residual tile loaded
+  uint64_t *rfree = rfull + 2;        // [2] row residual tile no longer read by MMAs
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::MISC_OFF);
   volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
-  // two accumulator buffers of N FP32 columns
-  constexpr uint32_t TMEM_COLS = 2 * N <= 32 ? 32 : (2 * N <= 64 ? 64 : (2 * N <= 128 ? 128 : 256));
+  constexpr uint32_t TMEM_COLS = 512;
+  constexpr uint32_t A_COL = Tmem<N>::A_COL, P_COL = Tmem<N>::P_COL;
+  constexpr uint32_t ACC_COL = P_COL + PD * TV;
+  static_assert(ACC_COL + 2 * N <= TMEM_COLS, "tensor memory plan");
+  constexpr uint32_t SBO_TF32 = (KP / 4) * 128;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int C = p.nColChunks;
   const int G = gridDim.x, b = blockIdx.x;
   const int64_t wb = (int64_t)b * p.work / G, we = (int64_t)(b + 1) * p.work / G;
   const int nIter = (int)(we - wb);
+  const int rt0 = (int)(wb / C), ch0 = (int)(wb % C);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NS; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&afull[i], PHASE_WARPS);
       mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < ABUF; ++i) {
+      mbar_init(&afull[i], PHASE_WARPS);
+      mbar_init(&aempty[i], 1);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&segdone[i], 1);
       mbar_init(&tmemfree[i], PHASE_WARPS);
+      mbar_init(&rfull[i], 1);
+      mbar_init(&rfree[i], 1);
+    }
+    for (int i = 0; i < PD; ++i) {
+      mbar_init(&pfull[i], 1);
+      mbar_init(&pfree[i], PHASE_WARPS);
     }
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -285,24 +377,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  // Work item w = (row tile w / C, chunk w % C).  A "group" is a run of at
-  // most GROUP consecutive chunks of one row tile; group g accumulates into
-  // TMEM buffer g & 1.
-  // first (row tile, chunk) of this CTA; later items advance incrementally
-  const int rt0 = (int)(wb / C), ch0 = (int)(wb % C);
   if (warp < PHASE_WARPS) {
-    // ---------------- phase generator: rows x (a quarter of the stage's columns).
+    // ---------------- phase generator: one row x 16 columns of each stage.
     // After the first stage of group g+1 (or at the end) all 16 warps add
     // group g's accumulator into register sums (columns split by warp
     // quarter) and, at the end of a row tile, write the sums to the partial slot.
     const int row = (warp & 3) * 32 + lane;
     const int qcol = warp >> 2;
+    const uint32_t laneBase = (uint32_t)((warp & 3) * 32) << 16;
     constexpr int NA = N / 4;  // accumulator columns owned by this thread
     float acc[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) acc[i] = 0.f;
-    float rv[RP];
-    int curRT = -1, curTile = -1, grp = -1, grow = 0;
+    int curRT = -1, curTile = -1, grp = -1;
     int pendGrp = -1, pendRT = -1;
     bool pendLast = false;
     float a = 0.f;
@@ -313,7 +400,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       bool got = ok && wait_bar(&segdone[g & 1], (g >> 1) & 1, abort, p.err);
       tc_fence_after();
       if (got) {
-        const uint32_t base = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((g & 1) * N + qcol * NA);
+        const uint32_t base = tmem + laneBase + ACC_COL + (uint32_t)((g & 1) * N + qcol * NA);
         if constexpr (NA % 16 == 0) {
 #pragma unroll
           for (int c0 = 0; c0 < NA; c0 += 16) {
@@ -361,19 +448,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
     for (int it = 0; it < nIter && ok; ++it, ++ch) {
       if (ch == C) { ch = 0; ++rt; }
       if (it == 0 || ch % GROUP == 0) ++grp;
-      if (rt != curRT) {
-        curRT = rt;
-        curTile = -1;
-        grow = rt * TM + row;
-#pragma unroll
-        for (int l = 0; l < RP; l += 4) {
-          float4 v = *reinterpret_cast<const float4 *>(p.rowvec + (int64_t)grow * RP + l);
-          rv[l] = v.x; rv[l + 1] = v.y; rv[l + 2] = v.z; rv[l + 3] = v.w;
-        }
-      }
+      if (rt != curRT) { curRT = rt; curTile = -1; }
       const int slot = it % NS, round = it / NS;
-      const int col0 = ch * TV;
-      const int colTile = col0 / 128;
+      const int colTile = ch * TV / 128;
       if (colTile != curTile) {
         a = aNext;
         curTile = colTile;
@@ -384,46 +461,46 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
         if (it + 1 < nIter && (nrt != rt || nch * TV / 128 != colTile))
           aNext = p.rowAnchor[(int64_t)(nch * TV / 128) * p.rowAnchorStride + nrt * TM + row];
       }
-      if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) { ok = false; break; }
+      // residual phase of this stage (TMEM), then release its buffer
+      const int pb = it % PD, pr = it / PD;
+      if (!wait_bar(&pfull[pb], pr & 1, abort, p.err)) { ok = false; break; }
+      tc_fence_after();
+      float d[16];
+      tmem_ld16(tmem + laneBase + P_COL + (uint32_t)(pb * TV + qcol * 16), d);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&pfree[pb]);
+      // column anchors of this stage
       if (!wait_bar(&full[slot], round & 1, abort, p.err)) { ok = false; break; }
-      const float *cv = sCV + slot * TV * RP;
-      const float *ca = sCA + slot * TV;
-      unsigned char *aHi = sA + (size_t)slot * 2 * A_TILE_BYTES;
-      unsigned char *aLo = aHi + A_TILE_BYTES;
-#pragma unroll 1
-      for (int cc = 0; cc < 2; ++cc) {
-        const int v0 = qcol * 8 + cc * 4;
-        const float4 c4 = *reinterpret_cast<const float4 *>(ca + v0);
-        float ph[4] = {a + c4.x, a + c4.y, a + c4.z, a + c4.w};
+      const float *ca = sCA + slot * TV + qcol * 16;
+      uint32_t hi[16], lo[16];
 #pragma unroll
-        for (int q = 0; q < RP / 4; ++q) {
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            float4 d = reinterpret_cast<const float4 *>(cv + (v0 + j) * RP)[q];
-            ph[j] = fmaf(rv[4 * q], d.x, ph[j]);
-            ph[j] = fmaf(rv[4 * q + 1], d.y, ph[j]);
-            ph[j] = fmaf(rv[4 * q + 2], d.z, ph[j]);
-            ph[j] = fmaf(rv[4 * q + 3], d.w, ph[j]);
-          }
-        }
-        uint32_t hi[4], lo[4];
+      for (int cc = 0; cc < 4; ++cc) {
+        const float4 c4 = *reinterpret_cast<const float4 *>(ca + cc * 4);
+        const float cav[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          float f = ph[j] - rintf(ph[j]);
+          float ph = (a + cav[j]) + d[cc * 4 + j];
+          float f = ph - rintf(ph);
           float sn, cs;
           __sincosf(kTwoPi * f, &sn, &cs);
           __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
           float2 hf = __bfloat1622float2(h);
-          hi[j] = *reinterpret_cast<uint32_t *>(&h);
-          lo[j] = pack_bf16(cs - hf.x, sn - hf.y);
+          hi[cc * 4 + j] = *reinterpret_cast<uint32_t *>(&h);
+          lo[cc * 4 + j] = pack_bf16(cs - hf.x, sn - hf.y);
         }
-        const uint32_t off = kmajor_off(row, 2 * v0);
-        *reinterpret_cast<uint4 *>(aHi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4 *>(aLo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      // TMEM phase tile buffer: free once the contraction of stage it-ABUF is done
+      const int ab = it % ABUF, ar = it / ABUF;
+      if (ar > 0 && !wait_bar(&aempty[ab], (ar - 1) & 1, abort, p.err)) { ok = false; break; }
+      tc_fence_after();
+      const uint32_t aBase = tmem + laneBase + A_COL + (uint32_t)(ab * 2 * TV + qcol * 16);
+      tmem_st16(aBase, hi);
+      tmem_st16(aBase + TV, lo);
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&afull[slot]);
+      if (lane == 0) mbar_arrive(&afull[ab]);
       // the previous group is flushed one stage late, so its MMAs are done by now
       if (pendGrp >= 0) flush();
       const bool endRT = (it == nIter - 1) || (ch + 1 == C);
@@ -435,62 +512,111 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
     }
     if (pendGrp >= 0) flush();
   } else if (warp == MMA_WARP) {
-    // ---------------- MMA issuer (one thread)
+    // ---------------- MMA issuer (one thread): the contraction of stage it,
+    // then the residual-phase tile of stage it+PD
     if (lane == 0 && nIter > 0) {
-      constexpr uint32_t idesc = idesc_bf16(TM, N);
-      int issued = 0, grp = -1;
-      int ch = ch0;
-      for (int it = 0; it < nIter; ++it, ++ch) {
+      constexpr uint32_t idescC = idesc_bf16(TM, N);
+      constexpr uint32_t idescP = idesc_tf32(TM, TV);
+      bool alive = true;
+      uint64_t *lastBar = nullptr;  // barrier of the most recent commit (for draining)
+      uint32_t lastPar = 0;
+      auto issue_phase = [&](int j) -> bool {
+        const int64_t w = wb + j;
+        const int kj = (int)(w / C) - rt0;
+        const bool lastOfRow = (j == nIter - 1) || ((w + 1) % C == 0);
+        const int s = j % NS, r = j / NS;
+        if (!wait_bar(&full[s], r & 1, abort, p.err)) return false;
+        if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) return false;
+        const int pb = j % PD, pr = j / PD;
+        if (j >= PD && !wait_bar(&pfree[pb], (pr - 1) & 1, abort, p.err)) return false;
+        tc_fence_after();
+        const uint32_t dt = tmem + P_COL + (uint32_t)(pb * TV);
+        const uint32_t rHi = smem_u32(sRV + (size_t)(kj & 1) * 2 * S::RV_TILE);
+        const uint32_t rLo = rHi + S::RV_TILE;
+        const uint32_t cHi = smem_u32(sCV + (size_t)s * 2 * S::CV_TILE);
+        const uint32_t cLo = cHi + S::CV_TILE;
+#pragma unroll
+        for (int ks = 0; ks < KP / 8; ++ks) {
+          const uint32_t ko = ks * 2 * LBO;  // 8 TF32 = two core matrices along K
+          umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, ks ? 1u : 0u);
+          umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
+          umma_tf32(dt, umma_desc(rLo + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
+        }
+        umma_commit(&pfull[pb]);
+        lastBar = &pfull[pb];
+        lastPar = pr & 1;
+        if (lastOfRow) umma_commit(&rfree[kj & 1]);
+        return true;
+      };
+      for (int j = 0; j < PD && j < nIter && alive; ++j) alive = issue_phase(j);
+      int grp = -1, ch = ch0;
+      for (int it = 0; it < nIter && alive; ++it, ++ch) {
         if (ch == C) ch = 0;
         const bool first = (it == 0) || (ch % GROUP == 0);
         if (first) {
           ++grp;
-          // buffer grp&1 was last used by group grp-2: wait until it was read out
+          // accumulator buffer grp&1 was last used by group grp-2: wait until it was read out
           if (grp >= 2 && !wait_bar(&tmemfree[grp & 1], ((grp >> 1) - 1) & 1, abort, p.err)) break;
         }
         const bool last = (it == nIter - 1) || (ch + 1 == C) || ((ch + 1) % GROUP == 0);
         const int slot = it % NS, round = it / NS;
-        if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
-        if (!wait_bar(&afull[slot], round & 1, abort, p.err)) break;
+        const int ab = it % ABUF, ar = it / ABUF;
+        if (!wait_bar(&afull[ab], ar & 1, abort, p.err)) break;
         tc_fence_after();
-        const uint32_t dt = tmem + (uint32_t)((grp & 1) * N);
-        const uint32_t aHi = smem_u32(sA + (size_t)slot * 2 * A_TILE_BYTES);
-        const uint32_t aLo = aHi + A_TILE_BYTES;
+        const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp & 1) * N);
+        const uint32_t aHi = tmem + A_COL + (uint32_t)(ab * 2 * TV);
+        const uint32_t aLo = aHi + TV;
         const uint32_t bHi = smem_u32(sB + (size_t)slot * 2 * S::B_TILE);
         const uint32_t bLo = bHi + S::B_TILE;
 #pragma unroll
         for (int ks = 0; ks < TK / 16; ++ks) {
-          const uint32_t ko = ks * 2 * LBO;  // 16 BF16 = two core matrices along K
-          umma(dt, umma_desc(aHi + ko), umma_desc(bHi + ko), idesc, (first && ks == 0) ? 0u : 1u);
-          umma(dt, umma_desc(aHi + ko), umma_desc(bLo + ko), idesc, 1u);
-          umma(dt, umma_desc(aLo + ko), umma_desc(bHi + ko), idesc, 1u);
+          const uint32_t ka = ks * 8;        // 16 BF16 = 8 TMEM columns
+          const uint32_t kb = ks * 2 * LBO;  // 16 BF16 = two core matrices along K
+          umma_ta(dt, aHi + ka, umma_desc(bHi + kb), idescC, (first && ks == 0) ? 0u : 1u);
+          umma_ta(dt, aHi + ka, umma_desc(bLo + kb), idescC, 1u);
+          umma_ta(dt, aLo + ka, umma_desc(bHi + kb), idescC, 1u);
         }
         umma_commit(&empty[slot]);
+        umma_commit(&aempty[ab]);
+        lastBar = &aempty[ab];
+        lastPar = ar & 1;
+        (void)round;
         if (last) umma_commit(&segdone[grp & 1]);
-        issued = it + 1;
+        if (it + PD < nIter) alive = issue_phase(it + PD);
       }
-      if (issued != nIter && issued > 0) {
+      if (*abort && lastBar) {
         // aborted: let the MMAs already issued finish before TMEM is freed
-        const int lastIt = issued - 1;
-        drain_bar(&empty[lastIt % NS], (lastIt / NS) & 1);
+        drain_bar(lastBar, lastPar);
       }
     }
     __syncwarp();
   } else {
-    // ---------------- loader (one thread): B tiles + column phase inputs
+    // ---------------- loader (one thread): row residual tiles per row tile,
+    // per stage the B tiles, column residual tiles and column anchors
     if (lane == 0) {
-      const uint32_t bBytes = 2 * S::B_TILE, cvBytes = TV * RP * 4, caBytes = TV * 4;
-      int issued = 0;
+      const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + TV * 4;
+      int issued = 0, kcount = -1, rowIssued = -1;
       int rt = rt0, ch = ch0;
       for (int it = 0; it < nIter; ++it, ++ch) {
         if (ch == C) { ch = 0; ++rt; }
+        if (it == 0 || ch == 0) {
+          ++kcount;
+          const int rb = kcount & 1;
+          if (kcount >= 2 && !wait_bar(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err)) break;
+          mbar_expect_tx(&rfull[rb], 2 * S::RV_TILE);
+          const size_t ro = (size_t)rt * TM * KP;
+          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE, p.rowHi + ro, S::RV_TILE, &rfull[rb]);
+          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE + S::RV_TILE, p.rowLo + ro, S::RV_TILE, &rfull[rb]);
+          rowIssued = kcount;
+        }
         const int slot = it % NS, round = it / NS;
         if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
-        const int col0 = ch * TV;
-        mbar_expect_tx(&full[slot], bBytes + cvBytes + caBytes);
-        bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, p.Bop + (size_t)ch * 2 * (N * TK), bBytes, &full[slot]);
-        bulk_g2s(sCV + slot * TV * RP, p.colvec + (size_t)col0 * RP, cvBytes, &full[slot]);
-        bulk_g2s(sCA + slot * TV, p.colAnchor + (int64_t)rt * p.colAnchorStride + col0, caBytes,
+        const size_t co = (size_t)ch * TV * KP;
+        mbar_expect_tx(&full[slot], stageBytes);
+        bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, p.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
+        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, p.colHi + co, S::CV_TILE, &full[slot]);
+        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, p.colLo + co, S::CV_TILE, &full[slot]);
+        bulk_g2s(sCA + slot * TV, p.colAnchor + (int64_t)rt * p.colAnchorStride + ch * TV, TV * 4,
                  &full[slot]);
         issued = it + 1;
       }
@@ -498,6 +624,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
         // drain the copies still in flight into this CTA's shared memory
         for (int it = max(0, issued - NS); it < issued; ++it)
           drain_bar(&full[it % NS], (it / NS) & 1);
+        if (rowIssued >= 0) drain_bar(&rfull[rowIssued & 1], (rowIssued >> 1) & 1);
       }
     }
     __syncwarp();
@@ -557,74 +684,69 @@ int tc_ncha(int nCha) {
   return n;  // 8, 16, 32 or 64 coils per MMA: N = 16, 32, 64, 128
 }
 
-template <int N, int RP>
+template <int N, int KP>
 struct Kern {
-  static constexpr int NS = N <= 64 ? 4 : 3;
-  using S = Smem<N, RP, NS>;
+  static constexpr int NS = pick_stages<N, KP>();
+  static_assert(Smem<N, KP, NS>::PD >= 1, "residual-phase look-ahead");
+  using S = Smem<N, KP, NS>;
   static_assert(S::BYTES <= 227 * 1024, "shared memory plan exceeds 227 KB");
-  static void *fn() { return (void *)k_tc_contract<N, RP, NS>; }
 };
 
-template <int N, int RP>
+template <int N, int KP>
 cudaError_t launch_contract(const hoe_handle *h, const TcParams &p, int G, cudaStream_t st) {
-  using K = Kern<N, RP>;
-  auto kern = k_tc_contract<N, RP, K::NS>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES);
-  if (e != cudaSuccess) return e;
+  using K = Kern<N, KP>;
+  auto kern = k_tc_contract<N, KP, K::NS>;
   kern<<<G, THREADS, K::S::BYTES, st>>>(p);
   h->launches += 1;
   return cudaGetLastError();
 }
 
-// resident CTAs per SM of the instantiation for (N, RP)
-template <int N, int RP>
-int blocks_per_sm() {
-  using K = Kern<N, RP>;
-  auto kern = k_tc_contract<N, RP, K::NS>;
+// One-time per (process, instantiation): shared-memory limit; returns the
+// resident CTAs per SM.
+template <int N, int KP>
+int configure() {
+  using K = Kern<N, KP>;
+  auto kern = k_tc_contract<N, KP, K::NS>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES) != cudaSuccess)
-    return 1;
+    return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, THREADS, K::S::BYTES) != cudaSuccess || nb < 1)
-    nb = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, THREADS, K::S::BYTES) != cudaSuccess) return 0;
   return nb;
 }
 
-
-template <int RP>
-cudaError_t dispatch_n(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
+template <int KP>
+cudaError_t launch_n(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
   switch (N) {
-    case 16: return launch_contract<16, RP>(h, p, G, st);
-    case 32: return launch_contract<32, RP>(h, p, G, st);
-    case 64: return launch_contract<64, RP>(h, p, G, st);
-    default: return launch_contract<128, RP>(h, p, G, st);
+    case 16: return launch_contract<16, KP>(h, p, G, st);
+    case 32: return launch_contract<32, KP>(h, p, G, st);
+    case 64: return launch_contract<64, KP>(h, p, G, st);
+    default: return launch_contract<128, KP>(h, p, G, st);
   }
 }
 
-cudaError_t dispatch(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
-  switch (h->t.Rp) {
-    case 8: return dispatch_n<8>(h, p, N, G, st);
-    case 12: return dispatch_n<12>(h, p, N, G, st);
-    case 16: return dispatch_n<16>(h, p, N, G, st);
-    default: return dispatch_n<24>(h, p, N, G, st);
+cudaError_t launch(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
+  switch (h->t.KP) {
+    case 8: return launch_n<8>(h, p, N, G, st);
+    case 16: return launch_n<16>(h, p, N, G, st);
+    default: return launch_n<24>(h, p, N, G, st);
   }
 }
 
-template <int RP>
-int bps_n(int N) {
+template <int KP>
+int configure_n(int N) {
   switch (N) {
-    case 16: return blocks_per_sm<16, RP>();
-    case 32: return blocks_per_sm<32, RP>();
-    case 64: return blocks_per_sm<64, RP>();
-    default: return blocks_per_sm<128, RP>();
+    case 16: return configure<16, KP>();
+    case 32: return configure<32, KP>();
+    case 64: return configure<64, KP>();
+    default: return configure<128, KP>();
   }
 }
 
-int bps(int Rp, int N) {
-  switch (Rp) {
-    case 8: return bps_n<8>(N);
-    case 12: return bps_n<12>(N);
-    case 16: return bps_n<16>(N);
-    default: return bps_n<24>(N);
+int configure_kernel(int KP, int N) {
+  switch (KP) {
+    case 8: return configure_n<8>(N);
+    case 16: return configure_n<16>(N);
+    default: return configure_n<24>(N);
   }
 }
 
@@ -672,8 +794,10 @@ cudaError_t tc_prepare(hoe_handle *h) {
   TcBuffers b;
   b.nChaTC = tc_ncha(t.nCha);
   b.N = 2 * b.nChaTC;
+  const int bps = configure_kernel(t.KP, b.N);
+  if (bps < 1) return cudaErrorInvalidConfiguration;
   const int chunksF = t.nVoxPad / TV, chunksA = t.nSamPad / TV;
-  const int G = h->numSMs * bps(t.Rp, b.N);
+  const int G = h->numSMs * bps;
   b.gridF = (int)std::min<int64_t>(G, (int64_t)t.nSt * chunksF);
   b.gridA = (int)std::min<int64_t>(G, (int64_t)t.nVt * chunksA);
   b.slotsF = max_slots(t.nSt, chunksF, b.gridF);
@@ -725,10 +849,10 @@ cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const flo
   k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Z, b.bopF, chunks, b.N, t.nChaPad);
   h->launches += 1;
   TcParams p = base_params(h, b);
-  p.rowvec = t.kappa;
+  p.rowHi = t.kpHi; p.rowLo = t.kpLo;
+  p.colHi = t.dbHi; p.colLo = t.dbLo;
   p.rowAnchor = t.Atab;
   p.rowAnchorStride = t.nSamPad;
-  p.colvec = t.dbeta;
   p.colAnchor = t.Btab;
   p.colAnchorStride = t.nVoxPad;
   p.Bop = b.bopF;
@@ -738,7 +862,7 @@ cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const flo
   cudaError_t e = cudaMemsetAsync(b.part, 0, (size_t)b.slotsF * t.nSamPad * t.nChaPad * sizeof(float2), st);
   if (e != cudaSuccess) return e;
   trace(h, EV_FK0, st);
-  e = dispatch(h, p, b.N, b.gridF, st);
+  e = launch(h, p, b.N, b.gridF, st);
   trace(h, EV_FK1, st);
   if (e != cudaSuccess) return e;
   return simt_reduce_forward(h, b.part, b.slotsF, y, D, mode, st);
@@ -752,10 +876,10 @@ cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) 
   k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Yt, b.bopA, chunks, b.N, t.nChaPad);
   h->launches += 1;
   TcParams p = base_params(h, b);
-  p.rowvec = t.dbeta;
+  p.rowHi = t.dbHi; p.rowLo = t.dbLo;
+  p.colHi = t.kpHi; p.colLo = t.kpLo;
   p.rowAnchor = t.Btab;
   p.rowAnchorStride = t.nVoxPad;
-  p.colvec = t.kappa;
   p.colAnchor = t.Atab;
   p.colAnchorStride = t.nSamPad;
   p.Bop = b.bopA;
@@ -765,7 +889,7 @@ cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) 
   cudaError_t e = cudaMemsetAsync(b.part, 0, (size_t)b.slotsA * t.nVoxPad * t.nChaPad * sizeof(float2), st);
   if (e != cudaSuccess) return e;
   trace(h, EV_AK0, st);
-  e = dispatch(h, p, b.N, b.gridA, st);
+  e = launch(h, p, b.N, b.gridA, st);
   trace(h, EV_AK1, st);
   if (e != cudaSuccess) return e;
   return simt_reduce_adjoint(h, b.part, b.slotsA, x, st);
