@@ -42,9 +42,14 @@ constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel
 constexpr int TV = 64;              // complex columns per pipeline stage
 constexpr int TK = 2 * TV;          // real K per stage (128 BF16 = 8 UMMA k-steps)
 constexpr int PHASE_WARPS = 16;     // four per TMEM lane quarter, a quarter of the stage's columns each
-constexpr int MMA_WARP = PHASE_WARPS;
-constexpr int LOAD_WARP = PHASE_WARPS + 1;
-constexpr int THREADS = (PHASE_WARPS + 2) * 32;
+// Warp roles: 16 phase warps, two contraction issuers (each one tcgen05.mma
+// stream; issue from a single thread costs ~50 cycles per instruction, so
+// the stage's k-steps are split between them), one residual-phase issuer
+// (TF32 MMAs) that also owns the TMEM allocation, and one loader.
+constexpr int CISS_WARP = PHASE_WARPS;        // contraction issuers: warps 16, 17
+constexpr int PISS_WARP = PHASE_WARPS + 2;    // residual-phase issuer, TMEM owner
+constexpr int LOAD_WARP = PHASE_WARPS + 3;
+constexpr int THREADS = (PHASE_WARPS + 4) * 32;
 constexpr float kTwoPi = 6.28318530717958647692f;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
 
@@ -264,11 +269,14 @@ __host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
 
 // Tensor-memory plan (512 columns): BF16 phase tiles ABUF x [hi TV | lo TV]
 // columns (one 32-bit column per complex element), residual-phase tiles
-// PD x TV FP32 columns, accumulators 2 x N FP32 columns.
+// PD x TV FP32 columns, accumulators 2 (groups) x NISS (issuers) x N FP32
+// columns.
 template <int N>
 struct Tmem {
-  static constexpr int ABUF = N <= 64 ? 2 : 1;
-  static constexpr int PD_MAX = (512 - 2 * N - ABUF * 2 * TV) / TV;
+  static constexpr int NISS = N <= 64 ? 2 : 1;
+  static constexpr int ABUF = N <= 32 ? 2 : 1;
+  static constexpr int ACC = 2 * NISS * N;
+  static constexpr int PD_MAX = (512 - ACC - ABUF * 2 * TV) / TV;
   static constexpr uint32_t A_COL = 0;
   static constexpr uint32_t P_COL = ABUF * 2 * TV;
 };
@@ -280,13 +288,11 @@ struct Tmem {
 //   CA  [NS][TV]      column anchors
 //   barriers: full[NS] empty[NS] afull[ABUF] aempty[ABUF] segdone[2]
 //             tmemfree[2] pfull[PD] pfree[PD] rfull[2] rfree[2]
-// The residual-phase tile of stage i+PD is issued right after the
-// contraction of stage i, PD <= NS-1 stages ahead of its use (the loader ring
-// of NS stages allows no more without a dependency cycle).
+// The residual-phase issuer runs up to PD stages ahead of the phase warps.
 template <int N, int KP, int NS>
 struct Smem {
   static constexpr int ABUF = Tmem<N>::ABUF;
-  static constexpr int PD = (NS - 1) < Tmem<N>::PD_MAX ? (NS - 1) : Tmem<N>::PD_MAX;
+  static constexpr int PD = (NS - 1) < Tmem<N>::PD_MAX ? (NS - 1) : (Tmem<N>::PD_MAX < 3 ? Tmem<N>::PD_MAX : 3);
   static constexpr int B_TILE = N * TK * 2;
   static constexpr int CV_TILE = TV * KP * 4;
   static constexpr int RV_TILE = TM * KP * 4;
@@ -311,7 +317,7 @@ constexpr int pick_stages() {
 template <int N, int KP, int NS>
 __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   using S = Smem<N, KP, NS>;
-  constexpr int ABUF = S::ABUF, PD = S::PD;
+  constexpr int ABUF = S::ABUF, PD = S::PD, NISS = Tmem<N>::NISS;
   static_assert(PD >= 1, "residual-phase look-ahead");
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -333,8 +339,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
   constexpr uint32_t TMEM_COLS = 512;
   constexpr uint32_t A_COL = Tmem<N>::A_COL, P_COL = Tmem<N>::P_COL;
-  constexpr uint32_t ACC_COL = P_COL + PD * TV;
-  static_assert(ACC_COL + 2 * N <= TMEM_COLS, "tensor memory plan");
+  constexpr uint32_t ACC_COL = P_COL + PD * TV;   // group g, issuer q: ACC_COL + (g&1)*NISS*N + q*N
+  static_assert(ACC_COL + 2 * NISS * N <= TMEM_COLS, "tensor memory plan");
   constexpr uint32_t SBO_TF32 = (KP / 4) * 128;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -347,14 +353,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   if (threadIdx.x == 0) {
     for (int i = 0; i < NS; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&empty[i], 1);
+      mbar_init(&empty[i], NISS);
     }
     for (int i = 0; i < ABUF; ++i) {
       mbar_init(&afull[i], PHASE_WARPS);
-      mbar_init(&aempty[i], 1);
+      mbar_init(&aempty[i], NISS);
     }
     for (int i = 0; i < 2; ++i) {
-      mbar_init(&segdone[i], 1);
+      mbar_init(&segdone[i], NISS);
       mbar_init(&tmemfree[i], PHASE_WARPS);
       mbar_init(&rfull[i], 1);
       mbar_init(&rfree[i], 1);
@@ -366,7 +372,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == MMA_WARP) {
+  if (warp == PISS_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(TMEM_COLS));
@@ -400,26 +406,30 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       bool got = ok && wait_bar(&segdone[g & 1], (g >> 1) & 1, abort, p.err);
       tc_fence_after();
       if (got) {
-        const uint32_t base = tmem + laneBase + ACC_COL + (uint32_t)((g & 1) * N + qcol * NA);
-        if constexpr (NA % 16 == 0) {
 #pragma unroll
-          for (int c0 = 0; c0 < NA; c0 += 16) {
-            float v[16];
-            tmem_ld16(base + c0, v);
+        for (int q = 0; q < NISS; ++q) {
+          const uint32_t base =
+              tmem + laneBase + ACC_COL + (uint32_t)((g & 1) * NISS * N + q * N + qcol * NA);
+          if constexpr (NA % 16 == 0) {
 #pragma unroll
-            for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+            for (int c0 = 0; c0 < NA; c0 += 16) {
+              float v[16];
+              tmem_ld16(base + c0, v);
+#pragma unroll
+              for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+            }
+          } else if constexpr (NA == 8) {
+            float v[8];
+            tmem_ld8(base, v);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] += v[i];
+          } else {
+            static_assert(NA == 4, "accumulator columns per thread");
+            float v[4];
+            tmem_ld4(base, v);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i] += v[i];
           }
-        } else if constexpr (NA == 8) {
-          float v[8];
-          tmem_ld8(base, v);
-#pragma unroll
-          for (int i = 0; i < 8; ++i) acc[i] += v[i];
-        } else {
-          static_assert(NA == 4, "accumulator columns per thread");
-          float v[4];
-          tmem_ld4(base, v);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) acc[i] += v[i];
         }
       }
       tc_fence_before();
@@ -511,24 +521,69 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       }
     }
     if (pendGrp >= 0) flush();
-  } else if (warp == MMA_WARP) {
-    // ---------------- MMA issuer (one thread): the contraction of stage it,
-    // then the residual-phase tile of stage it+PD
-    if (lane == 0 && nIter > 0) {
+  } else if (warp == CISS_WARP || warp == CISS_WARP + 1) {
+    // ---------------- contraction issuers: issuer q takes k-steps
+    // [q*KS, (q+1)*KS) of every stage into its own accumulator
+    const int q = warp - CISS_WARP;
+    if (lane == 0 && q < NISS && nIter > 0) {
+      constexpr int KS = (TK / 16) / NISS;
       constexpr uint32_t idescC = idesc_bf16(TM, N);
-      constexpr uint32_t idescP = idesc_tf32(TM, TV);
-      bool alive = true;
-      uint64_t *lastBar = nullptr;  // barrier of the most recent commit (for draining)
+      uint64_t *lastBar = nullptr;
       uint32_t lastPar = 0;
-      auto issue_phase = [&](int j) -> bool {
-        const int64_t w = wb + j;
-        const int kj = (int)(w / C) - rt0;
-        const bool lastOfRow = (j == nIter - 1) || ((w + 1) % C == 0);
+      int grp = -1, ch = ch0;
+      for (int it = 0; it < nIter; ++it, ++ch) {
+        if (ch == C) ch = 0;
+        const bool first = (it == 0) || (ch % GROUP == 0);
+        if (first) {
+          ++grp;
+          // accumulator buffer grp&1 was last used by group grp-2: wait until it was read out
+          if (grp >= 2 && !wait_bar(&tmemfree[grp & 1], ((grp >> 1) - 1) & 1, abort, p.err)) break;
+        }
+        const bool last = (it == nIter - 1) || (ch + 1 == C) || ((ch + 1) % GROUP == 0);
+        const int slot = it % NS, round = it / NS;
+        const int ab = it % ABUF, ar = it / ABUF;
+        if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
+        if (!wait_bar(&afull[ab], ar & 1, abort, p.err)) break;
+        tc_fence_after();
+        const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp & 1) * NISS * N + q * N);
+        const uint32_t aHi = tmem + A_COL + (uint32_t)(ab * 2 * TV);
+        const uint32_t aLo = aHi + TV;
+        const uint64_t bHi = umma_desc(smem_u32(sB + (size_t)slot * 2 * S::B_TILE));
+        const uint64_t bLo = umma_desc(smem_u32(sB + (size_t)slot * 2 * S::B_TILE + S::B_TILE));
+#pragma unroll
+        for (int kk = 0; kk < KS; ++kk) {
+          const int ks = q * KS + kk;
+          const uint32_t ka = ks * 8;                    // 16 BF16 = 8 TMEM columns
+          const uint64_t kb = (uint64_t)(ks * 2 * LBO) >> 4;  // two core matrices along K
+          umma_ta(dt, aHi + ka, bHi + kb, idescC, (first && kk == 0) ? 0u : 1u);
+          umma_ta(dt, aHi + ka, bLo + kb, idescC, 1u);
+          umma_ta(dt, aLo + ka, bHi + kb, idescC, 1u);
+        }
+        umma_commit(&empty[slot]);
+        umma_commit(&aempty[ab]);
+        lastBar = &aempty[ab];
+        lastPar = ar & 1;
+        if (last) umma_commit(&segdone[grp & 1]);
+      }
+      if (*abort && lastBar) drain_bar(lastBar, lastPar);  // MMAs done before TMEM is freed
+    }
+    __syncwarp();
+  } else if (warp == PISS_WARP) {
+    // ---------------- residual-phase issuer: TF32 tile of stage j, up to PD
+    // stages ahead of the phase warps
+    if (lane == 0 && nIter > 0) {
+      constexpr uint32_t idescP = idesc_tf32(TM, TV);
+      uint64_t *lastBar = nullptr;
+      uint32_t lastPar = 0;
+      int kj = 0, ch = ch0;
+      for (int j = 0; j < nIter; ++j, ++ch) {
+        if (ch == C) { ch = 0; ++kj; }
+        const bool lastOfRow = (j == nIter - 1) || (ch + 1 == C);
         const int s = j % NS, r = j / NS;
-        if (!wait_bar(&full[s], r & 1, abort, p.err)) return false;
-        if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) return false;
+        if (!wait_bar(&full[s], r & 1, abort, p.err)) break;
+        if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
         const int pb = j % PD, pr = j / PD;
-        if (j >= PD && !wait_bar(&pfree[pb], (pr - 1) & 1, abort, p.err)) return false;
+        if (j >= PD && !wait_bar(&pfree[pb], (pr - 1) & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t dt = tmem + P_COL + (uint32_t)(pb * TV);
         const uint32_t rHi = smem_u32(sRV + (size_t)(kj & 1) * 2 * S::RV_TILE);
@@ -546,48 +601,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
         lastBar = &pfull[pb];
         lastPar = pr & 1;
         if (lastOfRow) umma_commit(&rfree[kj & 1]);
-        return true;
-      };
-      for (int j = 0; j < PD && j < nIter && alive; ++j) alive = issue_phase(j);
-      int grp = -1, ch = ch0;
-      for (int it = 0; it < nIter && alive; ++it, ++ch) {
-        if (ch == C) ch = 0;
-        const bool first = (it == 0) || (ch % GROUP == 0);
-        if (first) {
-          ++grp;
-          // accumulator buffer grp&1 was last used by group grp-2: wait until it was read out
-          if (grp >= 2 && !wait_bar(&tmemfree[grp & 1], ((grp >> 1) - 1) & 1, abort, p.err)) break;
-        }
-        const bool last = (it == nIter - 1) || (ch + 1 == C) || ((ch + 1) % GROUP == 0);
-        const int slot = it % NS, round = it / NS;
-        const int ab = it % ABUF, ar = it / ABUF;
-        if (!wait_bar(&afull[ab], ar & 1, abort, p.err)) break;
-        tc_fence_after();
-        const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp & 1) * N);
-        const uint32_t aHi = tmem + A_COL + (uint32_t)(ab * 2 * TV);
-        const uint32_t aLo = aHi + TV;
-        const uint32_t bHi = smem_u32(sB + (size_t)slot * 2 * S::B_TILE);
-        const uint32_t bLo = bHi + S::B_TILE;
-#pragma unroll
-        for (int ks = 0; ks < TK / 16; ++ks) {
-          const uint32_t ka = ks * 8;        // 16 BF16 = 8 TMEM columns
-          const uint32_t kb = ks * 2 * LBO;  // 16 BF16 = two core matrices along K
-          umma_ta(dt, aHi + ka, umma_desc(bHi + kb), idescC, (first && ks == 0) ? 0u : 1u);
-          umma_ta(dt, aHi + ka, umma_desc(bLo + kb), idescC, 1u);
-          umma_ta(dt, aLo + ka, umma_desc(bHi + kb), idescC, 1u);
-        }
-        umma_commit(&empty[slot]);
-        umma_commit(&aempty[ab]);
-        lastBar = &aempty[ab];
-        lastPar = ar & 1;
-        (void)round;
-        if (last) umma_commit(&segdone[grp & 1]);
-        if (it + PD < nIter) alive = issue_phase(it + PD);
       }
-      if (*abort && lastBar) {
-        // aborted: let the MMAs already issued finish before TMEM is freed
-        drain_bar(lastBar, lastPar);
-      }
+      if (*abort && lastBar) drain_bar(lastBar, lastPar);
     }
     __syncwarp();
   } else {
@@ -632,7 +647,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
 
   tc_fence_before();
   __syncthreads();
-  if (warp == MMA_WARP) {
+  if (warp == PISS_WARP) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
   }
