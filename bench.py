@@ -41,9 +41,16 @@ METRIC = "E+E^H voxel·samples/s, TC vs plain FP32 on GB300 at <=1e-4 rel err vs
 UNIT = "voxel·samples/s"
 L2_FLUSH_BYTES = 256 << 20
 
-# DRAM traffic per launch of the dominant kernels from one ncu capture,
-# scaled to the full workload (see profiles/); None until captured.
-NCU_TRAFFIC_BYTES = {}
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# the dominant kernels, from one `ncu --set full` capture of this command on
+# the 200x200 / 12,000-sample / 16-coil workload (profiles/tc_engine_cfg2.md,
+# profiles/simt_engine_cfg2.md).  Other workloads report None.
+NCU_TRAFFIC_BYTES = {
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "forward"): 39_914_240 + 1_792,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "adjoint"): 47_090_688 + 32_512,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "forward"): 40_267_776 + 25_856,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "adjoint"): 36_679_424 + 11_776,
+}
 
 
 def parse_args():
@@ -264,7 +271,7 @@ def run_gb300(a):
     achieved = flops_per_launch / (dom_ms / 1e3) / 1e12
     bf16_peak, hbm_peak, peak_src = measured_peaks()
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved / bf16_peak, "traffic": NCU_TRAFFIC_BYTES.get((engine, dom)),
+                "frac": achieved / bf16_peak, "traffic": NCU_TRAFFIC_BYTES.get((w.name, engine, dom)),
                 "kernel": f"{engine} {dom} contraction", "peak_source": f"bf16_tflops ({peak_src}, burst)",
                 "kernel_ms": dom_ms, "flops_per_launch": flops_per_launch,
                 "frac_of_split_peak": achieved / (bf16_peak / 3.0) if engine == "tc" else None,
