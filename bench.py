@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true", help="skip timing the second engine")
+    ap.add_argument("--no-recon", action="store_true", help="skip timing the device CGNR solve")
+    ap.add_argument("--recon-iterations", type=int, default=20)
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -211,6 +213,45 @@ def time_engine(op, x, y, steps, warmup, flush, stream):
     return dict(step_ms=step_ms, fwd_kernel_ms=fk, adj_kernel_ms=ak, launches=launches)
 
 
+def time_recon(op, w, y, flush, stream, iterations, reps):
+    """recon_HOOp's weighted CGNR on the device (hoe_recon), as one cached CUDA
+    graph and as individual launches; CUDA events around each whole solve."""
+    import torch
+    from hoexplicit import recon as hrecon
+    dev = y.device
+    kr = np.hypot(w.kspha[1], w.kspha[2])
+    weight = torch.from_numpy(np.sqrt(0.05 + kr / kr.max()).astype(np.complex64)).to(dev)
+    data = y.reshape(w.nCha, w.nSam).t()
+    out = torch.empty(op.ncol, dtype=torch.complex64, device=dev)
+    units = (2.0 * iterations + 1.0) * w.nVox * w.nSam
+    res = {"iterations": iterations, "lambda": 1e-9, "weights": "sqrt-density-like, complex64",
+           "units_per_solve": units}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    for use_graph in (True, False):
+        _, st = hrecon.solve(op, data, weight, iterations=iterations, rel_tol=0.0, lam=1e-9,
+                             use_graph=use_graph, out=out)  # warm-up (captures the graph)
+        l0 = op.timings()["launches"]
+        ms = []
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            hrecon.solve(op, data, weight, iterations=iterations, rel_tol=0.0, lam=1e-9,
+                         use_graph=use_graph, out=out, stats=False)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        key = "graph" if use_graph else "direct"
+        m = statistics.mean(ms)
+        res[key] = {"ms_per_solve": m, "ms_per_iteration": m / iterations,
+                    "value": units / (m / 1e3), "unit": UNIT,
+                    "launches_per_solve": (op.timings()["launches"] - l0) / reps,
+                    "status": st["status"], "residual_ratio": st["residual"] / max(st["residual0"], 1e-300)}
+    res["graph_speedup"] = res["direct"]["ms_per_solve"] / res["graph"]["ms_per_solve"]
+    return res
+
+
 def run_gb300(a):
     import torch
     ws, rank, local = dist_env()
@@ -310,6 +351,12 @@ def run_gb300(a):
             op.set_engine("tc")
         except Exception as exc:  # report, do not substitute
             out["fp32_engine"] = {"error": str(exc)}
+
+    if not a.no_recon:
+        try:
+            out["recon"] = time_recon(op, w, y, flush, stream, a.recon_iterations, max(3, a.steps // 4))
+        except Exception as exc:  # report, do not substitute
+            out["recon"] = {"error": str(exc)}
 
     # end-to-end through the public API with host (pinned) buffers
     if not a.no_e2e:

@@ -92,6 +92,7 @@ void release_events(hoe_handle *h) {
 
 void release_device(hoe_handle *h) {
   release_events(h);
+  hoe::cg_release(h);
   hoe::tc_release(h);
   auto &t = h->t;
   dfree(t.dbeta); dfree(t.kappa); dfree(t.Atab); dfree(t.Btab); dfree(t.csm);
@@ -821,17 +822,71 @@ int hoe_normal(hoe_handle *h, const float *D, const void *x, void *out, void *st
   if (rc) return rc;
   if (!x || !out) return fail(h, HOE_ERR_ARG, "x and out must be device pointers");
   DeviceGuard guard(h->device);
-  cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
-  if (h->engine == HOE_ENGINE_TC_BF16X3) {
-    if (e == cudaSuccess) e = hoe::tc_forward(h, nullptr, nullptr, D, hoe::FWD_TO_YT_WEIGHTED, st);
-    if (e == cudaSuccess) e = hoe::tc_adjoint_from_Yt(h, (float2 *)out, st);
-  } else {
-    if (e == cudaSuccess) e = hoe::simt_forward(h, nullptr, nullptr, D, hoe::FWD_TO_YT_WEIGHTED, st);
-    if (e == cudaSuccess) e = hoe::simt_adjoint_from_Yt(h, (float2 *)out, st);
-  }
+  cudaError_t e = hoe::apply_normal(h, D, (const float2 *)x, (float2 *)out, (cudaStream_t)stream);
   return finish(h, e, "hoe_normal");
 }
+
+int hoe_recon(hoe_handle *h, const void *data, const void *weights, void *x, const hoe_cg_params *p,
+              hoe_cg_stats *stats, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!data || !x) return fail(h, HOE_ERR_ARG, "data and x must be device pointers");
+  if (!p) return fail(h, HOE_ERR_ARG, "solver parameters must not be NULL");
+  if (p->iterations < 0) return fail(h, HOE_ERR_ARG, "iterations must be >= 0 (got %d)", p->iterations);
+  if (!(p->rel_tol >= 0.0) || !std::isfinite(p->rel_tol))
+    return fail(h, HOE_ERR_ARG, "rel_tol must be finite and >= 0");
+  if (!(p->lambda >= 0.0) || !std::isfinite(p->lambda))
+    return fail(h, HOE_ERR_ARG, "lambda must be finite and >= 0");
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  hoe::CgRequest r;
+  r.iterations = p->iterations;
+  r.use_graph = p->use_graph != 0;
+  r.rel_tol = p->rel_tol;
+  r.lambda = p->lambda;
+  cudaError_t e = hoe::cg_solve(h, (const float2 *)data, (const float2 *)weights, (float2 *)x, r, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(h, e, "hoe_recon");
+  if (stats) {
+    hoe::CgScalars S{};
+    e = hoe::cg_read_stats(h, st, &S);
+    if (e != cudaSuccess) return cuda_fail(h, e, "hoe_recon: reading the solver state");
+    stats->iterations = S.iters;
+    const int status = S.status[r.iterations & 1];
+    stats->status = status;
+    stats->residual0 = std::sqrt(S.zz0);
+    stats->residual = std::sqrt(S.zz[r.iterations & 1]);
+  }
+  return HOE_OK;
+}
+
+}  // extern "C"
+
+namespace hoe {
+
+cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {
+  cudaError_t e = prep_Z(h, x, st);
+  if (h->engine == HOE_ENGINE_TC_BF16X3) {
+    if (e == cudaSuccess) e = tc_forward(h, nullptr, nullptr, D, FWD_TO_YT_WEIGHTED, st);
+    if (e == cudaSuccess) e = tc_adjoint_from_Yt(h, out, st);
+  } else {
+    if (e == cudaSuccess) e = simt_forward(h, nullptr, nullptr, D, FWD_TO_YT_WEIGHTED, st);
+    if (e == cudaSuccess) e = simt_adjoint_from_Yt(h, out, st);
+  }
+  return e;
+}
+
+cudaError_t apply_adjoint_weighted(hoe_handle *h, const float2 *y, const float *D, float2 *x,
+                                   cudaStream_t st) {
+  cudaError_t e = prep_Yt(h, y, D, st);
+  if (e == cudaSuccess)
+    e = (h->engine == HOE_ENGINE_TC_BF16X3) ? tc_adjoint_from_Yt(h, x, st) : simt_adjoint_from_Yt(h, x, st);
+  return e;
+}
+
+}  // namespace hoe
+
+extern "C" {
 
 int hoe_derivative(hoe_handle *h, const void *x, void *y, void *stream) {
   int rc = check_usable(h);

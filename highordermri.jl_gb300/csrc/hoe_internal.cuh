@@ -89,6 +89,40 @@ struct TcState {
   size_t bytes = 0;
 };
 
+// Device-resident CGNR (hoe_cg.cu).
+struct CgScalars {            // device scalars of one solve
+  double zz0;                 // ‖z₀‖²
+  double zz[2];               // ‖zₖ‖², slot k&1
+  double pq;                  // Re(pᴴq) of the last iteration
+  int status[2];              // 0 running, 1 converged, 2 stopped (pᴴq ≤ 0 / not finite), slot k&1
+  int iters;                  // iterations that updated x
+  int pad;
+};
+
+struct CgRequest {
+  int iterations = 0;
+  int use_graph = 1;
+  double rel_tol = 0.0;
+  double lambda = 0.0;
+};
+
+struct CgState {
+  void *base = nullptr;       // one allocation for the buffers below
+  size_t bytes = 0;
+  float2 *z = nullptr, *p = nullptr, *q = nullptr;   // [nFull] solver vectors
+  float *D = nullptr;         // [nSam*nCha] |w|²
+  double *part = nullptr;     // [2][304] block partials (pᴴq, ‖z‖²)
+  CgScalars *S = nullptr;
+  cudaStream_t cap = nullptr; // capture stream
+  cudaGraphExec_t exec = nullptr;
+  int64_t graphLaunches = 0;  // kernels per graph launch
+  // the request the cached graph was captured for
+  const void *kData = nullptr, *kW = nullptr;
+  void *kX = nullptr;
+  int kIters = -1, kEngine = -1;
+  double kTol = 0.0, kLambda = 0.0;
+};
+
 }  // namespace hoe
 
 struct hoe_handle {
@@ -108,6 +142,7 @@ struct hoe_handle {
   hoe::Scratch s;
   hoe::TcState tc;
   void *tc_host = nullptr;   // tensor-core buffer table (hoe_tc.cu)
+  hoe::CgState cg;           // device-resident CGNR (hoe_cg.cu)
 };
 
 namespace hoe {
@@ -127,6 +162,19 @@ cudaError_t simt_reduce_adjoint(const hoe_handle *h, const float2 *part, int spl
                                 cudaStream_t st);
 cudaError_t simt_backward(const hoe_handle *h, const float2 *x, const float2 *r,
                           float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
+
+// Operator applications on the active engine (hoe_api.cu), used by the solver:
+// out = HOOpᴴ diag(D) HOOp x, and x = HOOpᴴ (D · y) (D = NULL: ones).
+cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st);
+cudaError_t apply_adjoint_weighted(hoe_handle *h, const float2 *y, const float *D, float2 *x,
+                                   cudaStream_t st);
+
+// Device-resident CGNR (hoe_cg.cu).  cg_solve enqueues a whole solve on st
+// (as one cached CUDA graph when r.use_graph); cg_read_stats waits for st.
+cudaError_t cg_solve(hoe_handle *h, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
+                     cudaStream_t st);
+cudaError_t cg_read_stats(const hoe_handle *h, cudaStream_t st, CgScalars *out);
+void cg_release(hoe_handle *h);
 
 // Sets the thread's handle-less error message (hoe_last_error(NULL)).
 void record_error(const char *msg);

@@ -11,10 +11,11 @@ from .model import Grid, basisfunc_spha, prep_concomitant, prep_kspha  # noqa: F
 from .operator import (AdjointOp, ExplicitGB300Op, HighOrderExplicitOp, NormalOp,  # noqa: F401
                        WeightedOp, WeightingOp, close, compose, explicit_gpu_normal,
                        normalOperator)
+from .recon import CGNR, L2Regularization, recon_HOOp  # noqa: F401
 
 __all__ = [
     "ArgumentError", "DimensionMismatch", "HoeError", "OutOfMemoryError", "Grid",
     "basisfunc_spha", "prep_kspha", "prep_concomitant", "HighOrderExplicitOp", "ExplicitGB300Op",
     "AdjointOp", "NormalOp", "WeightingOp", "WeightedOp", "compose", "normalOperator",
-    "explicit_gpu_normal", "close", "load",
+    "explicit_gpu_normal", "close", "load", "CGNR", "L2Regularization", "recon_HOOp",
 ]

@@ -34,8 +34,12 @@ EXPORTED = (
     "hoe_version", "hoe_abi_version", "hoe_create", "hoe_close", "hoe_free", "hoe_is_closed",
     "hoe_last_error", "hoe_get_info", "hoe_set_engine", "hoe_forward", "hoe_adjoint",
     "hoe_normal", "hoe_derivative", "hoe_backward", "hoe_set_timing", "hoe_get_timings",
-    "hoe_forward_noalloc", "hoe_check", "hoe_plan",
+    "hoe_forward_noalloc", "hoe_check", "hoe_plan", "hoe_recon",
 )
+
+HOE_CG_ITERATION_LIMIT = 0
+HOE_CG_CONVERGED = 1
+HOE_CG_STOPPED = 2
 
 
 class ArgumentError(ValueError):
@@ -90,6 +94,20 @@ class HoeTimings(ctypes.Structure):
     ]
 
 
+class HoeCgParams(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int32), ("use_graph", ctypes.c_int32),
+        ("rel_tol", ctypes.c_double), ("lambda_", ctypes.c_double),
+    ]
+
+
+class HoeCgStats(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int32), ("status", ctypes.c_int32),
+        ("residual0", ctypes.c_double), ("residual", ctypes.c_double),
+    ]
+
+
 class HoeInfo(ctypes.Structure):
     _fields_ = [
         ("nSam", ctypes.c_int32), ("nCha", ctypes.c_int32), ("nVox", ctypes.c_int32),
@@ -138,6 +156,7 @@ def load():
     lib.hoe_check.argtypes = [H, vp]
     lib.hoe_plan.argtypes = [ctypes.POINTER(HoeDesc), ctypes.POINTER(HoeInfo)]
     lib.hoe_forward_noalloc.argtypes = [ctypes.POINTER(HoeRawModel), vp, vp, vp]
+    lib.hoe_recon.argtypes = [H, vp, vp, vp, ctypes.POINTER(HoeCgParams), ctypes.POINTER(HoeCgStats), vp]
     for name in EXPORTED:
         if name not in ("hoe_free",):
             getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int

@@ -34,6 +34,10 @@
  *                     (the kspha_dt mode used by FindDelay, FindDelay.jl:195-200)
  *   hoe_backward      no reference counterpart: gradient of 0.5*||E x - y||^2 with
  *                     respect to kspha, fieldmap and a time origin t0
+ *   hoe_recon         recon_HOOp, src/Recon/recon_HOOp.jl:52-88, for the resident
+ *                     explicit operator: the weighting W∘HOOp and normal EᴴWᴴWE of
+ *                     :73-78 and the CGNR solve!(solver, Data) of :79-80
+ *                     (RegularizedLeastSquares CGNR with L2Regularization)
  *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
  *   hoe_free          releases the host handle (Julia finalizer)
  *   hoe_set_timing / hoe_get_timings
@@ -117,6 +121,23 @@ typedef struct hoe_timings {
     int64_t launches;              /* kernels launched by this handle so far        */
 } hoe_timings;
 
+/* Parameters of hoe_recon (the recParams of recon_HOOp). */
+typedef struct hoe_cg_params {
+    int32_t iterations;            /* maximum CG iterations (:iterations), >= 0          */
+    int32_t use_graph;             /* nonzero: run the solve as one cached CUDA graph    */
+    double  rel_tol;               /* stop once ||z_k|| <= rel_tol*||z_0|| (:relTol)     */
+    double  lambda;                /* L2Regularization weight, >= 0 (:reg)               */
+} hoe_cg_params;
+
+/* Solver state after hoe_recon (filled when a stats pointer is given). */
+typedef struct hoe_cg_stats {
+    int32_t iterations;            /* iterations that updated x                          */
+    int32_t status;                /* 0 iteration limit, 1 converged (rel_tol),
+                                      2 stopped: p^H(E^H E + lambda I)p <= 0 or not finite */
+    double  residual0;             /* ||z_0|| = ||E^H W^H W data||                        */
+    double  residual;              /* ||z_k|| = ||E^H W^H (W data - W E x) - lambda x||   */
+} hoe_cg_stats;
+
 typedef struct hoe_info {
     int32_t nSam, nCha, nVox, nTermEff, nFull;
     int32_t engine;
@@ -171,6 +192,22 @@ HOE_API int  hoe_derivative(hoe_handle *h, const void *x_dev, void *y_dev, void 
 HOE_API int  hoe_backward(hoe_handle *h, const void *x_dev, const void *r_dev,
                   float *dk_dev, float *ddf_dev, double *dt0_dev,
                   int32_t flags, void *stream);
+
+/* Weighted reconstruction, recon_HOOp for this operator:
+ *   x = argmin ||W (E x - data)||^2 + lambda ||x||^2   by CGNR from x = 0,
+ * with W = diag(weights) repeated over the coils.
+ *   data_dev     complex64 [nSam*nCha], samples fastest (Data of recon_HOOp)
+ *   weights_dev  complex64 [nSam] raw sample weights (NULL: ones); a weight
+ *                contributes |w|^2 to the normal, as in recon_HOOp
+ *   x_dev        complex64 [prod(matrixSize)] output image, x fastest
+ * All vectors and scalars stay on the device; the call is stream-ordered and
+ * does not wait unless stats is non-NULL (then it waits for the stream and
+ * reports the solver state).  With use_graph the iterations are captured once
+ * into a CUDA graph that is cached on the handle and replayed while the
+ * pointers, parameters and engine stay the same.  Results are deterministic
+ * and identical with and without the graph. */
+HOE_API int  hoe_recon(hoe_handle *h, const void *data_dev, const void *weights_dev, void *x_dev,
+                       const hoe_cg_params *params, hoe_cg_stats *stats, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free forward.  No counterpart in the reference.

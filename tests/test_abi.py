@@ -37,6 +37,8 @@ def test_struct_layouts_match_header():
     # two int32 blocks followed by pointers / doubles, natural alignment
     assert ctypes.sizeof(_lib.HoeDesc) == 14 * 4 + 7 * 8
     assert ctypes.sizeof(_lib.HoeInfo) == 14 * 4 + 8 + 8
+    assert ctypes.sizeof(_lib.HoeCgParams) == 2 * 4 + 2 * 8
+    assert ctypes.sizeof(_lib.HoeCgStats) == 2 * 4 + 2 * 8
 
 
 def _desc(**over):
@@ -72,6 +74,8 @@ def test_null_arguments():
     h = ctypes.c_void_p()
     assert lib.hoe_create(ctypes.byref(h), None) == _lib.HOE_ERR_ARG
     assert lib.hoe_forward(None, None, None, None) == _lib.HOE_ERR_ARG
+    p = _lib.HoeCgParams(10, 1, 0.0, 0.0)
+    assert lib.hoe_recon(None, None, None, None, ctypes.byref(p), None, None) == _lib.HOE_ERR_ARG
     assert lib.hoe_is_closed(None) == 1
     lib.hoe_free(None)  # no-op
 
