@@ -60,7 +60,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--engine", default="auto", choices=["auto", "tc", "fp32"])
-    ap.add_argument("--config", default="2", choices=["1", "2", "3"])
+    ap.add_argument("--config", default="2", choices=["1", "2", "3", "5"],
+                    help="2: 200x200 spiral (headline); 5: 24-slice batch in one persistent launch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -74,7 +75,8 @@ def parse_args():
 
 def workload(cfg: str):
     from hoexplicit import workloads
-    return {"1": workloads.config1, "2": workloads.config2, "3": workloads.config3}[cfg]()
+    return {"1": workloads.config1, "2": workloads.config2, "3": workloads.config3,
+            "5": lambda: workloads.config5()[0]}[cfg]()
 
 
 def dist_env():
@@ -250,6 +252,134 @@ def time_recon(op, w, y, flush, stream, iterations, reps):
                     "status": st["status"], "residual_ratio": st["residual"] / max(st["residual0"], 1e-300)}
     res["graph_speedup"] = res["direct"]["ms_per_solve"] / res["graph"]["ms_per_solve"]
     return res
+
+
+def run_batch(a):
+    """24 slices (160^2-224^2 voxels, 8,000-20,000 samples, 16 coils): all
+    slices' E and E^H in one persistent launch per direction (OperatorBatch),
+    and recon_HOOp's 30-iteration weighted CGNR for every slice in one graph."""
+    import torch
+    from hoexplicit import HighOrderExplicitOp, OperatorBatch, workloads
+    ws_, rank, local = dist_env()
+    if ws_ > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    engine = "fp32" if a.engine == "fp32" else "tc"
+    slices = workloads.config5()
+    ops = [HighOrderExplicitOp(w.grid, w.kspha, w.times, engine=engine, **w.op_kwargs()) for w in slices]
+    B = OperatorBatch(ops)
+    stream = torch.cuda.current_stream()
+    xs = [torch.from_numpy(w.x.astype(np.complex64)).to(dev) for w in slices]
+    ys = [y + 0.01 * y.abs().pow(2).mean().sqrt() * torch.randn_like(y) for y in B.forward(xs)]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    pairs = float(sum(w.nVox * w.nSam for w in slices))
+    units = 2.0 * pairs
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            fn()
+            ev1.record(stream)
+            ev1.synchronize()
+            ms.append(ev0.elapsed_time(ev1))
+        return statistics.mean(ms)
+
+    l0 = B.info()["launches"]
+    with Clocks(dev) as clk:
+        ms = timed(lambda: (B.forward(xs), B.adjoint(ys)), a.steps, a.warmup)
+    launches = (B.info()["launches"] - l0) / (a.steps + a.warmup)
+    if ws_ > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    bf16_peak, _, peak_src = measured_peaks()
+    flops = 8.0 * 16 * pairs  # contraction flops per direction
+    out = {"metric": METRIC, "value": ws_ * units / (ms / 1e3), "unit": UNIT, "n_gpus": ws_,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "bf16x3/f32-acc" if engine == "tc" else "f32",
+           "data": "synthetic (seeded, shapes/distributions of the named configuration)",
+           "config": {"workload": f"cfg5-{len(slices)}slices-160..224sq-8k..20k-samples-16c",
+                      "slices": len(slices), "voxel_samples_per_direction": pairs, "engine": engine,
+                      "parallelism": f"replicas x{ws_}", "l2": "flushed between timed steps (256 MiB write)",
+                      "contraction_launches_per_direction": B.info()["contraction_launches"]},
+           "roofline": {"bound": "tensor", "achieved": 2 * flops / (ms / 1e3) / 1e12, "peak": bf16_peak,
+                        "unit": "TFLOP/s", "frac": 2 * flops / (ms / 1e3) / 1e12 / bf16_peak,
+                        "traffic": None, "kernel": "whole step (both directions, all slices)",
+                        "peak_source": f"bf16_tflops ({peak_src}, burst)"},
+           "clocks": clk.summary(), "gpu_launches": launches}
+    # the same products slice by slice (one launch per slice and direction)
+    def per_slice():
+        for op, x, y in zip(ops, xs, ys):
+            op * x
+            op.H * y
+    ms1 = timed(per_slice, max(3, a.steps // 2), 2)
+    out["per_slice_launches"] = {"ms_per_step": ms1, "value": units / (ms1 / 1e3), "batched_speedup": ms1 / ms}
+    if not a.no_recon:
+        rng = np.random.default_rng(5)
+        datas = [y.reshape(w.nCha, w.nSam).t() for w, y in zip(slices, ys)]
+        weights = []
+        for w in slices:
+            kr = np.hypot(w.kspha[1], w.kspha[2])
+            weights.append(torch.from_numpy(np.sqrt(0.05 + kr / kr.max()).astype(np.complex64)).to(dev))
+        iters = 30
+        outs = [torch.empty(op.ncol, dtype=torch.complex64, device=dev) for op in ops]
+        _, st = B.recon(datas, weights, iterations=iters, rel_tol=0.0, lam=1e-9, out=outs)
+        l0 = B.info()["launches"]
+        msr = timed(lambda: B.recon(datas, weights, iterations=iters, rel_tol=0.0, lam=1e-9, out=outs,
+                                    stats=False), 3, 0)
+        ru = (2.0 * iters + 1.0) * pairs
+        out["recon"] = {"iterations": iters, "ms_per_solve": msr, "value": ru / (msr / 1e3), "unit": UNIT,
+                        "graph": True, "launches_per_solve": (B.info()["launches"] - l0) / 3,
+                        "status": sorted({s["status"] for s in st}),
+                        "max_residual_ratio": max(s["residual"] / max(s["residual0"], 1e-300) for s in st)}
+        del rng
+    if not a.no_e2e:
+        xh = [x.cpu().pin_memory() for x in xs]
+        yh = [y.cpu().pin_memory() for y in ys]
+        xo = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in xs]
+        yo = [torch.empty(y.shape, dtype=y.dtype).pin_memory() for y in ys]
+        def e2e():
+            yr = B.forward([x.to(dev, non_blocking=True) for x in xh])
+            xr = B.adjoint([y.to(dev, non_blocking=True) for y in yh])
+            for dst, src in zip(yo, yr):
+                dst.copy_(src, non_blocking=True)
+            for dst, src in zip(xo, xr):
+                dst.copy_(src, non_blocking=True)
+        e2e()
+        torch.cuda.synchronize()
+        n_e2e = max(3, a.steps // 2)
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            e2e()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        out["e2e"] = {"value": ws_ * units / e2e_s, "unit": UNIT,
+                      "h2d_bytes_per_step": int(sum(x.numel() * 8 for x in xh) + sum(y.numel() * 8 for y in yh)),
+                      "d2h_bytes_per_step": int(sum(x.numel() * 8 for x in xo) + sum(y.numel() * 8 for y in yo)),
+                      "ms_per_step": e2e_s * 1e3}
+    if rank == 0 and ws_ == 1 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(slices[0], a.cpu_seconds)
+        out["cpu_baseline"]["sample"] += " (slice 0 of the batch)"
+    B.check()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    B.close()
+    for op in ops:
+        op.close()
+    if ws_ > 1:
+        torch.distributed.destroy_process_group()
 
 
 def run_gb300(a):
@@ -428,6 +558,8 @@ def run_reference(a):
     value = units / s
     sample = (f"each step: E and E^H over {n_rows} of {nSam} samples x {len(idx)} voxels x {w.nCha} coils "
               "(FP64 C restatement of array_operator.jl:241-348; the Julia reference cannot run here)")
+    if a.config == "5":
+        sample += "; slice 0 of the 24-slice batch (the reference applies slices one by one)"
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
            "steps": a.steps, "warmup": a.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -443,6 +575,8 @@ def main():
     a = parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == "5":
+        run_batch(a)
     else:
         run_gb300(a)
 

@@ -233,57 +233,178 @@ cudaError_t ensure_buffers(hoe_handle *h) {
   return cudaSuccess;
 }
 
-void drop_graph(CgState &c) {
-  if (c.exec) cudaGraphExecDestroy(c.exec);
-  c.exec = nullptr;
-  c.graphLaunches = 0;
+// The operators of one solve: a single handle, or the members of a batch
+// (with a batched tensor-core plan when every member runs that engine).
+struct Members {
+  hoe_handle *const *hs;
+  int n;
+  void *tcplan;
+};
+
+// out_i = HOOp_iᴴ diag(D_i) HOOp_i x_i for every member.
+cudaError_t normal_all(const Members &m, const std::vector<float2 *> &xs, const std::vector<float2 *> &outs,
+                       cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (m.tcplan) {
+    std::vector<const float *> D(m.n);
+    for (int i = 0; i < m.n && e == cudaSuccess; ++i) {
+      D[i] = m.hs[i]->cg.D;
+      e = prep_Z(m.hs[i], xs[i], st);
+    }
+    if (e == cudaSuccess) e = tc_batch_forward(m.tcplan, nullptr, D.data(), FWD_TO_YT_WEIGHTED, st);
+    if (e == cudaSuccess) e = tc_batch_adjoint_from_Yt(m.tcplan, outs.data(), st);
+    return e;
+  }
+  for (int i = 0; i < m.n && e == cudaSuccess; ++i) e = apply_normal(m.hs[i], m.hs[i]->cg.D, xs[i], outs[i], st);
+  return e;
 }
 
-// Enqueues the whole solve on `st` (a capturing stream or an ordinary one).
-cudaError_t enqueue_solve(hoe_handle *h, const float2 *data, const float2 *w, float2 *x,
-                          const CgRequest &r, cudaStream_t st) {
-  auto &c = h->cg;
-  const auto &t = h->t;
-  const int64_t n = t.nFull;
-  const int G = grid_for(n);
-  double *partPQ = c.part, *partZZ = c.part + kMaxBlocks;
-  const int64_t nd = (int64_t)t.nSam * t.nCha;
-  k_cg_weights<<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(w, c.D, t.nSam, t.nCha);
-  h->launches += 1;
-  cudaError_t e = cudaGetLastError();
+// Enqueues the whole solve of every member on `st` (a capturing stream or an
+// ordinary one).  Member i solves for x[i] from data[i] with weights w[i].
+cudaError_t enqueue_solve(const Members &m, const float2 *const *data, const float2 *const *w,
+                          float2 *const *x, const CgRequest &r, cudaStream_t st) {
+  const int n = m.n;
+  std::vector<float2 *> zs(n), ps(n), qs(n);
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n; ++i) {
+    hoe_handle *h = m.hs[i];
+    const auto &t = h->t;
+    zs[i] = h->cg.z; ps[i] = h->cg.p; qs[i] = h->cg.q;
+    const int64_t nd = (int64_t)t.nSam * t.nCha;
+    k_cg_weights<<<(unsigned)((nd + 255) / 256), 256, 0, st>>>(w[i], h->cg.D, t.nSam, t.nCha);
+    h->launches += 1;
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // z₀ = HOOpᴴ (|w|² · Data)
-  if (e == cudaSuccess) e = apply_adjoint_weighted(h, data, c.D, c.z, st);
+  if (m.tcplan) {
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = prep_Yt(m.hs[i], data[i], m.hs[i]->cg.D, st);
+    if (e == cudaSuccess) e = tc_batch_adjoint_from_Yt(m.tcplan, zs.data(), st);
+  } else {
+    for (int i = 0; i < n && e == cudaSuccess; ++i)
+      e = apply_adjoint_weighted(m.hs[i], data[i], m.hs[i]->cg.D, zs[i], st);
+  }
   if (e != cudaSuccess) return e;
-  k_cg_start<<<G, kThreads, 0, st>>>(c.z, c.p, x, n, partZZ);
-  k_cg_start_fin<<<1, kThreads, 0, st>>>(partZZ, G, c.S);
-  h->launches += 2;
+  for (int i = 0; i < n; ++i) {
+    hoe_handle *h = m.hs[i];
+    const int64_t nv = h->t.nFull;
+    const int G = grid_for(nv);
+    double *partZZ = h->cg.part + kMaxBlocks;
+    k_cg_start<<<G, kThreads, 0, st>>>(h->cg.z, h->cg.p, x[i], nv, partZZ);
+    k_cg_start_fin<<<1, kThreads, 0, st>>>(partZZ, G, h->cg.S);
+    h->launches += 2;
+  }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const double tol2 = r.rel_tol * r.rel_tol;
   for (int k = 0; k < r.iterations; ++k) {
-    e = apply_normal(h, c.D, c.p, c.q, st);
+    e = normal_all(m, ps, qs, st);
     if (e != cudaSuccess) return e;
-    k_cg_pq<<<G, kThreads, 0, st>>>(c.p, c.q, n, (float)r.lambda, partPQ);
-    k_cg_step<<<G, kThreads, 0, st>>>(x, c.z, c.p, c.q, n, partPQ, partZZ, G, c.S, k);
-    k_cg_dir<<<G, kThreads, 0, st>>>(c.z, c.p, n, partPQ, partZZ, G, c.S, k, tol2);
-    h->launches += 3;
+    for (int i = 0; i < n; ++i) {
+      hoe_handle *h = m.hs[i];
+      auto &c = h->cg;
+      const int64_t nv = h->t.nFull;
+      const int G = grid_for(nv);
+      double *partPQ = c.part, *partZZ = c.part + kMaxBlocks;
+      k_cg_pq<<<G, kThreads, 0, st>>>(c.p, c.q, nv, (float)r.lambda, partPQ);
+      k_cg_step<<<G, kThreads, 0, st>>>(x[i], c.z, c.p, c.q, nv, partPQ, partZZ, G, c.S, k);
+      k_cg_dir<<<G, kThreads, 0, st>>>(c.z, c.p, nv, partPQ, partZZ, G, c.S, k, tol2);
+      h->launches += 3;
+    }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
-bool same_request(const CgState &c, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
-                  int engine) {
-  return c.exec && c.kData == data && c.kW == w && c.kX == x && c.kIters == r.iterations &&
-         c.kTol == r.rel_tol && c.kLambda == r.lambda && c.kEngine == engine;
+std::vector<const void *> request_key(const Members &m, const float2 *const *data, const float2 *const *w,
+                                      float2 *const *x) {
+  std::vector<const void *> k;
+  k.reserve(4 * m.n);
+  for (int i = 0; i < m.n; ++i) {
+    k.push_back(m.hs[i]);
+    k.push_back(data[i]);
+    k.push_back(w[i]);
+    k.push_back(x[i]);
+  }
+  return k;
+}
+
+int engine_key(const Members &m) {
+  int e = 0;
+  for (int i = 0; i < m.n; ++i) e = e * 2 + m.hs[i]->engine;
+  return m.tcplan ? -1 - e : e;
+}
+
+// Runs the solve through g: captured on the first call for a request,
+// replayed afterwards.  Kernel launches are counted into *launches.
+cudaError_t run(CgGraph &g, const Members &m, const float2 *const *data, const float2 *const *w,
+                float2 *const *x, const CgRequest &r, cudaStream_t st, int64_t *launches) {
+  for (int i = 0; i < m.n; ++i) {
+    cudaError_t e = ensure_buffers(m.hs[i]);
+    if (e != cudaSuccess) return e;
+  }
+  if (!r.use_graph) {
+    int64_t l0 = 0, l1 = 0;
+    for (int i = 0; i < m.n; ++i) l0 += m.hs[i]->launches;
+    cudaError_t e = enqueue_solve(m, data, w, x, r, st);
+    for (int i = 0; i < m.n; ++i) l1 += m.hs[i]->launches;
+    *launches += l1 - l0;
+    return e;
+  }
+  std::vector<const void *> key = request_key(m, data, w, x);
+  const int ek = engine_key(m);
+  cudaError_t e = cudaSuccess;
+  if (!(g.exec && g.key == key && g.kIters == r.iterations && g.kTol == r.rel_tol && g.kLambda == r.lambda &&
+        g.kEngine == ek)) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+    if (!g.cap) {
+      e = cudaStreamCreateWithFlags(&g.cap, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return e;
+    }
+    std::vector<int> timing(m.n);
+    std::vector<int64_t> l0(m.n);
+    for (int i = 0; i < m.n; ++i) {
+      timing[i] = m.hs[i]->timing;
+      m.hs[i]->timing = 0;  // no trace events inside a graph
+      l0[i] = m.hs[i]->launches;
+    }
+    e = cudaStreamBeginCapture(g.cap, cudaStreamCaptureModeThreadLocal);
+    cudaError_t eq = e == cudaSuccess ? enqueue_solve(m, data, w, x, r, g.cap) : e;
+    cudaGraph_t graph = nullptr;
+    if (e == cudaSuccess) e = cudaStreamEndCapture(g.cap, &graph);
+    int64_t per = 0;
+    for (int i = 0; i < m.n; ++i) {
+      m.hs[i]->timing = timing[i];
+      per += m.hs[i]->launches - l0[i];
+      m.hs[i]->launches = l0[i];
+    }
+    if (eq != cudaSuccess || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return eq != cudaSuccess ? eq : e;
+    }
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { g.exec = nullptr; return e; }
+    g.launches = per;
+    g.key = std::move(key);
+    g.kIters = r.iterations; g.kTol = r.rel_tol; g.kLambda = r.lambda; g.kEngine = ek;
+  }
+  e = cudaGraphLaunch(g.exec, st);
+  if (e == cudaSuccess) *launches += g.launches;
+  return e;
 }
 
 }  // namespace
 
+void cg_graph_release(CgGraph &g) {
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.cap) cudaStreamDestroy(g.cap);
+  g = CgGraph{};
+}
+
 void cg_release(hoe_handle *h) {
   auto &c = h->cg;
-  drop_graph(c);
-  if (c.cap) cudaStreamDestroy(c.cap);
-  c.cap = nullptr;
+  cg_graph_release(c.graph);
   if (c.base) cudaFree(c.base);
   h->bytes -= (int64_t)c.bytes;
   c = CgState{};
@@ -291,41 +412,20 @@ void cg_release(hoe_handle *h) {
 
 cudaError_t cg_solve(hoe_handle *h, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
                      cudaStream_t st) {
-  cudaError_t e = ensure_buffers(h);
-  if (e != cudaSuccess) return e;
-  auto &c = h->cg;
-  if (!r.use_graph) return enqueue_solve(h, data, w, x, r, st);
-  if (!same_request(c, data, w, x, r, h->engine)) {
-    drop_graph(c);
-    if (!c.cap) {
-      e = cudaStreamCreateWithFlags(&c.cap, cudaStreamNonBlocking);
-      if (e != cudaSuccess) return e;
-    }
-    const int savedTiming = h->timing;
-    const int64_t l0 = h->launches;
-    h->timing = 0;  // no trace events inside a graph
-    e = cudaStreamBeginCapture(c.cap, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) { h->timing = savedTiming; return e; }
-    cudaError_t eq = enqueue_solve(h, data, w, x, r, c.cap);
-    cudaGraph_t g = nullptr;
-    e = cudaStreamEndCapture(c.cap, &g);
-    h->timing = savedTiming;
-    const int64_t perGraph = h->launches - l0;
-    h->launches = l0;
-    if (eq != cudaSuccess || e != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      cudaGetLastError();
-      return eq != cudaSuccess ? eq : e;
-    }
-    e = cudaGraphInstantiate(&c.exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) { c.exec = nullptr; return e; }
-    c.graphLaunches = perGraph;
-    c.kData = data; c.kW = w; c.kX = x;
-    c.kIters = r.iterations; c.kTol = r.rel_tol; c.kLambda = r.lambda; c.kEngine = h->engine;
-  }
-  e = cudaGraphLaunch(c.exec, st);
-  if (e == cudaSuccess) h->launches += c.graphLaunches;
+  hoe_handle *hs[1] = {h};
+  const Members m{hs, 1, nullptr};
+  int64_t launches = 0;
+  cudaError_t e = run(h->cg.graph, m, &data, &w, &x, r, st, &launches);
+  h->launches += r.use_graph ? launches : 0;
+  return e;
+}
+
+cudaError_t cg_batch_solve(hoe_batch *b, const float2 *const *data, const float2 *const *w, float2 *const *x,
+                           const CgRequest &r, cudaStream_t st) {
+  const Members m{b->hs.data(), (int)b->hs.size(), b->tcplan};
+  int64_t launches = 0;
+  cudaError_t e = run(b->graph, m, data, w, x, r, st, &launches);
+  b->launches += launches;
   return e;
 }
 

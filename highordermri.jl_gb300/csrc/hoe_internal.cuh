@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 #include "hoexplicit.h"
 
 #define HOE_MAGIC 0x484f4531  // "HOE1"
@@ -106,6 +107,16 @@ struct CgRequest {
   double lambda = 0.0;
 };
 
+// A solve captured as a CUDA graph, replayed while its request is unchanged.
+struct CgGraph {
+  cudaStream_t cap = nullptr;         // capture stream
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches = 0;               // kernels per graph launch
+  std::vector<const void *> key;      // pointers of the captured request
+  int kIters = -1, kEngine = -1;
+  double kTol = 0.0, kLambda = 0.0;
+};
+
 struct CgState {
   void *base = nullptr;       // one allocation for the buffers below
   size_t bytes = 0;
@@ -113,14 +124,7 @@ struct CgState {
   float *D = nullptr;         // [nSam*nCha] |w|²
   double *part = nullptr;     // [2][304] block partials (pᴴq, ‖z‖²)
   CgScalars *S = nullptr;
-  cudaStream_t cap = nullptr; // capture stream
-  cudaGraphExec_t exec = nullptr;
-  int64_t graphLaunches = 0;  // kernels per graph launch
-  // the request the cached graph was captured for
-  const void *kData = nullptr, *kW = nullptr;
-  void *kX = nullptr;
-  int kIters = -1, kEngine = -1;
-  double kTol = 0.0, kLambda = 0.0;
+  CgGraph graph;
 };
 
 }  // namespace hoe
@@ -143,6 +147,19 @@ struct hoe_handle {
   hoe::TcState tc;
   void *tc_host = nullptr;   // tensor-core buffer table (hoe_tc.cu)
   hoe::CgState cg;           // device-resident CGNR (hoe_cg.cu)
+};
+
+#define HOE_BATCH_MAGIC 0x484f4542u
+
+// Several operators applied together (hoe_batch.cu).  Borrows its members.
+struct hoe_batch {
+  uint32_t magic = HOE_BATCH_MAGIC;
+  int device = 0;
+  std::vector<hoe_handle *> hs;
+  void *tcplan = nullptr;    // one persistent launch per direction (tensor-core members)
+  std::string err;
+  int64_t launches = 0;
+  hoe::CgGraph graph;        // cached batched CGNR
 };
 
 namespace hoe {
@@ -173,8 +190,12 @@ cudaError_t apply_adjoint_weighted(hoe_handle *h, const float2 *y, const float *
 // (as one cached CUDA graph when r.use_graph); cg_read_stats waits for st.
 cudaError_t cg_solve(hoe_handle *h, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
                      cudaStream_t st);
+// The same solve for every member of a batch in lockstep (one graph).
+cudaError_t cg_batch_solve(hoe_batch *b, const float2 *const *data, const float2 *const *w, float2 *const *x,
+                           const CgRequest &r, cudaStream_t st);
 cudaError_t cg_read_stats(const hoe_handle *h, cudaStream_t st, CgScalars *out);
 void cg_release(hoe_handle *h);
+void cg_graph_release(CgGraph &g);
 
 // Sets the thread's handle-less error message (hoe_last_error(NULL)).
 void record_error(const char *msg);
@@ -196,5 +217,15 @@ cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y,
 cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
 bool tc_supported(const hoe_handle *h, std::string *why);
 int *tc_error_word(const hoe_handle *h);   // device word set by a timed-out wait
+// Several operators (tensor-core engine, equal coil counts) in one persistent
+// launch per direction and residual width.  The plan borrows the handles.
+// tc_batch_forward reads each handle's prepared Z; y/D may be NULL per the
+// forward mode as in tc_forward.  tc_batch_adjoint_from_Yt reads each Yt.
+void *tc_batch_plan(hoe_handle *const *hs, int n, std::string *why);
+void tc_batch_plan_free(void *plan);
+int *tc_batch_error_word(void *plan);
+int tc_batch_launches(void *plan);         // contraction launches per direction
+cudaError_t tc_batch_forward(void *plan, float2 *const *y, const float *const *D, int mode, cudaStream_t st);
+cudaError_t tc_batch_adjoint_from_Yt(void *plan, float2 *const *x, cudaStream_t st);
 
 }  // namespace hoe

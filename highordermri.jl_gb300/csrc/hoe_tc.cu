@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 #include "hoe_internal.cuh"
 
@@ -247,25 +249,72 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
-struct TcParams {
+// One operator's operands for one direction.  A launch walks the work items
+// (row tile, column chunk) of its slices in order: slice si owns the global
+// items [first, first + nRowTiles*nColChunks).
+struct TcSlice {
   const float *rowHi, *rowLo;   // TF32 row-side residual tables: kappa (forward) / dbeta (adjoint)
   const float *colHi, *colLo;   // TF32 column-side residual tables: dbeta (forward) / kappa (adjoint)
   const float *rowAnchor;       // [colTile][rowAnchorStride]: Atab (forward) / Btab (adjoint)
   const float *colAnchor;       // [rowTile][colAnchorStride]: Btab (forward) / Atab (adjoint)
   const uint16_t *Bop;          // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
   float2 *part;                 // [slot][nRowPad][nChaPad] partial sums (zeroed before launch)
-  int *err;
+  int64_t first;                // global index of the slice's first work item
   int rowAnchorStride, colAnchorStride;
-  int nRowPad, nChaPad, nChaTC;
+  int nRowPad;
   int nColChunks;               // column chunks per row tile (C)
-  int64_t work;                 // nRowTiles * C work items, split evenly over gridDim.x CTAs
+  int nRowTiles;
+  int pad;
 };
+
+// Up to MS slices per launch (passed by value as a __grid_constant__
+// parameter: 96 bytes per slice, 32 slices fit the 4 KB parameter space).
+template <int MS>
+struct TcParams {
+  int *err;
+  int64_t work;                 // all slices' work items, split evenly over gridDim.x CTAs
+  int nSlices, nChaPad, nChaTC, pad;
+  TcSlice s[MS];
+};
+constexpr int kBatchSlices = 32;
+static_assert(sizeof(TcParams<kBatchSlices>) <= 4096, "kernel parameter space");
 
 // CTA that owns work item w when W items are split into G contiguous ranges
 // [b*W/G, (b+1)*W/G).
 __host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
   return (int)(((w + 1) * (int64_t)G - 1) / W);
 }
+
+// Position in the work sequence: slice si, row tile rt, column chunk ch.
+template <int MS>
+struct Cursor {
+  int si, rt, ch, C, nRT;
+  __device__ __forceinline__ void init(const TcParams<MS> &p, int64_t w) {
+    si = 0;
+    if constexpr (MS > 1) {
+      while (si + 1 < p.nSlices && p.s[si + 1].first <= w) ++si;
+    }
+    C = p.s[si].nColChunks;
+    nRT = p.s[si].nRowTiles;
+    const int64_t off = w - p.s[si].first;
+    rt = (int)(off / C);
+    ch = (int)(off % C);
+  }
+  __device__ __forceinline__ void next(const TcParams<MS> &p) {
+    if (++ch == C) {
+      ch = 0;
+      ++rt;
+      if constexpr (MS > 1) {
+        if (rt == nRT && si + 1 < p.nSlices) {
+          rt = 0;
+          ++si;
+          C = p.s[si].nColChunks;
+          nRT = p.s[si].nRowTiles;
+        }
+      }
+    }
+  }
+};
 
 // Tensor-memory plan (512 columns): BF16 phase tiles ABUF x [hi TV | lo TV]
 // columns (one 32-bit column per complex element), residual-phase tiles
@@ -314,8 +363,8 @@ constexpr int pick_stages() {
        : Smem<N, KP, 3>::BYTES <= 227 * 1024 ? 3 : 2;
 }
 
-template <int N, int KP, int NS>
-__global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
+template <int N, int KP, int NS, int MS>
+__global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
   using S = Smem<N, KP, NS>;
   constexpr int ABUF = S::ABUF, PD = S::PD, NISS = Tmem<N>::NISS;
   static_assert(PD >= 1, "residual-phase look-ahead");
@@ -344,11 +393,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
   constexpr uint32_t SBO_TF32 = (KP / 4) * 128;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int C = p.nColChunks;
   const int G = gridDim.x, b = blockIdx.x;
   const int64_t wb = (int64_t)b * p.work / G, we = (int64_t)(b + 1) * p.work / G;
   const int nIter = (int)(we - wb);
-  const int rt0 = (int)(wb / C), ch0 = (int)(wb % C);
+  Cursor<MS> c0;
+  c0.init(p, wb);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < NS; ++i) {
@@ -395,8 +444,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
     float acc[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) acc[i] = 0.f;
-    int curRT = -1, curTile = -1, grp = -1;
-    int pendGrp = -1, pendRT = -1;
+    int curTile = -1, grp = -1;
+    int pendGrp = -1, pendRT = -1, pendSI = 0;
     bool pendLast = false;
     float a = 0.f;
     bool ok = true;
@@ -412,11 +461,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
               tmem + laneBase + ACC_COL + (uint32_t)((g & 1) * NISS * N + q * N + qcol * NA);
           if constexpr (NA % 16 == 0) {
 #pragma unroll
-            for (int c0 = 0; c0 < NA; c0 += 16) {
+            for (int k0 = 0; k0 < NA; k0 += 16) {
               float v[16];
-              tmem_ld16(base + c0, v);
+              tmem_ld16(base + k0, v);
 #pragma unroll
-              for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+              for (int i = 0; i < 16; ++i) acc[k0 + i] += v[i];
             }
           } else if constexpr (NA == 8) {
             float v[8];
@@ -436,8 +485,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmemfree[g & 1]);
       if (pendLast) {
-        const int slot = b - work_owner((int64_t)pendRT * C, p.work, G);
-        float2 *dst = p.part + ((int64_t)slot * p.nRowPad + (int64_t)pendRT * TM + row) * p.nChaPad;
+        const TcSlice &ps = p.s[pendSI];
+        const int slot = b - work_owner(ps.first + (int64_t)pendRT * ps.nColChunks, p.work, G);
+        float2 *dst = ps.part + ((int64_t)slot * ps.nRowPad + (int64_t)pendRT * TM + row) * p.nChaPad;
         const int nOut = min(p.nChaTC, p.nChaPad);
         if (ok) {
 #pragma unroll
@@ -451,25 +501,25 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       }
       pendGrp = -1;
     };
-    int rt = rt0, ch = ch0;
+    Cursor<MS> c = c0;
     // anchor phase of the next anchor tile, loaded one stage ahead
     float aNext = nIter > 0
-        ? p.rowAnchor[(int64_t)(ch0 * TV / 128) * p.rowAnchorStride + rt0 * TM + row] : 0.f;
-    for (int it = 0; it < nIter && ok; ++it, ++ch) {
-      if (ch == C) { ch = 0; ++rt; }
-      if (it == 0 || ch % GROUP == 0) ++grp;
-      if (rt != curRT) { curRT = rt; curTile = -1; }
+        ? p.s[c.si].rowAnchor[(int64_t)(c.ch * TV / 128) * p.s[c.si].rowAnchorStride + c.rt * TM + row] : 0.f;
+    for (int it = 0; it < nIter && ok; ++it) {
+      if (it > 0) c.next(p);
+      if (it == 0 || c.ch % GROUP == 0) ++grp;
+      if (it == 0 || c.ch == 0) curTile = -1;  // new row tile
       const int slot = it % NS, round = it / NS;
-      const int colTile = ch * TV / 128;
+      const int colTile = c.ch * TV / 128;
       if (colTile != curTile) {
         a = aNext;
         curTile = colTile;
       }
-      {
-        int nch = ch + 1, nrt = rt;
-        if (nch == C) { nch = 0; ++nrt; }
-        if (it + 1 < nIter && (nrt != rt || nch * TV / 128 != colTile))
-          aNext = p.rowAnchor[(int64_t)(nch * TV / 128) * p.rowAnchorStride + nrt * TM + row];
+      if (it + 1 < nIter) {
+        Cursor<MS> n = c;
+        n.next(p);
+        if (n.ch == 0 || n.ch * TV / 128 != colTile)
+          aNext = p.s[n.si].rowAnchor[(int64_t)(n.ch * TV / 128) * p.s[n.si].rowAnchorStride + n.rt * TM + row];
       }
       // residual phase of this stage (TMEM), then release its buffer
       const int pb = it % PD, pr = it / PD;
@@ -513,10 +563,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       if (lane == 0) mbar_arrive(&afull[ab]);
       // the previous group is flushed one stage late, so its MMAs are done by now
       if (pendGrp >= 0) flush();
-      const bool endRT = (it == nIter - 1) || (ch + 1 == C);
-      if (endRT || (ch + 1) % GROUP == 0) {
+      const bool endRT = (it == nIter - 1) || (c.ch + 1 == c.C);
+      if (endRT || (c.ch + 1) % GROUP == 0) {
         pendGrp = grp;
-        pendRT = rt;
+        pendRT = c.rt;
+        pendSI = c.si;
         pendLast = endRT;
       }
     }
@@ -530,16 +581,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       constexpr uint32_t idescC = idesc_bf16(TM, N);
       uint64_t *lastBar = nullptr;
       uint32_t lastPar = 0;
-      int grp = -1, ch = ch0;
-      for (int it = 0; it < nIter; ++it, ++ch) {
-        if (ch == C) ch = 0;
+      int grp = -1;
+      Cursor<MS> c = c0;
+      for (int it = 0; it < nIter; ++it) {
+        if (it > 0) c.next(p);
+        const int ch = c.ch;
         const bool first = (it == 0) || (ch % GROUP == 0);
         if (first) {
           ++grp;
           // accumulator buffer grp&1 was last used by group grp-2: wait until it was read out
           if (grp >= 2 && !wait_bar(&tmemfree[grp & 1], ((grp >> 1) - 1) & 1, abort, p.err)) break;
         }
-        const bool last = (it == nIter - 1) || (ch + 1 == C) || ((ch + 1) % GROUP == 0);
+        const bool last = (it == nIter - 1) || (ch + 1 == c.C) || ((ch + 1) % GROUP == 0);
         const int slot = it % NS, round = it / NS;
         const int ab = it % ABUF, ar = it / ABUF;
         if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
@@ -575,10 +628,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
       constexpr uint32_t idescP = idesc_tf32(TM, TV);
       uint64_t *lastBar = nullptr;
       uint32_t lastPar = 0;
-      int kj = 0, ch = ch0;
-      for (int j = 0; j < nIter; ++j, ++ch) {
-        if (ch == C) { ch = 0; ++kj; }
-        const bool lastOfRow = (j == nIter - 1) || (ch + 1 == C);
+      int kj = 0;
+      Cursor<MS> c = c0;
+      for (int j = 0; j < nIter; ++j) {
+        if (j > 0) {
+          c.next(p);
+          if (c.ch == 0) ++kj;
+        }
+        const bool lastOfRow = (j == nIter - 1) || (c.ch + 1 == c.C);
         const int s = j % NS, r = j / NS;
         if (!wait_bar(&full[s], r & 1, abort, p.err)) break;
         if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
@@ -611,27 +668,29 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(TcParams p) {
     if (lane == 0) {
       const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + TV * 4;
       int issued = 0, kcount = -1, rowIssued = -1;
-      int rt = rt0, ch = ch0;
-      for (int it = 0; it < nIter; ++it, ++ch) {
-        if (ch == C) { ch = 0; ++rt; }
+      Cursor<MS> c = c0;
+      for (int it = 0; it < nIter; ++it) {
+        if (it > 0) c.next(p);
+        const TcSlice &sl = p.s[c.si];
+        const int rt = c.rt, ch = c.ch;
         if (it == 0 || ch == 0) {
           ++kcount;
           const int rb = kcount & 1;
           if (kcount >= 2 && !wait_bar(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err)) break;
           mbar_expect_tx(&rfull[rb], 2 * S::RV_TILE);
           const size_t ro = (size_t)rt * TM * KP;
-          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE, p.rowHi + ro, S::RV_TILE, &rfull[rb]);
-          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE + S::RV_TILE, p.rowLo + ro, S::RV_TILE, &rfull[rb]);
+          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE, sl.rowHi + ro, S::RV_TILE, &rfull[rb]);
+          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE + S::RV_TILE, sl.rowLo + ro, S::RV_TILE, &rfull[rb]);
           rowIssued = kcount;
         }
         const int slot = it % NS, round = it / NS;
         if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
         const size_t co = (size_t)ch * TV * KP;
         mbar_expect_tx(&full[slot], stageBytes);
-        bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, p.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
-        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, p.colHi + co, S::CV_TILE, &full[slot]);
-        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, p.colLo + co, S::CV_TILE, &full[slot]);
-        bulk_g2s(sCA + slot * TV, p.colAnchor + (int64_t)rt * p.colAnchorStride + ch * TV, TV * 4,
+        bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, sl.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
+        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, sl.colHi + co, S::CV_TILE, &full[slot]);
+        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, sl.colLo + co, S::CV_TILE, &full[slot]);
+        bulk_g2s(sCA + slot * TV, sl.colAnchor + (int64_t)rt * sl.colAnchorStride + ch * TV, TV * 4,
                  &full[slot]);
         issued = it + 1;
       }
@@ -707,10 +766,10 @@ struct Kern {
   static_assert(S::BYTES <= 227 * 1024, "shared memory plan exceeds 227 KB");
 };
 
-template <int N, int KP>
-cudaError_t launch_contract(const hoe_handle *h, const TcParams &p, int G, cudaStream_t st) {
+template <int N, int KP, int MS>
+cudaError_t launch_contract(const hoe_handle *h, const TcParams<MS> &p, int G, cudaStream_t st) {
   using K = Kern<N, KP>;
-  auto kern = k_tc_contract<N, KP, K::NS>;
+  auto kern = k_tc_contract<N, KP, K::NS, MS>;
   kern<<<G, THREADS, K::S::BYTES, st>>>(p);
   h->launches += 1;
   return cudaGetLastError();
@@ -718,10 +777,10 @@ cudaError_t launch_contract(const hoe_handle *h, const TcParams &p, int G, cudaS
 
 // One-time per (process, instantiation): shared-memory limit; returns the
 // resident CTAs per SM.
-template <int N, int KP>
+template <int N, int KP, int MS>
 int configure() {
   using K = Kern<N, KP>;
-  auto kern = k_tc_contract<N, KP, K::NS>;
+  auto kern = k_tc_contract<N, KP, K::NS, MS>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES) != cudaSuccess)
     return 0;
   int nb = 0;
@@ -729,39 +788,41 @@ int configure() {
   return nb;
 }
 
-template <int KP>
-cudaError_t launch_n(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
+template <int KP, int MS>
+cudaError_t launch_n(const hoe_handle *h, const TcParams<MS> &p, int N, int G, cudaStream_t st) {
   switch (N) {
-    case 16: return launch_contract<16, KP>(h, p, G, st);
-    case 32: return launch_contract<32, KP>(h, p, G, st);
-    case 64: return launch_contract<64, KP>(h, p, G, st);
-    default: return launch_contract<128, KP>(h, p, G, st);
+    case 16: return launch_contract<16, KP, MS>(h, p, G, st);
+    case 32: return launch_contract<32, KP, MS>(h, p, G, st);
+    case 64: return launch_contract<64, KP, MS>(h, p, G, st);
+    default: return launch_contract<128, KP, MS>(h, p, G, st);
   }
 }
 
-cudaError_t launch(const hoe_handle *h, const TcParams &p, int N, int G, cudaStream_t st) {
-  switch (h->t.KP) {
-    case 8: return launch_n<8>(h, p, N, G, st);
-    case 16: return launch_n<16>(h, p, N, G, st);
-    default: return launch_n<24>(h, p, N, G, st);
+template <int MS>
+cudaError_t launch(const hoe_handle *h, const TcParams<MS> &p, int KP, int N, int G, cudaStream_t st) {
+  switch (KP) {
+    case 8: return launch_n<8, MS>(h, p, N, G, st);
+    case 16: return launch_n<16, MS>(h, p, N, G, st);
+    default: return launch_n<24, MS>(h, p, N, G, st);
   }
 }
 
-template <int KP>
+template <int KP, int MS>
 int configure_n(int N) {
   switch (N) {
-    case 16: return configure<16, KP>();
-    case 32: return configure<32, KP>();
-    case 64: return configure<64, KP>();
-    default: return configure<128, KP>();
+    case 16: return configure<16, KP, MS>();
+    case 32: return configure<32, KP, MS>();
+    case 64: return configure<64, KP, MS>();
+    default: return configure<128, KP, MS>();
   }
 }
 
+template <int MS>
 int configure_kernel(int KP, int N) {
   switch (KP) {
-    case 8: return configure_n<8>(N);
-    case 16: return configure_n<16>(N);
-    default: return configure_n<24>(N);
+    case 8: return configure_n<8, MS>(N);
+    case 16: return configure_n<16, MS>(N);
+    default: return configure_n<24, MS>(N);
   }
 }
 
@@ -809,7 +870,7 @@ cudaError_t tc_prepare(hoe_handle *h) {
   TcBuffers b;
   b.nChaTC = tc_ncha(t.nCha);
   b.N = 2 * b.nChaTC;
-  const int bps = configure_kernel(t.KP, b.N);
+  const int bps = configure_kernel<1>(t.KP, b.N);
   if (bps < 1) return cudaErrorInvalidConfiguration;
   const int chunksF = t.nVoxPad / TV, chunksA = t.nSamPad / TV;
   const int G = h->numSMs * bps;
@@ -846,69 +907,231 @@ void tc_release(hoe_handle *h) {
   h->tc = TcState();
 }
 
-static TcParams base_params(const hoe_handle *h, const TcBuffers &b) {
-  TcParams p{};
-  p.part = b.part;
-  p.err = b.err;
-  p.nChaPad = h->t.nChaPad;
-  p.nChaTC = b.nChaTC;
-  return p;
+namespace {
+
+// Operands of one operator for one direction.
+TcSlice slice_forward(const hoe_handle *h, const TcBuffers &b) {
+  const auto &t = h->t;
+  TcSlice sl{};
+  sl.rowHi = t.kpHi; sl.rowLo = t.kpLo;
+  sl.colHi = t.dbHi; sl.colLo = t.dbLo;
+  sl.rowAnchor = t.Atab;
+  sl.rowAnchorStride = t.nSamPad;
+  sl.colAnchor = t.Btab;
+  sl.colAnchorStride = t.nVoxPad;
+  sl.Bop = b.bopF;
+  sl.part = b.part;
+  sl.nRowPad = t.nSamPad;
+  sl.nColChunks = t.nVoxPad / TV;
+  sl.nRowTiles = t.nSt;
+  return sl;
 }
 
-cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const float *D, int mode,
-                       cudaStream_t st) {
+TcSlice slice_adjoint(const hoe_handle *h, const TcBuffers &b) {
   const auto &t = h->t;
-  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  TcSlice sl{};
+  sl.rowHi = t.dbHi; sl.rowLo = t.dbLo;
+  sl.colHi = t.kpHi; sl.colLo = t.kpLo;
+  sl.rowAnchor = t.Btab;
+  sl.rowAnchorStride = t.nVoxPad;
+  sl.colAnchor = t.Atab;
+  sl.colAnchorStride = t.nSamPad;
+  sl.Bop = b.bopA;
+  sl.part = b.part;
+  sl.nRowPad = t.nVoxPad;
+  sl.nColChunks = t.nSamPad / TV;
+  sl.nRowTiles = t.nVt;
+  return sl;
+}
+
+// B operand tiles and zeroed partial slots before a contraction launch.
+cudaError_t pre_forward(const hoe_handle *h, const TcBuffers &b, int slots, cudaStream_t st) {
+  const auto &t = h->t;
   const int chunks = t.nVoxPad / TV;
   int64_t n = (int64_t)chunks * b.N * TK;
   k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Z, b.bopF, chunks, b.N, t.nChaPad);
   h->launches += 1;
-  TcParams p = base_params(h, b);
-  p.rowHi = t.kpHi; p.rowLo = t.kpLo;
-  p.colHi = t.dbHi; p.colLo = t.dbLo;
-  p.rowAnchor = t.Atab;
-  p.rowAnchorStride = t.nSamPad;
-  p.colAnchor = t.Btab;
-  p.colAnchorStride = t.nVoxPad;
-  p.Bop = b.bopF;
-  p.nRowPad = t.nSamPad;
-  p.nColChunks = chunks;
-  p.work = (int64_t)t.nSt * chunks;
-  cudaError_t e = cudaMemsetAsync(b.part, 0, (size_t)b.slotsF * t.nSamPad * t.nChaPad * sizeof(float2), st);
+  return cudaMemsetAsync(b.part, 0, (size_t)slots * t.nSamPad * t.nChaPad * sizeof(float2), st);
+}
+
+cudaError_t pre_adjoint(const hoe_handle *h, const TcBuffers &b, int slots, cudaStream_t st) {
+  const auto &t = h->t;
+  const int chunks = t.nSamPad / TV;
+  int64_t n = (int64_t)chunks * b.N * TK;
+  k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Yt, b.bopA, chunks, b.N, t.nChaPad);
+  h->launches += 1;
+  return cudaMemsetAsync(b.part, 0, (size_t)slots * t.nVoxPad * t.nChaPad * sizeof(float2), st);
+}
+
+TcParams<1> single_params(const hoe_handle *h, const TcBuffers &b, const TcSlice &sl) {
+  TcParams<1> p{};
+  p.err = b.err;
+  p.nSlices = 1;
+  p.nChaPad = h->t.nChaPad;
+  p.nChaTC = b.nChaTC;
+  p.s[0] = sl;
+  p.s[0].first = 0;
+  p.work = (int64_t)sl.nRowTiles * sl.nColChunks;
+  return p;
+}
+
+// Several operators with the same coil count in one persistent launch per
+// direction: slices grouped by residual width KP, at most kBatchSlices per
+// launch, work items of a group split evenly over its CTAs.
+struct TcBatchPlan {
+  struct Group {
+    int KP = 0, G_F = 1, G_A = 1;
+    std::vector<int> idx;                 // slices of this launch
+    TcParams<kBatchSlices> pF{}, pA{};
+  };
+  std::vector<hoe_handle *> hs;
+  std::vector<int> slotsF, slotsA;        // partial slots per slice
+  std::vector<Group> groups;
+  int *err = nullptr;                     // device word shared by the batch's launches
+};
+
+int slots_needed(int64_t first, int rowTiles, int C, int64_t W, int G) {
+  int J = 1;
+  for (int r = 0; r < rowTiles; ++r) {
+    int b0 = work_owner(first + (int64_t)r * C, W, G), b1 = work_owner(first + (int64_t)(r + 1) * C - 1, W, G);
+    J = std::max(J, b1 - b0 + 1);
+  }
+  return J;
+}
+
+}  // namespace
+
+cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const float *D, int mode,
+                       cudaStream_t st) {
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  cudaError_t e = pre_forward(h, b, b.slotsF, st);
   if (e != cudaSuccess) return e;
+  const TcParams<1> p = single_params(h, b, slice_forward(h, b));
   trace(h, EV_FK0, st);
-  e = launch(h, p, b.N, b.gridF, st);
+  e = launch(h, p, h->t.KP, b.N, b.gridF, st);
   trace(h, EV_FK1, st);
   if (e != cudaSuccess) return e;
   return simt_reduce_forward(h, b.part, b.slotsF, y, D, mode, st);
 }
 
 cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) {
-  const auto &t = h->t;
   const TcBuffers &b = *(const TcBuffers *)h->tc_host;
-  const int chunks = t.nSamPad / TV;
-  int64_t n = (int64_t)chunks * b.N * TK;
-  k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Yt, b.bopA, chunks, b.N, t.nChaPad);
-  h->launches += 1;
-  TcParams p = base_params(h, b);
-  p.rowHi = t.dbHi; p.rowLo = t.dbLo;
-  p.colHi = t.kpHi; p.colLo = t.kpLo;
-  p.rowAnchor = t.Btab;
-  p.rowAnchorStride = t.nVoxPad;
-  p.colAnchor = t.Atab;
-  p.colAnchorStride = t.nSamPad;
-  p.Bop = b.bopA;
-  p.nRowPad = t.nVoxPad;
-  p.nColChunks = chunks;
-  p.work = (int64_t)t.nVt * chunks;
-  cudaError_t e = cudaMemsetAsync(b.part, 0, (size_t)b.slotsA * t.nVoxPad * t.nChaPad * sizeof(float2), st);
+  cudaError_t e = pre_adjoint(h, b, b.slotsA, st);
   if (e != cudaSuccess) return e;
+  const TcParams<1> p = single_params(h, b, slice_adjoint(h, b));
   trace(h, EV_AK0, st);
-  e = launch(h, p, b.N, b.gridA, st);
+  e = launch(h, p, h->t.KP, b.N, b.gridA, st);
   trace(h, EV_AK1, st);
   if (e != cudaSuccess) return e;
   return simt_reduce_adjoint(h, b.part, b.slotsA, x, st);
 }
+
+void *tc_batch_plan(hoe_handle *const *hs, int n, std::string *why) {
+  auto *P = new TcBatchPlan();
+  P->hs.assign(hs, hs + n);
+  P->slotsF.assign(n, 1);
+  P->slotsA.assign(n, 1);
+  const TcBuffers &b0 = *(const TcBuffers *)hs[0]->tc_host;
+  // group by KP, in input order, at most kBatchSlices per launch
+  for (int KP : {8, 16, 24}) {
+    TcBatchPlan::Group g;
+    for (int i = 0; i < n; ++i) {
+      if (hs[i]->t.KP != KP) continue;
+      g.idx.push_back(i);
+      if ((int)g.idx.size() == kBatchSlices) { g.KP = KP; P->groups.push_back(g); g = TcBatchPlan::Group(); }
+    }
+    if (!g.idx.empty()) { g.KP = KP; P->groups.push_back(g); }
+  }
+  for (auto &g : P->groups) {
+    const int bps = configure_kernel<kBatchSlices>(g.KP, b0.N);
+    if (bps < 1) { if (why) *why = "batched kernel configuration"; delete P; return nullptr; }
+    for (int dir = 0; dir < 2; ++dir) {
+      TcParams<kBatchSlices> &p = dir == 0 ? g.pF : g.pA;
+      p = TcParams<kBatchSlices>{};
+      p.nSlices = (int)g.idx.size();
+      p.nChaPad = hs[g.idx[0]]->t.nChaPad;
+      p.nChaTC = b0.nChaTC;
+      int64_t W = 0;
+      for (int k = 0; k < p.nSlices; ++k) {
+        const hoe_handle *h = hs[g.idx[k]];
+        const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+        p.s[k] = dir == 0 ? slice_forward(h, b) : slice_adjoint(h, b);
+        p.s[k].first = W;
+        W += (int64_t)p.s[k].nRowTiles * p.s[k].nColChunks;
+      }
+      p.work = W;
+      const int G = (int)std::min<int64_t>((int64_t)hs[g.idx[0]]->numSMs * bps, W);
+      (dir == 0 ? g.G_F : g.G_A) = G;
+      for (int k = 0; k < p.nSlices; ++k) {
+        const int i = g.idx[k];
+        const hoe_handle *h = hs[i];
+        const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+        const int J = slots_needed(p.s[k].first, p.s[k].nRowTiles, p.s[k].nColChunks, W, G);
+        if ((size_t)J * p.s[k].nRowPad * h->t.nChaPad > b.partElems) {
+          if (why) *why = "partial-sum buffer of a slice too small for the batched schedule";
+          delete P;
+          return nullptr;
+        }
+        (dir == 0 ? P->slotsF : P->slotsA)[i] = J;
+      }
+    }
+  }
+  if (cudaMalloc(&P->err, sizeof(int)) != cudaSuccess || cudaMemset(P->err, 0, sizeof(int)) != cudaSuccess) {
+    if (P->err) cudaFree(P->err);
+    if (why) *why = "device allocation";
+    delete P;
+    return nullptr;
+  }
+  for (auto &g : P->groups) { g.pF.err = P->err; g.pA.err = P->err; }
+  return P;
+}
+
+void tc_batch_plan_free(void *plan) {
+  auto *P = (TcBatchPlan *)plan;
+  if (!P) return;
+  if (P->err) cudaFree(P->err);
+  delete P;
+}
+
+int *tc_batch_error_word(void *plan) { return plan ? ((TcBatchPlan *)plan)->err : nullptr; }
+
+cudaError_t tc_batch_forward(void *plan, float2 *const *y, const float *const *D, int mode, cudaStream_t st) {
+  auto *P = (TcBatchPlan *)plan;
+  const int n = (int)P->hs.size();
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i)
+    e = pre_forward(P->hs[i], *(const TcBuffers *)P->hs[i]->tc_host, P->slotsF[i], st);
+  for (size_t k = 0; k < P->groups.size() && e == cudaSuccess; ++k) {
+    const auto &g = P->groups[k];
+    const hoe_handle *h0 = P->hs[g.idx[0]];
+    e = launch(h0, g.pF, g.KP, ((const TcBuffers *)h0->tc_host)->N, g.G_F, st);
+  }
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    const TcBuffers &b = *(const TcBuffers *)P->hs[i]->tc_host;
+    e = simt_reduce_forward(P->hs[i], b.part, P->slotsF[i], y ? y[i] : nullptr, D ? D[i] : nullptr, mode, st);
+  }
+  return e;
+}
+
+cudaError_t tc_batch_adjoint_from_Yt(void *plan, float2 *const *x, cudaStream_t st) {
+  auto *P = (TcBatchPlan *)plan;
+  const int n = (int)P->hs.size();
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i)
+    e = pre_adjoint(P->hs[i], *(const TcBuffers *)P->hs[i]->tc_host, P->slotsA[i], st);
+  for (size_t k = 0; k < P->groups.size() && e == cudaSuccess; ++k) {
+    const auto &g = P->groups[k];
+    const hoe_handle *h0 = P->hs[g.idx[0]];
+    e = launch(h0, g.pA, g.KP, ((const TcBuffers *)h0->tc_host)->N, g.G_A, st);
+  }
+  for (int i = 0; i < n && e == cudaSuccess; ++i) {
+    const TcBuffers &b = *(const TcBuffers *)P->hs[i]->tc_host;
+    e = simt_reduce_adjoint(P->hs[i], b.part, P->slotsA[i], x[i], st);
+  }
+  return e;
+}
+
+int tc_batch_launches(void *plan) { return plan ? (int)((TcBatchPlan *)plan)->groups.size() : 0; }
 
 int *tc_error_word(const hoe_handle *h) {
   return h->tc_host ? ((const TcBuffers *)h->tc_host)->err : nullptr;

@@ -12,10 +12,12 @@ from .operator import (AdjointOp, ExplicitGB300Op, HighOrderExplicitOp, NormalOp
                        WeightedOp, WeightingOp, close, compose, explicit_gpu_normal,
                        normalOperator)
 from .recon import CGNR, L2Regularization, recon_HOOp  # noqa: F401
+from .batch import OperatorBatch  # noqa: F401
 
 __all__ = [
     "ArgumentError", "DimensionMismatch", "HoeError", "OutOfMemoryError", "Grid",
     "basisfunc_spha", "prep_kspha", "prep_concomitant", "HighOrderExplicitOp", "ExplicitGB300Op",
     "AdjointOp", "NormalOp", "WeightingOp", "WeightedOp", "compose", "normalOperator",
     "explicit_gpu_normal", "close", "load", "CGNR", "L2Regularization", "recon_HOOp",
+    "OperatorBatch",
 ]

@@ -35,6 +35,8 @@ EXPORTED = (
     "hoe_last_error", "hoe_get_info", "hoe_set_engine", "hoe_forward", "hoe_adjoint",
     "hoe_normal", "hoe_derivative", "hoe_backward", "hoe_set_timing", "hoe_get_timings",
     "hoe_forward_noalloc", "hoe_check", "hoe_plan", "hoe_recon",
+    "hoe_batch_create", "hoe_batch_free", "hoe_batch_last_error", "hoe_batch_get_info",
+    "hoe_batch_forward", "hoe_batch_adjoint", "hoe_batch_normal", "hoe_batch_recon", "hoe_batch_check",
 )
 
 HOE_CG_ITERATION_LIMIT = 0
@@ -108,6 +110,12 @@ class HoeCgStats(ctypes.Structure):
     ]
 
 
+class HoeBatchInfo(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int32), ("contraction_launches", ctypes.c_int32), ("launches", ctypes.c_int64),
+    ]
+
+
 class HoeInfo(ctypes.Structure):
     _fields_ = [
         ("nSam", ctypes.c_int32), ("nCha", ctypes.c_int32), ("nVox", ctypes.c_int32),
@@ -157,8 +165,20 @@ def load():
     lib.hoe_plan.argtypes = [ctypes.POINTER(HoeDesc), ctypes.POINTER(HoeInfo)]
     lib.hoe_forward_noalloc.argtypes = [ctypes.POINTER(HoeRawModel), vp, vp, vp]
     lib.hoe_recon.argtypes = [H, vp, vp, vp, ctypes.POINTER(HoeCgParams), ctypes.POINTER(HoeCgStats), vp]
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    lib.hoe_batch_create.argtypes = [ctypes.POINTER(H), PP, ctypes.c_int32]
+    lib.hoe_batch_free.argtypes = [H]
+    lib.hoe_batch_free.restype = None
+    lib.hoe_batch_last_error.argtypes = [H]
+    lib.hoe_batch_last_error.restype = ctypes.c_char_p
+    lib.hoe_batch_get_info.argtypes = [H, ctypes.POINTER(HoeBatchInfo)]
+    lib.hoe_batch_forward.argtypes = [H, PP, PP, vp]
+    lib.hoe_batch_adjoint.argtypes = [H, PP, PP, vp]
+    lib.hoe_batch_normal.argtypes = [H, PP, PP, PP, vp]
+    lib.hoe_batch_recon.argtypes = [H, PP, PP, PP, ctypes.POINTER(HoeCgParams), ctypes.POINTER(HoeCgStats), vp]
+    lib.hoe_batch_check.argtypes = [H, vp]
     for name in EXPORTED:
-        if name not in ("hoe_free",):
+        if name not in ("hoe_free", "hoe_batch_free"):
             getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int
     if lib.hoe_abi_version() != HOE_ABI_VERSION:
         raise ImportError("libhoexplicit.so ABI version mismatch")
@@ -166,11 +186,14 @@ def load():
     return lib
 
 
-def check(rc: int, handle=None) -> None:
+def check(rc: int, handle=None, batch=None) -> None:
     """Map a status code to the exception type the reference would raise."""
     if rc == HOE_OK:
         return
-    msg = load().hoe_last_error(handle).decode(errors="replace")
+    if batch is not None:
+        msg = load().hoe_batch_last_error(batch).decode(errors="replace")
+    else:
+        msg = load().hoe_last_error(handle).decode(errors="replace")
     if rc in (HOE_ERR_ARG, HOE_ERR_CLOSED):
         raise ArgumentError(msg)
     if rc == HOE_ERR_DIM:

@@ -245,6 +245,43 @@ def config3(seed: int = 1003, n: int = 200, lines: int = 50, per_line: int = 200
                     kspha_dt=np.gradient(kspha, dwell, axis=1))
 
 
+def spiral_slice(seed, n: int, nSam: int, nCha: int = 16, d: float = 1e-3, dwell: float = 2e-6,
+                 name: str = "slice") -> Workload:
+    """One slice seeded as the 64x64 spiral workload, scaled to an n x n grid
+    at spacing d: single-shot Archimedean spiral of nSam samples to
+    kmax = 1/(2d), zeroth/second/third-order terms, +-50 Hz fieldmap, ring coils."""
+    rng = np.random.default_rng(seed)
+    grid = Grid(n, n, 1, d, d, d)
+    fov = n * d
+    kmax = 1.0 / (2 * d)
+    t = np.arange(nSam) * dwell
+    u = np.arange(nSam) / (nSam - 1)
+    turns = fov * kmax / 2
+    k = kmax * u * np.exp(2j * np.pi * turns * u)
+    kspha = np.zeros((16, nSam))
+    kspha[1], kspha[2] = k.real, k.imag
+    mask = np.ones(n * n, dtype=bool)
+    lin_peak = kmax * np.max(np.hypot(grid.x, grid.y))
+    _higher_orders(rng, grid, mask, kspha, t, lin_peak)
+    fm = _gauss_fieldmap(rng, grid, 3, 50.0)
+    csm = _ring_coils(rng, grid, nCha, fov)
+    x = _ellipse_phantom(rng, grid)
+    return Workload(f"{name}-{n}x{n}-{nSam}s-{nCha}c-16t", grid, kspha, t,
+                    fm.reshape(n, n, order="F"), csm.reshape(n, n, nCha, order="F"),
+                    mask.reshape(n, n, order="F"), x, dwell=dwell,
+                    kspha_dt=np.gradient(kspha, dwell, axis=1))
+
+
+def config5(seed: int = 1005, slices: int = 24, nCha: int = 16):
+    """24 slices of 160^2-224^2 voxels (steps of 8) with 8,000-20,000 samples
+    each (uneven), 16 coils: a list of Workloads."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(20, 29, slices) * 8
+    nsams = rng.integers(8000, 20001, slices)
+    return [spiral_slice(seed * 100 + i, int(sizes[i]), int(nsams[i]), nCha, name=f"cfg5-s{i:02d}")
+            for i in range(slices)]
+
+
 def small(seed: int = 7, shape=(9, 7, 1), nSam=300, nCha=3, nTerm=16, conc=False,
           masked=True) -> Workload:
     """Small random problem for parity tests at odd (non tile-multiple) sizes."""

@@ -38,6 +38,11 @@
  *                     explicit operator: the weighting W∘HOOp and normal EᴴWᴴWE of
  *                     :73-78 and the CGNR solve!(solver, Data) of :79-80
  *                     (RegularizedLeastSquares CGNR with L2Regularization)
+ *   hoe_batch_*       no batched counterpart: the reference builds one operator per
+ *                     slice (explicit_gpu_operator.jl:299-392) and calls its products
+ *                     and recon_HOOp (recon_HOOp.jl:52-88) slice by slice; a batch
+ *                     runs all slices' products in one persistent launch per
+ *                     direction and their CGNR solves in one CUDA graph
  *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
  *   hoe_free          releases the host handle (Julia finalizer)
  *   hoe_set_timing / hoe_get_timings
@@ -90,6 +95,7 @@ extern "C" {
 #define HOE_GRAD_T0_COEF   8     /* dL/dt0 includes the coefficient part -bf.kspha_dt */
 
 typedef struct hoe_handle hoe_handle;
+typedef struct hoe_batch hoe_batch;
 
 typedef struct hoe_desc {
     int32_t abi_version;      /* = HOE_ABI_VERSION                                     */
@@ -137,6 +143,12 @@ typedef struct hoe_cg_stats {
     double  residual0;             /* ||z_0|| = ||E^H W^H W data||                        */
     double  residual;              /* ||z_k|| = ||E^H W^H (W data - W E x) - lambda x||   */
 } hoe_cg_stats;
+
+typedef struct hoe_batch_info {
+    int32_t n;                     /* member operators                                   */
+    int32_t contraction_launches;  /* contraction kernels per direction for all members  */
+    int64_t launches;              /* kernels launched by batch calls so far             */
+} hoe_batch_info;
 
 typedef struct hoe_info {
     int32_t nSam, nCha, nVox, nTermEff, nFull;
@@ -208,6 +220,31 @@ HOE_API int  hoe_backward(hoe_handle *h, const void *x_dev, const void *r_dev,
  * and identical with and without the graph. */
 HOE_API int  hoe_recon(hoe_handle *h, const void *data_dev, const void *weights_dev, void *x_dev,
                        const hoe_cg_params *params, hoe_cg_stats *stats, void *stream);
+
+/* Batches of operators on one device (e.g. the slices of a multi-slice scan).
+ * A batch borrows its members: free the batch before freeing a member, and a
+ * closed member makes every batch call return HOE_ERR_CLOSED.  When every
+ * member uses the tensor-core engine and all have the same coil count, each
+ * direction of all members runs in one persistent contraction launch (one per
+ * residual width, at most 32 members per launch); otherwise the members are
+ * applied one after another.  Vector arguments are HOST arrays of n device
+ * pointers, one per member, in member order. */
+HOE_API int  hoe_batch_create(hoe_batch **out, hoe_handle *const *ops, int32_t n);
+HOE_API void hoe_batch_free(hoe_batch *b);
+HOE_API const char *hoe_batch_last_error(const hoe_batch *b);
+HOE_API int  hoe_batch_get_info(const hoe_batch *b, hoe_batch_info *out);
+HOE_API int  hoe_batch_forward(hoe_batch *b, const void *const *x_dev, void *const *y_dev, void *stream);
+HOE_API int  hoe_batch_adjoint(hoe_batch *b, const void *const *y_dev, void *const *x_dev, void *stream);
+/* D_dev may be NULL (ones for every member) or hold NULL entries. */
+HOE_API int  hoe_batch_normal(hoe_batch *b, const float *const *D_dev, const void *const *x_dev,
+                              void *const *out_dev, void *stream);
+/* hoe_recon for every member with the same parameters, in lockstep; weights_dev
+ * may be NULL or hold NULL entries (ones); stats: NULL or n entries. */
+HOE_API int  hoe_batch_recon(hoe_batch *b, const void *const *data_dev, const void *const *weights_dev,
+                             void *const *x_dev, const hoe_cg_params *params, hoe_cg_stats *stats,
+                             void *stream);
+/* hoe_check for the batch's launches and for every member. */
+HOE_API int  hoe_batch_check(hoe_batch *b, void *stream);
 
 /* ---------------------------------------------------------------------------
  * Allocation-free forward.  No counterpart in the reference.
