@@ -382,6 +382,30 @@ def run_batch(a):
         torch.distributed.destroy_process_group()
 
 
+def time_backward(op, x, y, flush, stream, reps):
+    """dL/d(kspha, fieldmap, t0) of L = 0.5*||E x - y||^2 at the workload's
+    shapes (hoe_backward, gradients 20 x nSam, nFull and one scalar)."""
+    import torch
+    r = op * x - y
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    op.backward(x, r)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        op.backward(x, r, kspha=True, fieldmap=True, t0_b0=True)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms.append(ev0.elapsed_time(ev1))
+    m = statistics.mean(ms)
+    pairs = float(op.nVox) * op.nSam
+    return {"ms_per_call": m, "value": pairs / (m / 1e3), "unit": UNIT,
+            "outputs": f"dL/dkspha {op.nTermEff}x{op.nSam}, dL/dfieldmap {op.ncol}, dL/dt0 scalar",
+            "engine": "fp32 (CUDA cores)"}
+
+
 def run_gb300(a):
     import torch
     ws, rank, local = dist_env()
@@ -487,6 +511,10 @@ def run_gb300(a):
             out["recon"] = time_recon(op, w, y, flush, stream, a.recon_iterations, max(3, a.steps // 4))
         except Exception as exc:  # report, do not substitute
             out["recon"] = {"error": str(exc)}
+        try:
+            out["backward"] = time_backward(op, x, y, flush, stream, max(3, a.steps // 4))
+        except Exception as exc:  # report, do not substitute
+            out["backward"] = {"error": str(exc)}
 
     # end-to-end through the public API with host (pinned) buffers
     if not a.no_e2e:

@@ -98,6 +98,8 @@ void release_device(hoe_handle *h) {
   dfree(t.dbeta); dfree(t.kappa); dfree(t.Atab); dfree(t.Btab); dfree(t.csm);
   dfree(t.dbHi); dfree(t.dbLo); dfree(t.kpHi); dfree(t.kpLo);
   dfree(t.perm);  dfree(t.bfraw); dfree(t.kdot); dfree(t.times);
+  dfree(t.beta64); dfree(t.betabar); dfree(t.gambar); dfree(t.kap64); dfree(t.times64);
+  dfree(t.bal); dfree(t.Vr);
   auto &s = h->s;
   dfree(s.Z); dfree(s.Yt); dfree(s.part); dfree(s.gpart); dfree(s.dred);
   h->bytes = 0;
@@ -189,7 +191,7 @@ namespace {
 struct Plan {
   hoe::Tables t;                                   // sizes (device pointers unused)
   std::vector<int> order, perm;
-  std::vector<double> beta64, gam64, betabar, gambar, kap64;
+  std::vector<double> beta64, gam64, betabar, gambar, kap64, bal, Vr;
   std::vector<float> dbeta, kappa, bfraw, kdot, times_f;
   std::vector<float> dbHi, dbLo, kpHi, kpLo;   // TF32 hi/lo, UMMA K-major tiles
   std::vector<float2> csm;
@@ -368,7 +370,8 @@ int make_plan(const hoe_desc *d, Plan &P) {
   for (int s = 0; s < nSam; ++s)
     for (int l = 0; l < R; ++l)
       kap64[(size_t)s * R + l] = gam64[(size_t)s * R + l] - gambar[(size_t)(s / t.ST) * R + l];
-  std::vector<double> bal(R, 1.0);
+  auto &bal = P.bal;
+  bal.assign(R, 1.0);
   for (int l = 0; l < R; ++l) {
     double a = 0, b = 0;
     for (int p = 0; p < nVox; ++p) a = std::max(a, std::fabs(db64[(size_t)p * R + l]));
@@ -376,7 +379,7 @@ int make_plan(const hoe_desc *d, Plan &P) {
     if (a > 0 && b > 0) bal[l] = std::sqrt(b / a);
   }
   // ---- reduced basis: Householder QR of the balanced dbeta, Jacobi SVD of R ----
-  std::vector<double> Vr;  // [R][r] right singular vectors kept
+  auto &Vr = P.Vr;  // [R][r] right singular vectors kept
   int rank = 0;
   {
     std::vector<double> A((size_t)nVox * R);  // column-major nVox x R
@@ -588,7 +591,6 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
 
   // ---- device allocations ----
   Allocator al(h);
-  double *d_beta64 = nullptr, *d_kap64 = nullptr, *d_betabar = nullptr, *d_gambar = nullptr;
   cudaError_t e = cudaSuccess;
   auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
   A(al.alloc(&t.dbeta, dbeta.size()));
@@ -608,16 +610,20 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   A(al.alloc(&h->s.Yt, (size_t)t.nSamPad * t.nChaPad));
   h->s.partElems = std::max((size_t)h->splitF * t.nSamPad, (size_t)h->splitA * t.nVoxPad) * t.nChaPad;
   A(al.alloc(&h->s.part, h->s.partElems));
+  A(al.alloc(&t.beta64, beta64.size()));
+  A(al.alloc(&t.betabar, betabar.size()));
+  A(al.alloc(&t.gambar, gambar.size()));
+  A(al.alloc(&t.kap64, kap64.size()));
+  A(al.alloc(&t.times64, (size_t)t.nSamPad));
+  A(al.alloc(&t.bal, P.bal.size()));
+  A(al.alloc(&t.Vr, std::max<size_t>(P.Vr.size(), 1)));
   if (e != cudaSuccess) {
     release_device(h);
     delete h;
     return cuda_fail(nullptr, e, "hoe_create: device allocation");
   }
-  // staging for the FP64 tables (freed before returning)
-  A(cudaMalloc(&d_beta64, beta64.size() * sizeof(double)));
-  A(cudaMalloc(&d_kap64, kap64.size() * sizeof(double)));
-  A(cudaMalloc(&d_betabar, betabar.size() * sizeof(double)));
-  A(cudaMalloc(&d_gambar, gambar.size() * sizeof(double)));
+  std::vector<double> times64(t.nSamPad, 0.0);
+  for (int s = 0; s < nSam; ++s) times64[s] = d->times[s];
   auto H2D = [&](void *dst, const void *src, size_t bytes) { A(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice)); };
   if (e == cudaSuccess) {
     H2D(t.dbeta, dbeta.data(), dbeta.size() * sizeof(float));
@@ -631,19 +637,18 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
     H2D(t.bfraw, bfraw.data(), bfraw.size() * sizeof(float));
     H2D(t.kdot, kdot.data(), kdot.size() * sizeof(float));
     H2D(t.times, times_f.data(), times_f.size() * sizeof(float));
-    H2D(d_beta64, beta64.data(), beta64.size() * sizeof(double));
-    H2D(d_kap64, kap64.data(), kap64.size() * sizeof(double));
-    H2D(d_betabar, betabar.data(), betabar.size() * sizeof(double));
-    H2D(d_gambar, gambar.data(), gambar.size() * sizeof(double));
+    H2D(t.beta64, beta64.data(), beta64.size() * sizeof(double));
+    H2D(t.kap64, kap64.data(), kap64.size() * sizeof(double));
+    H2D(t.betabar, betabar.data(), betabar.size() * sizeof(double));
+    H2D(t.gambar, gambar.data(), gambar.size() * sizeof(double));
+    H2D(t.times64, times64.data(), times64.size() * sizeof(double));
+    H2D(t.bal, P.bal.data(), P.bal.size() * sizeof(double));
+    if (!P.Vr.empty()) H2D(t.Vr, P.Vr.data(), P.Vr.size() * sizeof(double));
   }
   if (e == cudaSuccess) {
-    int64_t nA = (int64_t)t.nVt * t.nSamPad, nB = (int64_t)t.nSt * t.nVoxPad;
-    k_table_A<<<(unsigned)((nA + 255) / 256), 256>>>(d_betabar, d_kap64, t.Atab, R, t.nVt, t.nSamPad, nSam);
-    k_table_B<<<(unsigned)((nB + 255) / 256), 256>>>(d_beta64, d_gambar, t.perm, t.Btab, R, t.nSt, t.nVoxPad);
-    A(cudaGetLastError());
+    A(hoe::build_anchor_tables(h, 0));
     A(cudaDeviceSynchronize());
   }
-  cudaFree(d_beta64); cudaFree(d_kap64); cudaFree(d_betabar); cudaFree(d_gambar);
   if (e != cudaSuccess) {
     release_device(h);
     delete h;
@@ -860,9 +865,73 @@ int hoe_recon(hoe_handle *h, const void *data, const void *weights, void *x, con
   return HOE_OK;
 }
 
+int hoe_set_kspha(hoe_handle *h, const double *kspha, const double *kspha_dt, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!kspha) return fail(h, HOE_ERR_ARG, "kspha must be a device pointer");
+  DeviceGuard guard(h->device);
+  cudaError_t e = hoe::replan_samples(h, kspha, h->t.R0, kspha_dt, h->t.nTerm, nullptr, (cudaStream_t)stream);
+  return finish(h, e, "hoe_set_kspha");
+}
+
+int hoe_kdot_stencil(const double *traj, int64_t nField, int32_t nTerm, double dt, double *out, void *stream) {
+  if (!traj || !out) return fail(nullptr, HOE_ERR_ARG, "traj and out must be device pointers");
+  if (nField < 1 || nTerm < 1) return fail(nullptr, HOE_ERR_ARG, "nField and nTerm must be positive");
+  if (!(dt > 0.0) || !std::isfinite(dt)) return fail(nullptr, HOE_ERR_ARG, "dt must be finite and positive");
+  cudaError_t e = hoe::kdot_stencil(traj, nField, nTerm, dt, out, (cudaStream_t)stream);
+  return finish(nullptr, e, "hoe_kdot_stencil");
+}
+
+int hoe_interp_traj_time(const double *traj, int64_t nField, int32_t nTerm, double dt, double delTime,
+                         const double *datatime, int64_t nData, double *out, int32_t layout, void *stream) {
+  if (!traj || !datatime || !out) return fail(nullptr, HOE_ERR_ARG, "traj, datatime and out must be device pointers");
+  if (nField < 2 || nTerm < 1 || nData < 1)
+    return fail(nullptr, HOE_ERR_ARG, "need nField >= 2, nTerm >= 1 and nData >= 1");
+  if (!(dt > 0.0) || !std::isfinite(dt) || !std::isfinite(delTime))
+    return fail(nullptr, HOE_ERR_ARG, "dt must be finite and positive, delTime finite");
+  if (layout != 0 && layout != 1) return fail(nullptr, HOE_ERR_ARG, "layout must be 0 or 1");
+  cudaError_t e = hoe::interp_akima(traj, nField, nTerm, dt, nullptr, delTime, datatime, nData, out, layout, nTerm,
+                                    nullptr, (cudaStream_t)stream);
+  return finish(nullptr, e, "hoe_interp_traj_time");
+}
+
+int hoe_find_delay(hoe_handle *h, const hoe_delay_params *p, const void *data, const void *weights,
+                   const double *traj, int64_t nField, void *x, hoe_delay_result *out, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!p || !out) return fail(h, HOE_ERR_ARG, "params and out must not be NULL");
+  if (!data || !traj) return fail(h, HOE_ERR_ARG, "data and traj must be device pointers");
+  if (h->t.R0 != h->t.nTerm)
+    return fail(h, HOE_ERR_ARG, "delay estimation needs an operator without concomitant terms");
+  if (nField < 2) return fail(h, HOE_ERR_ARG, "need at least two coefficient samples");
+  if (!(p->dt > 0.0) || !std::isfinite(p->dt)) return fail(h, HOE_ERR_ARG, "dt must be finite and positive");
+  if (!(p->dtau_min > 0.0) || !std::isfinite(p->dtau_min))
+    return fail(h, HOE_ERR_ARG, "dtau_min must be finite and positive");
+  if (!(p->jump_fact >= 1.0) || !std::isfinite(p->jump_fact)) return fail(h, HOE_ERR_ARG, "jump_fact must be >= 1");
+  if (!(p->lambda >= 0.0) || !std::isfinite(p->lambda)) return fail(h, HOE_ERR_ARG, "lambda must be finite and >= 0");
+  if (!std::isfinite(p->start_time)) return fail(h, HOE_ERR_ARG, "start_time must be finite");
+  if (p->iter_max < 0 || p->max_outer < 1) return fail(h, HOE_ERR_ARG, "iter_max >= 0 and max_outer >= 1 required");
+  DeviceGuard guard(h->device);
+  memset(out, 0, sizeof(*out));
+  cudaError_t e = hoe::find_delay(h, *p, (const float2 *)data, (const float2 *)weights, traj, nField, (float2 *)x,
+                                  out, (cudaStream_t)stream);
+  return finish(h, e, "hoe_find_delay");
+}
+
 }  // extern "C"
 
 namespace hoe {
+
+cudaError_t build_anchor_tables(const hoe_handle *h, cudaStream_t st) {
+  const auto &t = h->t;
+  int64_t nA = (int64_t)t.nVt * t.nSamPad, nB = (int64_t)t.nSt * t.nVoxPad;
+  k_table_A<<<(unsigned)((nA + 255) / 256), 256, 0, st>>>(t.betabar, t.kap64, t.Atab, t.R, t.nVt, t.nSamPad,
+                                                          t.nSam);
+  k_table_B<<<(unsigned)((nB + 255) / 256), 256, 0, st>>>(t.beta64, t.gambar, t.perm, t.Btab, t.R, t.nSt,
+                                                          t.nVoxPad);
+  h->launches += 2;
+  return cudaGetLastError();
+}
 
 cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {
   cudaError_t e = prep_Z(h, x, st);

@@ -429,6 +429,15 @@ cudaError_t cg_batch_solve(hoe_batch *b, const float2 *const *data, const float2
   return e;
 }
 
+cudaError_t cg_prepare(hoe_handle *h) { return ensure_buffers(h); }
+
+cudaError_t cg_enqueue(hoe_handle *h, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
+                       cudaStream_t st) {
+  hoe_handle *hs[1] = {h};
+  const Members m{hs, 1, nullptr};
+  return enqueue_solve(m, &data, &w, &x, r, st);
+}
+
 cudaError_t cg_read_stats(const hoe_handle *h, cudaStream_t st, CgScalars *out) {
   cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return e;

@@ -71,6 +71,16 @@ struct Tables {
   float  *bfraw = nullptr;   // [nVoxPad][kRF] bf (R0 terms) and fieldmap at slot R0
   float  *kdot  = nullptr;   // [nSamPad][kRF] kspha_dt (nTerm terms), zero elsewhere
   float  *times = nullptr;   // [nSamPad]
+  // FP64 planning arrays kept for re-planning the sample side on the device
+  // (hoe_set_kspha): beta and its tile anchors, the sample-tile anchors and
+  // residuals, times, and the balancing / reduced basis of the residual.
+  double *beta64 = nullptr;   // [nVoxPad][R]
+  double *betabar = nullptr;  // [nVt][R]
+  double *gambar = nullptr;   // [nSt][R]
+  double *kap64 = nullptr;    // [nSamPad][R]
+  double *times64 = nullptr;  // [nSamPad]
+  double *bal = nullptr;      // [R]
+  double *Vr = nullptr;       // [R][rank]
 };
 
 struct Scratch {
@@ -196,6 +206,30 @@ cudaError_t cg_batch_solve(hoe_batch *b, const float2 *const *data, const float2
 cudaError_t cg_read_stats(const hoe_handle *h, cudaStream_t st, CgScalars *out);
 void cg_release(hoe_handle *h);
 void cg_graph_release(CgGraph &g);
+
+// Anchor-phase tables Atab/Btab from the FP64 planning arrays (hoe_api.cu).
+cudaError_t build_anchor_tables(const hoe_handle *h, cudaStream_t st);
+
+// Sample-side re-plan for new coefficients (hoe_sync.cu): kspha[s*ldk + l]
+// (l < R0, FP64), kdot[s*ldd + l] (l < nTerm, FP64) or NULL.  Scaled by
+// termMask[l] when given.  Stream-ordered.
+cudaError_t replan_samples(hoe_handle *h, const double *kspha, int ldk, const double *kdot, int ldd,
+                           const double *termMask, cudaStream_t st);
+
+// Trajectory preprocessing and delay estimation (hoe_sync.cu).
+cudaError_t kdot_stencil(const double *traj, int64_t n, int nTerm, double dt, double *out, cudaStream_t st);
+cudaError_t interp_akima(const double *traj, int64_t n, int nTerm, double dt, const double *delTimeDev,
+                         double delTimeHost, const double *datatime, int64_t nData, double *out, int layout,
+                         int ldo, const double *termMask, cudaStream_t st);
+cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *data, const float2 *weights,
+                       const double *traj, int64_t nField, float2 *xOut, hoe_delay_result *res, cudaStream_t st);
+
+// Solver building blocks for larger captured sequences (hoe_cg.cu):
+// cg_prepare allocates the solver buffers (outside any capture), cg_enqueue
+// enqueues one complete solve without a graph of its own.
+cudaError_t cg_prepare(hoe_handle *h);
+cudaError_t cg_enqueue(hoe_handle *h, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
+                       cudaStream_t st);
 
 // Sets the thread's handle-less error message (hoe_last_error(NULL)).
 void record_error(const char *msg);

@@ -13,11 +13,12 @@ from .operator import (AdjointOp, ExplicitGB300Op, HighOrderExplicitOp, NormalOp
                        normalOperator)
 from .recon import CGNR, L2Regularization, recon_HOOp  # noqa: F401
 from .batch import OperatorBatch  # noqa: F401
+from .sync import FindDelay, InterpTrajTime, kspha_dt, set_kspha  # noqa: F401
 
 __all__ = [
     "ArgumentError", "DimensionMismatch", "HoeError", "OutOfMemoryError", "Grid",
     "basisfunc_spha", "prep_kspha", "prep_concomitant", "HighOrderExplicitOp", "ExplicitGB300Op",
     "AdjointOp", "NormalOp", "WeightingOp", "WeightedOp", "compose", "normalOperator",
     "explicit_gpu_normal", "close", "load", "CGNR", "L2Regularization", "recon_HOOp",
-    "OperatorBatch",
+    "OperatorBatch", "FindDelay", "InterpTrajTime", "kspha_dt", "set_kspha",
 ]

@@ -37,6 +37,7 @@ EXPORTED = (
     "hoe_forward_noalloc", "hoe_check", "hoe_plan", "hoe_recon",
     "hoe_batch_create", "hoe_batch_free", "hoe_batch_last_error", "hoe_batch_get_info",
     "hoe_batch_forward", "hoe_batch_adjoint", "hoe_batch_normal", "hoe_batch_recon", "hoe_batch_check",
+    "hoe_set_kspha", "hoe_kdot_stencil", "hoe_interp_traj_time", "hoe_find_delay",
 )
 
 HOE_CG_ITERATION_LIMIT = 0
@@ -110,6 +111,22 @@ class HoeCgStats(ctypes.Structure):
     ]
 
 
+class HoeDelayParams(ctypes.Structure):
+    _fields_ = [
+        ("start_time", ctypes.c_double), ("dt", ctypes.c_double), ("dtau_min", ctypes.c_double),
+        ("jump_fact", ctypes.c_double), ("lambda_", ctypes.c_double),
+        ("term_mask", ctypes.POINTER(ctypes.c_double)),
+        ("iter_max", ctypes.c_int32), ("max_outer", ctypes.c_int32),
+    ]
+
+
+class HoeDelayResult(ctypes.Structure):
+    _fields_ = [
+        ("tau", ctypes.c_double), ("tau_last", ctypes.c_double), ("dtau", ctypes.c_double),
+        ("jump", ctypes.c_double), ("iterations", ctypes.c_int32), ("status", ctypes.c_int32),
+    ]
+
+
 class HoeBatchInfo(ctypes.Structure):
     _fields_ = [
         ("n", ctypes.c_int32), ("contraction_launches", ctypes.c_int32), ("launches", ctypes.c_int64),
@@ -177,6 +194,13 @@ def load():
     lib.hoe_batch_normal.argtypes = [H, PP, PP, PP, vp]
     lib.hoe_batch_recon.argtypes = [H, PP, PP, PP, ctypes.POINTER(HoeCgParams), ctypes.POINTER(HoeCgStats), vp]
     lib.hoe_batch_check.argtypes = [H, vp]
+    I64 = ctypes.c_int64
+    lib.hoe_set_kspha.argtypes = [H, vp, vp, vp]
+    lib.hoe_kdot_stencil.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, vp, vp]
+    lib.hoe_interp_traj_time.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, ctypes.c_double, vp, I64, vp,
+                                         ctypes.c_int32, vp]
+    lib.hoe_find_delay.argtypes = [H, ctypes.POINTER(HoeDelayParams), vp, vp, vp, I64, vp,
+                                   ctypes.POINTER(HoeDelayResult), vp]
     for name in EXPORTED:
         if name not in ("hoe_free", "hoe_batch_free"):
             getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int

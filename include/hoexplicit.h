@@ -43,6 +43,13 @@
  *                     and recon_HOOp (recon_HOOp.jl:52-88) slice by slice; a batch
  *                     runs all slices' products in one persistent launch per
  *                     direction and their CGNR solves in one CUDA graph
+ *   hoe_set_kspha     the per-iteration operator rebuilds of FindDelay.jl:190-193
+ *                     (HighOrderExplicitOp(gridding, kspha_τ, datatime; ...)), done on
+ *                     the device for the sample side only
+ *   hoe_kdot_stencil  kspha_dt of FindDelay.jl:179-180
+ *   hoe_interp_traj_time
+ *                     InterpTrajTime, src/Synchronization/InterpTraj.jl:18-40 (Akima)
+ *   hoe_find_delay    FindDelay, src/Synchronization/FindDelay.jl:139-214
  *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
  *   hoe_free          releases the host handle (Julia finalizer)
  *   hoe_set_timing / hoe_get_timings
@@ -144,6 +151,29 @@ typedef struct hoe_cg_stats {
     double  residual;              /* ||z_k|| = ||E^H W^H (W data - W E x) - lambda x||   */
 } hoe_cg_stats;
 
+/* Parameters of hoe_find_delay (the keywords of FindDelay). */
+typedef struct hoe_delay_params {
+    double  start_time;            /* StartTime (s): coefficient sample j sits at
+                                      (j-1)*dt - (start_time + tau)                      */
+    double  dt;                    /* coefficient sampling interval (s), > 0             */
+    double  dtau_min;              /* Δτ_min (s), > 0: stop once |Δτ| <= dtau_min        */
+    double  jump_fact;             /* JumpFact, >= 1 (reference default 3)               */
+    double  lambda;                /* L2Regularization weight of the image solve, >= 0   */
+    const double *term_mask;       /* HOST [nTerm] factors from recon_terms, or NULL     */
+    int32_t iter_max;              /* CGNR iterations per image solve (default 10)       */
+    int32_t max_outer;             /* bound on delay updates (the reference has none)    */
+} hoe_delay_params;
+
+typedef struct hoe_delay_result {
+    double  tau;                   /* returned delay tau_last - dtau/J*(J-1) (s)         */
+    double  tau_last;              /* accumulated delay (s)                              */
+    double  dtau;                  /* last increment (s)                                 */
+    double  jump;                  /* final JumpFact                                     */
+    int32_t iterations;            /* delay updates made                                 */
+    int32_t status;                /* 0 converged, 1 max_outer reached,
+                                      2 stopped: ||B x|| = 0 or a non-finite update      */
+} hoe_delay_result;
+
 typedef struct hoe_batch_info {
     int32_t n;                     /* member operators                                   */
     int32_t contraction_launches;  /* contraction kernels per direction for all members  */
@@ -220,6 +250,35 @@ HOE_API int  hoe_backward(hoe_handle *h, const void *x_dev, const void *r_dev,
  * and identical with and without the graph. */
 HOE_API int  hoe_recon(hoe_handle *h, const void *data_dev, const void *weights_dev, void *x_dev,
                        const hoe_cg_params *params, hoe_cg_stats *stats, void *stream);
+
+/* Trajectory preprocessing (no handle).  traj_dev: float64 [nField x nTerm]
+ * column-major (the reference's (nFieldSample, nTerm) coefficient series). */
+HOE_API int  hoe_kdot_stencil(const double *traj_dev, int64_t nField, int32_t nTerm, double dt,
+                              double *out_dev, void *stream);
+/* InterpTrajTime: Akima interpolation of every column at datatime_dev
+ * [nData], coefficient sample j at j*dt - delTime (0-based), zero outside.
+ * layout 0: out [nData x nTerm] column-major (the reference's result);
+ * layout 1: out [nTerm x nData] column-major (the operator's kspha layout). */
+HOE_API int  hoe_interp_traj_time(const double *traj_dev, int64_t nField, int32_t nTerm, double dt,
+                                  double delTime, const double *datatime_dev, int64_t nData,
+                                  double *out_dev, int32_t layout, void *stream);
+/* Replaces the operator's coefficients on the device: kspha_dev float64
+ * [nTermEff x nSam] as desc.kspha (after prep_kspha / prep_concomitant),
+ * kspha_dt_dev float64 [nTerm x nSam] or NULL (keeps the derivative table).
+ * The voxel side and the reduced residual basis are kept; the sample-tile
+ * anchors, residual vectors, TF32 tables and anchor-phase tables are rebuilt
+ * by kernels on `stream` (no host synchronisation). */
+HOE_API int  hoe_set_kspha(hoe_handle *h, const double *kspha_dev, const double *kspha_dt_dev, void *stream);
+/* FindDelay on the device for an operator built on the ADC times without
+ * concomitant terms: every outer iteration (coefficients and k̇ interpolated
+ * at the current delay, sample-side re-plan, weighted CGNR image, y1 = data -
+ * E x, y2 = B x, Δτ = J*Re(y2 \ y1)) runs as one CUDA graph; the host reads
+ * a few scalars between iterations.  Density weights are the fixed
+ * weights_dev (complex64 [nSam] or NULL).  x_dev (complex64 [nFull] or NULL)
+ * receives the last image.  The operator keeps the last coefficients. */
+HOE_API int  hoe_find_delay(hoe_handle *h, const hoe_delay_params *params, const void *data_dev,
+                            const void *weights_dev, const double *traj_dev, int64_t nField,
+                            void *x_dev, hoe_delay_result *out, void *stream);
 
 /* Batches of operators on one device (e.g. the slices of a multi-slice scan).
  * A batch borrows its members: free the batch before freeing a member, and a
