@@ -216,12 +216,12 @@ inline size_t tf32_index(size_t row, int k, int KP) {
 }
 
 void split_tf32(const std::vector<double> &v, int n, int rank, int KP, size_t nPad,
-                std::vector<float> &hi, std::vector<float> &lo) {
+                std::vector<float> &hi, std::vector<float> &lo, double scale = 1.0) {
   hi.assign(nPad * KP, 0.f);
   lo.assign(nPad * KP, 0.f);
   for (int i = 0; i < n; ++i)
     for (int k = 0; k < rank; ++k) {
-      double x = v[(size_t)i * rank + k];
+      double x = scale * v[(size_t)i * rank + k];
       float h = tf32_round((float)x);
       float l = tf32_round((float)(x - (double)h));
       size_t o = tf32_index((size_t)i, k, KP);
@@ -483,7 +483,8 @@ int make_plan(const hoe_desc *d, Plan &P) {
     }
   t.KP = rank <= 8 ? 8 : (rank <= 16 ? 16 : 24);
   split_tf32(dbr, nVox, rank, t.KP, t.nVoxPad, P.dbHi, P.dbLo);
-  split_tf32(kpr, nSam, rank, t.KP, t.nSamPad, P.kpHi, P.kpLo);
+  // the tensor-core residual phase is formed in radians: 2*pi on the sample side
+  split_tf32(kpr, nSam, rank, t.KP, t.nSamPad, P.kpHi, P.kpLo, 2.0 * M_PI);
   // worst-case residual magnitude over tile pairs (reported)
   {
     std::vector<double> dmx((size_t)t.nVt * rank, 0.0), kmx((size_t)t.nSt * rank, 0.0);
@@ -566,7 +567,6 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
 
   auto &t = h->t;
   t = P.t;
-  const int R = t.R;
   const int nSam = t.nSam;
   auto &dbeta = P.dbeta, &kappa = P.kappa, &bfraw = P.bfraw, &kdot = P.kdot, &times_f = P.times_f;
   auto &beta64 = P.beta64, &kap64 = P.kap64, &betabar = P.betabar, &gambar = P.gambar;

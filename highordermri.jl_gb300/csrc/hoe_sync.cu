@@ -86,8 +86,10 @@ k_replan_samples(const double *__restrict__ kspha, int ldk, const double *__rest
     double acc = 0.0;
     for (int l = 0; l < R; ++l) acc += kap[l] / bal[l] * Vr[(size_t)l * rank + k];
     kappa[(size_t)s * Rp + k] = (float)acc;
-    const float h = tf32_round_dev((float)acc);
-    const float lo = tf32_round_dev((float)(acc - (double)h));
+    // the tensor-core tables hold the sample side in radians
+    const double accr = 6.283185307179586476925 * acc;
+    const float h = tf32_round_dev((float)accr);
+    const float lo = tf32_round_dev((float)(accr - (double)h));
     const size_t o = tf32_index_dev((size_t)s, k, KP);
     kpHi[o] = h;
     kpLo[o] = lo;

@@ -14,11 +14,11 @@
 //            so D[v,2c..2c+1] = (Re, Im) of sum_s conj(P[s,v]) Y[s,c]
 //
 // The A operand (the phase tile) never touches global or shared memory.  Per
-// stage of 64 columns the MMA thread first computes the residual phase
-// dbeta.kappa of the 128 x 64 tile on the tensor cores (TF32, 3 products of
-// hi/lo splits made at create time, K = reduced rank) into a TMEM tile, a
-// few stages ahead; 16 "phase" warps read it, add the FP32 anchors (see
-// hoe_internal.cuh), range-reduce, take the FP32 sincos, split the result
+// stage of 64 columns a residual-phase warp first computes the residual
+// phase dbeta.kappa of the 128 x 64 tile on the tensor cores (TF32, 3
+// products of hi/lo splits made at create time, K = reduced rank, in radians)
+// into a TMEM tile, a few stages ahead; 16 "phase" warps read it, add the
+// FP32 anchors (see hoe_internal.cuh), take the FP32 sincos, split the result
 // into BF16 hi/lo and write both into a TMEM A tile with tcgen05.st (lane =
 // row, one 32-bit column = one (re, im) pair).  A loader warp streams the
 // pre-tiled B operand, the TF32 residual tiles and the anchors with
@@ -275,6 +275,8 @@ struct TcParams {
   int64_t work;                 // all slices' work items, split evenly over gridDim.x CTAs
   int nSlices, nChaPad, nChaTC, pad;
   TcSlice s[MS];
+  // slice i (a compile-time index for single-slice launches)
+  __host__ __device__ __forceinline__ const TcSlice &at(int i) const { return s[MS == 1 ? 0 : i]; }
 };
 constexpr int kBatchSlices = 32;
 static_assert(sizeof(TcParams<kBatchSlices>) <= 4096, "kernel parameter space");
@@ -294,9 +296,9 @@ struct Cursor {
     if constexpr (MS > 1) {
       while (si + 1 < p.nSlices && p.s[si + 1].first <= w) ++si;
     }
-    C = p.s[si].nColChunks;
-    nRT = p.s[si].nRowTiles;
-    const int64_t off = w - p.s[si].first;
+    C = p.at(si).nColChunks;
+    nRT = p.at(si).nRowTiles;
+    const int64_t off = w - p.at(si).first;
     rt = (int)(off / C);
     ch = (int)(off % C);
   }
@@ -485,7 +487,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       __syncwarp();
       if (lane == 0) mbar_arrive(&tmemfree[g & 1]);
       if (pendLast) {
-        const TcSlice &ps = p.s[pendSI];
+        const TcSlice &ps = p.at(pendSI);
         const int slot = b - work_owner(ps.first + (int64_t)pendRT * ps.nColChunks, p.work, G);
         float2 *dst = ps.part + ((int64_t)slot * ps.nRowPad + (int64_t)pendRT * TM + row) * p.nChaPad;
         const int nOut = min(p.nChaTC, p.nChaPad);
@@ -504,7 +506,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     Cursor<MS> c = c0;
     // anchor phase of the next anchor tile, loaded one stage ahead
     float aNext = nIter > 0
-        ? p.s[c.si].rowAnchor[(int64_t)(c.ch * TV / 128) * p.s[c.si].rowAnchorStride + c.rt * TM + row] : 0.f;
+        ? p.at(c.si).rowAnchor[(int64_t)(c.ch * TV / 128) * p.at(c.si).rowAnchorStride + c.rt * TM + row] : 0.f;
     for (int it = 0; it < nIter && ok; ++it) {
       if (it > 0) c.next(p);
       if (it == 0 || c.ch % GROUP == 0) ++grp;
@@ -519,7 +521,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         Cursor<MS> n = c;
         n.next(p);
         if (n.ch == 0 || n.ch * TV / 128 != colTile)
-          aNext = p.s[n.si].rowAnchor[(int64_t)(n.ch * TV / 128) * p.s[n.si].rowAnchorStride + n.rt * TM + row];
+          aNext = p.at(n.si).rowAnchor[(int64_t)(n.ch * TV / 128) * p.at(n.si).rowAnchorStride + n.rt * TM + row];
       }
       // residual phase of this stage (TMEM), then release its buffer
       const int pb = it % PD, pr = it / PD;
@@ -540,10 +542,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         const float cav[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          float ph = (a + cav[j]) + d[cc * 4 + j];
-          float f = ph - rintf(ph);
+          // anchors in cycles (each in [-1/2, 1/2]), residual in radians; the
+          // sum stays within a few hundred radians, where the fast sincos
+          // keeps an absolute error near |ph| * 2^-24
+          const float ph = fmaf(a + cav[j], kTwoPi, d[cc * 4 + j]);
           float sn, cs;
-          __sincosf(kTwoPi * f, &sn, &cs);
+          __sincosf(ph, &sn, &cs);
           __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
           float2 hf = __bfloat1622float2(h);
           hi[cc * 4 + j] = *reinterpret_cast<uint32_t *>(&h);
@@ -671,7 +675,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       Cursor<MS> c = c0;
       for (int it = 0; it < nIter; ++it) {
         if (it > 0) c.next(p);
-        const TcSlice &sl = p.s[c.si];
+        const TcSlice &sl = p.at(c.si);
         const int rt = c.rt, ch = c.ch;
         if (it == 0 || ch == 0) {
           ++kcount;
