@@ -930,7 +930,9 @@ cudaError_t build_anchor_tables(const hoe_handle *h, cudaStream_t st) {
   k_table_B<<<(unsigned)((nB + 255) / 256), 256, 0, st>>>(t.beta64, t.gambar, t.perm, t.Btab, t.R, t.nSt,
                                                           t.nVoxPad);
   h->launches += 2;
-  return cudaGetLastError();
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = tc_anchor_tables(h, st);
+  return e;
 }
 
 cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {

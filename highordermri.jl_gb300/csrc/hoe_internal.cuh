@@ -251,6 +251,8 @@ cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y,
 cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
 bool tc_supported(const hoe_handle *h, std::string *why);
 int *tc_error_word(const hoe_handle *h);   // device word set by a timed-out wait
+// Rebuilds the tensor-core anchor tables from Atab/Btab (no-op before tc_prepare).
+cudaError_t tc_anchor_tables(const hoe_handle *h, cudaStream_t st);
 // Several operators (tensor-core engine, equal coil counts) in one persistent
 // launch per direction and residual width.  The plan borrows the handles.
 // tc_batch_forward reads each handle's prepared Z; y/D may be NULL per the

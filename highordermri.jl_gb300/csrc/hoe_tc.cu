@@ -14,11 +14,12 @@
 //            so D[v,2c..2c+1] = (Re, Im) of sum_s conj(P[s,v]) Y[s,c]
 //
 // The A operand (the phase tile) never touches global or shared memory.  Per
-// stage of 64 columns a residual-phase warp first computes the residual
-// phase dbeta.kappa of the 128 x 64 tile on the tensor cores (TF32, 3
-// products of hi/lo splits made at create time, K = reduced rank, in radians)
-// into a TMEM tile, a few stages ahead; 16 "phase" warps read it, add the
-// FP32 anchors (see hoe_internal.cuh), take the FP32 sincos, split the result
+// stage of 64 columns a residual-phase warp first computes the whole phase of
+// the 128 x 64 tile in radians on the tensor cores into a TMEM tile, a few
+// stages ahead: the residual dbeta.kappa (TF32, 3 products of hi/lo splits
+// made at create time, K = reduced rank) plus one more k-step that adds the
+// row and column anchors (see hoe_internal.cuh) as [a_hi, a_lo, 1, 1] .
+// [1, 1, c_hi, c_lo].  16 "phase" warps read it, take the FP32 sincos, split the result
 // into BF16 hi/lo and write both into a TMEM A tile with tcgen05.st (lane =
 // row, one 32-bit column = one (re, im) pair).  A loader warp streams the
 // pre-tiled B operand, the TF32 residual tiles and the anchors with
@@ -52,7 +53,6 @@ constexpr int CISS_WARP = PHASE_WARPS;        // contraction issuers: warps 16, 
 constexpr int PISS_WARP = PHASE_WARPS + 2;    // residual-phase issuer, TMEM owner
 constexpr int LOAD_WARP = PHASE_WARPS + 3;
 constexpr int THREADS = (PHASE_WARPS + 4) * 32;
-constexpr float kTwoPi = 6.28318530717958647692f;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
 
 // The tensor-core FP32 accumulator sums at most GROUP stages (GROUP*24 MMAs)
@@ -85,8 +85,8 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
 
 // Shared-memory matrix descriptor, no swizzle: start address, LBO (K step of
 // core matrices), SBO (step of 8-row groups), descriptor version 1.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo = SBO) {
-  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(LBO >> 4) << 16) |
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo = SBO, uint32_t lbo = LBO) {
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
          ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
 }
 
@@ -255,12 +255,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
 struct TcSlice {
   const float *rowHi, *rowLo;   // TF32 row-side residual tables: kappa (forward) / dbeta (adjoint)
   const float *colHi, *colLo;   // TF32 column-side residual tables: dbeta (forward) / kappa (adjoint)
-  const float *rowAnchor;       // [colTile][rowAnchorStride]: Atab (forward) / Btab (adjoint)
-  const float *colAnchor;       // [rowTile][colAnchorStride]: Btab (forward) / Atab (adjoint)
+  const float *rowX;            // [colTile][rowXStride][4] TF32 anchor rows: AtabP (forward) / BtabQ (adjoint)
+  const float *colX;            // [rowTile][colXStride][4] TF32 anchor columns: BtabQ (forward) / AtabP (adjoint)
   const uint16_t *Bop;          // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
   float2 *part;                 // [slot][nRowPad][nChaPad] partial sums (zeroed before launch)
   int64_t first;                // global index of the slice's first work item
-  int rowAnchorStride, colAnchorStride;
+  int rowXStride, colXStride;
   int nRowPad;
   int nColChunks;               // column chunks per row tile (C)
   int nRowTiles;
@@ -336,7 +336,8 @@ struct Tmem {
 //   B   [NS][hi,lo]   BF16 contraction operand, N x TK
 //   CV  [NS][hi,lo]   TF32 column residual tile, TV x KP
 //   RV  [2][hi,lo]    TF32 row residual tile, 128 x KP (one per row-tile parity)
-//   CA  [NS][TV]      column anchors
+//   XR  [NS][data,0]  TF32 anchor k-step, row side: 128 rows x 4, then 128 x 4 zeros
+//   XC  [NS][data,0]  TF32 anchor k-step, column side: TV columns x 4, then zeros
 //   barriers: full[NS] empty[NS] afull[ABUF] aempty[ABUF] segdone[2]
 //             tmemfree[2] pfull[PD] pfree[PD] rfull[2] rfree[2]
 // The residual-phase issuer runs up to PD stages ahead of the phase warps.
@@ -350,8 +351,11 @@ struct Smem {
   static constexpr size_t B_OFF = 0;
   static constexpr size_t CV_OFF = B_OFF + (size_t)NS * 2 * B_TILE;
   static constexpr size_t RV_OFF = CV_OFF + (size_t)NS * 2 * CV_TILE;
-  static constexpr size_t CA_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
-  static constexpr size_t BAR_OFF = (CA_OFF + (size_t)NS * TV * 4 + 7) / 8 * 8;
+  static constexpr int XR_BYTES = TM * 4 * 4;    // one core-matrix column of 128 rows
+  static constexpr int XC_BYTES = TV * 4 * 4;
+  static constexpr size_t XR_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
+  static constexpr size_t XC_OFF = XR_OFF + (size_t)NS * 2 * XR_BYTES;
+  static constexpr size_t BAR_OFF = (XC_OFF + (size_t)NS * 2 * XC_BYTES + 7) / 8 * 8;
   static constexpr int NBAR = 2 * NS + 2 * ABUF + 8 + 2 * PD;
   static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
@@ -375,7 +379,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   unsigned char *sB = smem + S::B_OFF;
   unsigned char *sCV = smem + S::CV_OFF;
   unsigned char *sRV = smem + S::RV_OFF;
-  float *sCA = reinterpret_cast<float *>(smem + S::CA_OFF);
+  unsigned char *sXR = smem + S::XR_OFF;
+  unsigned char *sXC = smem + S::XC_OFF;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
   uint64_t *empty = full + NS;        // B-ring stage consumed by the contraction MMAs
   uint64_t *afull = empty + NS;       // [ABUF] TMEM phase tile written (16 phase warps)
@@ -423,6 +428,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // the second core-matrix column of every anchor k-step operand is zero
+  for (int i = threadIdx.x; i < NS * (S::XR_BYTES + S::XC_BYTES) / 16; i += THREADS) {
+    const int nr = NS * S::XR_BYTES / 16;
+    float4 *dst = i < nr
+        ? reinterpret_cast<float4 *>(sXR + (size_t)(i / (S::XR_BYTES / 16)) * 2 * S::XR_BYTES + S::XR_BYTES) + i % (S::XR_BYTES / 16)
+        : reinterpret_cast<float4 *>(sXC + (size_t)((i - nr) / (S::XC_BYTES / 16)) * 2 * S::XC_BYTES + S::XC_BYTES) + (i - nr) % (S::XC_BYTES / 16);
+    *dst = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == PISS_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
@@ -446,10 +460,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     float acc[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) acc[i] = 0.f;
-    int curTile = -1, grp = -1;
+    int grp = -1;
     int pendGrp = -1, pendRT = -1, pendSI = 0;
     bool pendLast = false;
-    float a = 0.f;
     bool ok = true;
     auto flush = [&]() {
       // add group pendGrp into acc; write acc out if it closed its row tile
@@ -504,26 +517,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       pendGrp = -1;
     };
     Cursor<MS> c = c0;
-    // anchor phase of the next anchor tile, loaded one stage ahead
-    float aNext = nIter > 0
-        ? p.at(c.si).rowAnchor[(int64_t)(c.ch * TV / 128) * p.at(c.si).rowAnchorStride + c.rt * TM + row] : 0.f;
     for (int it = 0; it < nIter && ok; ++it) {
       if (it > 0) c.next(p);
       if (it == 0 || c.ch % GROUP == 0) ++grp;
-      if (it == 0 || c.ch == 0) curTile = -1;  // new row tile
-      const int slot = it % NS, round = it / NS;
-      const int colTile = c.ch * TV / 128;
-      if (colTile != curTile) {
-        a = aNext;
-        curTile = colTile;
-      }
-      if (it + 1 < nIter) {
-        Cursor<MS> n = c;
-        n.next(p);
-        if (n.ch == 0 || n.ch * TV / 128 != colTile)
-          aNext = p.at(n.si).rowAnchor[(int64_t)(n.ch * TV / 128) * p.at(n.si).rowAnchorStride + n.rt * TM + row];
-      }
-      // residual phase of this stage (TMEM), then release its buffer
+      // phase of this stage in radians (TMEM), then release its buffer
       const int pb = it % PD, pr = it / PD;
       if (!wait_bar(&pfull[pb], pr & 1, abort, p.err)) { ok = false; break; }
       tc_fence_after();
@@ -532,27 +529,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&pfree[pb]);
-      // column anchors of this stage
-      if (!wait_bar(&full[slot], round & 1, abort, p.err)) { ok = false; break; }
-      const float *ca = sCA + slot * TV + qcol * 16;
       uint32_t hi[16], lo[16];
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
-        const float4 c4 = *reinterpret_cast<const float4 *>(ca + cc * 4);
-        const float cav[4] = {c4.x, c4.y, c4.z, c4.w};
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          // anchors in cycles (each in [-1/2, 1/2]), residual in radians; the
-          // sum stays within a few hundred radians, where the fast sincos
-          // keeps an absolute error near |ph| * 2^-24
-          const float ph = fmaf(a + cav[j], kTwoPi, d[cc * 4 + j]);
-          float sn, cs;
-          __sincosf(ph, &sn, &cs);
-          __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
-          float2 hf = __bfloat1622float2(h);
-          hi[cc * 4 + j] = *reinterpret_cast<uint32_t *>(&h);
-          lo[cc * 4 + j] = pack_bf16(cs - hf.x, sn - hf.y);
-        }
+      for (int j = 0; j < 16; ++j) {
+        // the phase stays within a few hundred radians, where the fast
+        // sincos keeps an absolute error near |phase| * 2^-24
+        float sn, cs;
+        __sincosf(d[j], &sn, &cs);
+        __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
+        float2 hf = __bfloat1622float2(h);
+        hi[j] = *reinterpret_cast<uint32_t *>(&h);
+        lo[j] = pack_bf16(cs - hf.x, sn - hf.y);
       }
       // TMEM phase tile buffer: free once the contraction of stage it-ABUF is done
       const int ab = it % ABUF, ar = it / ABUF;
@@ -658,6 +645,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
           umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
           umma_tf32(dt, umma_desc(rLo + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
         }
+        // anchor k-step: [a_hi, a_lo, 1, 1 | 0] . [1, 1, c_hi, c_lo | 0] adds both anchors
+        umma_tf32(dt, umma_desc(smem_u32(sXR + (size_t)s * 2 * S::XR_BYTES), 128, S::XR_BYTES),
+                  umma_desc(smem_u32(sXC + (size_t)s * 2 * S::XC_BYTES), 128, S::XC_BYTES), idescP, 1u);
         umma_commit(&pfull[pb]);
         lastBar = &pfull[pb];
         lastPar = pr & 1;
@@ -670,7 +660,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     // ---------------- loader (one thread): row residual tiles per row tile,
     // per stage the B tiles, column residual tiles and column anchors
     if (lane == 0) {
-      const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + TV * 4;
+      const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + S::XR_BYTES + S::XC_BYTES;
       int issued = 0, kcount = -1, rowIssued = -1;
       Cursor<MS> c = c0;
       for (int it = 0; it < nIter; ++it) {
@@ -694,8 +684,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, sl.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
         bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, sl.colHi + co, S::CV_TILE, &full[slot]);
         bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, sl.colLo + co, S::CV_TILE, &full[slot]);
-        bulk_g2s(sCA + slot * TV, sl.colAnchor + (int64_t)rt * sl.colAnchorStride + ch * TV, TV * 4,
-                 &full[slot]);
+        bulk_g2s(sXR + (size_t)slot * 2 * S::XR_BYTES,
+                 sl.rowX + ((int64_t)(ch * TV / 128) * sl.rowXStride + (int64_t)rt * TM) * 4, S::XR_BYTES, &full[slot]);
+        bulk_g2s(sXC + (size_t)slot * 2 * S::XC_BYTES,
+                 sl.colX + ((int64_t)rt * sl.colXStride + (int64_t)ch * TV) * 4, S::XC_BYTES, &full[slot]);
         issued = it + 1;
       }
       if (*abort) {
@@ -754,6 +746,26 @@ __global__ void k_tc_bop_adjoint(const float2 *__restrict__ Yt, uint16_t *__rest
   uint32_t o = kmajor_off(n, k) / 2;
   tile[o] = *reinterpret_cast<uint16_t *>(&h);
   tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+}
+
+// Anchor tables of the anchor k-step: v = 2*pi*tab[i] (radians) split into
+// TF32 hi + lo, stored as [hi, lo, 1, 1] (format 0) or [1, 1, hi, lo] (format 1).
+__device__ __forceinline__ float tf32_rn(float f) {
+  uint32_t b = __float_as_uint(f);
+  if ((b & 0x7f800000u) != 0x7f800000u) {
+    b += 0x00000fffu + ((b >> 13) & 1u);
+    b &= 0xffffe000u;
+  }
+  return __uint_as_float(b);
+}
+
+__global__ void k_tc_anchor_tf32(const float *__restrict__ tab, int64_t n, float4 *__restrict__ out, int format) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = 6.283185307179586476925 * (double)tab[i];
+  const float h = tf32_rn((float)v);
+  const float l = tf32_rn((float)(v - (double)h));
+  out[i] = format == 0 ? make_float4(h, l, 1.f, 1.f) : make_float4(1.f, 1.f, h, l);
 }
 
 int tc_ncha(int nCha) {
@@ -844,6 +856,7 @@ int max_slots(int rowTiles, int C, int G) {
 
 struct TcBuffers {
   uint16_t *bopF = nullptr, *bopA = nullptr;
+  float *AtabP = nullptr, *BtabQ = nullptr;   // anchors in radians, TF32 [hi, lo, 1, 1] / [1, 1, hi, lo]
   float2 *part = nullptr;
   int *err = nullptr;
   int N = 0, nChaTC = 0;
@@ -885,7 +898,9 @@ cudaError_t tc_prepare(hoe_handle *h) {
   b.bopFElems = (size_t)chunksF * 2 * b.N * TK;
   b.bopAElems = (size_t)chunksA * 2 * b.N * TK;
   b.partElems = std::max((size_t)b.slotsF * t.nSamPad, (size_t)b.slotsA * t.nVoxPad) * t.nChaPad;
-  size_t bytes = b.bopFElems * 2 + 256 + b.bopAElems * 2 + 256 + b.partElems * sizeof(float2) + 256 + 256;
+  const size_t nAP = (size_t)t.nVt * t.nSamPad, nBQ = (size_t)t.nSt * t.nVoxPad;
+  size_t bytes = b.bopFElems * 2 + 256 + b.bopAElems * 2 + 256 + b.partElems * sizeof(float2) + 256 + 256 +
+                 (nAP + nBQ) * 16 + 512;
   unsigned char *buf = nullptr;
   cudaError_t e = cudaMalloc(&buf, bytes);
   if (e != cudaSuccess) return e;
@@ -895,13 +910,17 @@ cudaError_t tc_prepare(hoe_handle *h) {
   b.bopA = (uint16_t *)take(b.bopAElems * 2);
   b.part = (float2 *)take(b.partElems * sizeof(float2));
   b.err = (int *)take(sizeof(int));
+  b.AtabP = (float *)take(nAP * 16);
+  b.BtabQ = (float *)take(nBQ * 16);
   e = cudaMemset(b.err, 0, sizeof(int));
   if (e != cudaSuccess) { cudaFree(buf); return e; }
   h->tc.buf = buf;
   h->tc.bytes = bytes;
   h->tc.ready = true;
   h->tc_host = new TcBuffers(b);
-  return cudaSuccess;
+  e = tc_anchor_tables(h, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  return e;
 }
 
 void tc_release(hoe_handle *h) {
@@ -919,10 +938,10 @@ TcSlice slice_forward(const hoe_handle *h, const TcBuffers &b) {
   TcSlice sl{};
   sl.rowHi = t.kpHi; sl.rowLo = t.kpLo;
   sl.colHi = t.dbHi; sl.colLo = t.dbLo;
-  sl.rowAnchor = t.Atab;
-  sl.rowAnchorStride = t.nSamPad;
-  sl.colAnchor = t.Btab;
-  sl.colAnchorStride = t.nVoxPad;
+  sl.rowX = b.AtabP;
+  sl.rowXStride = t.nSamPad;
+  sl.colX = b.BtabQ;
+  sl.colXStride = t.nVoxPad;
   sl.Bop = b.bopF;
   sl.part = b.part;
   sl.nRowPad = t.nSamPad;
@@ -936,10 +955,10 @@ TcSlice slice_adjoint(const hoe_handle *h, const TcBuffers &b) {
   TcSlice sl{};
   sl.rowHi = t.dbHi; sl.rowLo = t.dbLo;
   sl.colHi = t.kpHi; sl.colLo = t.kpLo;
-  sl.rowAnchor = t.Btab;
-  sl.rowAnchorStride = t.nVoxPad;
-  sl.colAnchor = t.Atab;
-  sl.colAnchorStride = t.nSamPad;
+  sl.rowX = b.BtabQ;
+  sl.rowXStride = t.nVoxPad;
+  sl.colX = b.AtabP;
+  sl.colXStride = t.nSamPad;
   sl.Bop = b.bopA;
   sl.part = b.part;
   sl.nRowPad = t.nVoxPad;
@@ -1136,6 +1155,17 @@ cudaError_t tc_batch_adjoint_from_Yt(void *plan, float2 *const *x, cudaStream_t 
 }
 
 int tc_batch_launches(void *plan) { return plan ? (int)((TcBatchPlan *)plan)->groups.size() : 0; }
+
+cudaError_t tc_anchor_tables(const hoe_handle *h, cudaStream_t st) {
+  if (!h->tc.ready) return cudaSuccess;
+  const auto &t = h->t;
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  const int64_t nAP = (int64_t)t.nVt * t.nSamPad, nBQ = (int64_t)t.nSt * t.nVoxPad;
+  k_tc_anchor_tf32<<<(unsigned)((nAP + 255) / 256), 256, 0, st>>>(t.Atab, nAP, (float4 *)b.AtabP, 0);
+  k_tc_anchor_tf32<<<(unsigned)((nBQ + 255) / 256), 256, 0, st>>>(t.Btab, nBQ, (float4 *)b.BtabQ, 1);
+  h->launches += 2;
+  return cudaGetLastError();
+}
 
 int *tc_error_word(const hoe_handle *h) {
   return h->tc_host ? ((const TcBuffers *)h->tc_host)->err : nullptr;
