@@ -44,7 +44,12 @@ namespace {
 constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel tile)
 constexpr int TV = 64;              // complex columns per pipeline stage
 constexpr int TK = 2 * TV;          // real K per stage (128 BF16 = 8 UMMA k-steps)
-constexpr int PHASE_WARPS = 16;     // four per TMEM lane quarter, a quarter of the stage's columns each
+// Phase warps: two groups of 8 take alternate stages (group = warp >> 3), so
+// one group's barrier and tensor-memory latencies overlap the other's
+// arithmetic; within a group a warp covers one TMEM lane quarter (warp & 3)
+// and half of the stage's columns ((warp >> 2) & 1).
+constexpr int PHASE_WARPS = 16;
+constexpr int GROUP_WARPS = PHASE_WARPS / 2;
 // Warp roles: 16 phase warps, two contraction issuers (each one tcgen05.mma
 // stream; issue from a single thread costs ~50 cycles per instruction, so
 // the stage's k-steps are split between them), one residual-phase issuer
@@ -412,7 +417,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       mbar_init(&empty[i], NISS);
     }
     for (int i = 0; i < ABUF; ++i) {
-      mbar_init(&afull[i], PHASE_WARPS);
+      mbar_init(&afull[i], GROUP_WARPS);
       mbar_init(&aempty[i], NISS);
     }
     for (int i = 0; i < 2; ++i) {
@@ -423,7 +428,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     }
     for (int i = 0; i < PD; ++i) {
       mbar_init(&pfull[i], 1);
-      mbar_init(&pfree[i], PHASE_WARPS);
+      mbar_init(&pfree[i], GROUP_WARPS);
     }
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -449,19 +454,21 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   const uint32_t tmem = *tmem_slot;
 
   if (warp < PHASE_WARPS) {
-    // ---------------- phase generator: one row x 16 columns of each stage.
-    // After the first stage of group g+1 (or at the end) all 16 warps add
-    // group g's accumulator into register sums (columns split by warp
-    // quarter) and, at the end of a row tile, write the sums to the partial slot.
+    // ---------------- phase generator: one row x 32 columns of every other
+    // stage.  Two stages after a group of GROUP stages closes (or at the end),
+    // all 16 warps add its accumulator into register sums (columns split by
+    // warp >> 2) and, at the end of a row tile, write the sums to the partial slot.
     const int row = (warp & 3) * 32 + lane;
-    const int qcol = warp >> 2;
+    const int qcol = warp >> 2;          // accumulator quarter
+    const int half = (warp >> 2) & 1;    // stage columns [half*32, half*32+32)
+    const int par = warp >> 3;           // stages with it % 2 == par
     const uint32_t laneBase = (uint32_t)((warp & 3) * 32) << 16;
     constexpr int NA = N / 4;  // accumulator columns owned by this thread
     float acc[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) acc[i] = 0.f;
     int grp = -1;
-    int pendGrp = -1, pendRT = -1, pendSI = 0;
+    int pendGrp = -1, pendRT = -1, pendSI = 0, pendIt = 0;
     bool pendLast = false;
     bool ok = true;
     auto flush = [&]() {
@@ -516,24 +523,12 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       }
       pendGrp = -1;
     };
-    Cursor<MS> c = c0;
-    for (int it = 0; it < nIter && ok; ++it) {
-      if (it > 0) c.next(p);
-      if (it == 0 || c.ch % GROUP == 0) ++grp;
-      // phase of this stage in radians (TMEM), then release its buffer
-      const int pb = it % PD, pr = it / PD;
-      if (!wait_bar(&pfull[pb], pr & 1, abort, p.err)) { ok = false; break; }
-      tc_fence_after();
-      float d[16];
-      tmem_ld16(tmem + laneBase + P_COL + (uint32_t)(pb * TV + qcol * 16), d);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&pfree[pb]);
-      uint32_t hi[16], lo[16];
+    // sincos of 16 phases (radians) -> BF16 hi/lo pairs.  The phase stays
+    // within a few hundred radians, where the fast sincos keeps an absolute
+    // error near |phase| * 2^-24.
+    auto phase16 = [&](const float *d, uint32_t *hi, uint32_t *lo) {
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        // the phase stays within a few hundred radians, where the fast
-        // sincos keeps an absolute error near |phase| * 2^-24
         float sn, cs;
         __sincosf(d[j], &sn, &cs);
         __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
@@ -541,25 +536,50 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         hi[j] = *reinterpret_cast<uint32_t *>(&h);
         lo[j] = pack_bf16(cs - hf.x, sn - hf.y);
       }
-      // TMEM phase tile buffer: free once the contraction of stage it-ABUF is done
-      const int ab = it % ABUF, ar = it / ABUF;
-      if (ar > 0 && !wait_bar(&aempty[ab], (ar - 1) & 1, abort, p.err)) { ok = false; break; }
-      tc_fence_after();
-      const uint32_t aBase = tmem + laneBase + A_COL + (uint32_t)(ab * 2 * TV + qcol * 16);
-      tmem_st16(aBase, hi);
-      tmem_st16(aBase + TV, lo);
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&afull[ab]);
-      // the previous group is flushed one stage late, so its MMAs are done by now
-      if (pendGrp >= 0) flush();
+    };
+    Cursor<MS> c = c0;
+    for (int it = 0; it < nIter && ok; ++it) {
+      if (it > 0) c.next(p);
+      if (it == 0 || c.ch % GROUP == 0) ++grp;
+      if ((it & 1) == par) {
+        // phase of this stage in radians (TMEM), then release its buffer
+        const int pb = it % PD, pr = it / PD;
+        if (!wait_bar(&pfull[pb], pr & 1, abort, p.err)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t pBase = tmem + laneBase + P_COL + (uint32_t)(pb * TV + half * 32);
+        const int ab = it % ABUF, ar = it / ABUF;
+        const uint32_t aBase = tmem + laneBase + A_COL + (uint32_t)(ab * 2 * TV + half * 32);
+        float d[16];
+        uint32_t hi[16], lo[16];
+        tmem_ld16(pBase, d);
+        phase16(d, hi, lo);
+        // TMEM phase tile buffer: free once the contraction of stage it-ABUF is done
+        if (ar > 0 && !wait_bar(&aempty[ab], (ar - 1) & 1, abort, p.err)) { ok = false; break; }
+        tc_fence_after();
+        tmem_st16(aBase, hi);
+        tmem_st16(aBase + TV, lo);
+        tmem_ld16(pBase + 16, d);
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&pfree[pb]);
+        phase16(d, hi, lo);
+        tmem_st16(aBase + 16, hi);
+        tmem_st16(aBase + TV + 16, lo);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&afull[ab]);
+      }
+      // a closed group is flushed two stages later, when its MMAs are done
+      if (pendGrp >= 0 && it >= pendIt + 2) flush();
       const bool endRT = (it == nIter - 1) || (c.ch + 1 == c.C);
       if (endRT || (c.ch + 1) % GROUP == 0) {
+        if (pendGrp >= 0) flush();  // a short group closed within two stages of the previous one
         pendGrp = grp;
         pendRT = c.rt;
         pendSI = c.si;
         pendLast = endRT;
+        pendIt = it;
       }
     }
     if (pendGrp >= 0) flush();
