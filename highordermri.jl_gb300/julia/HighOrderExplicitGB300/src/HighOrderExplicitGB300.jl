@@ -22,7 +22,7 @@ using ChainRulesCore
 import HighOrderMRI
 import HighOrderMRI: Grid, HighOrderExplicitOp, prep_kspha, basisfunc_spha, prep_concomitant
 
-export GB300ExplicitOp, explicit_backward, encode
+export GB300ExplicitOp, explicit_backward, encode, GB300Batch, set_kspha!
 
 const libhoe = get(ENV, "HOE_LIBRARY",
     normpath(joinpath(@__DIR__, "..", "..", "..", "libhoexplicit.so")))
@@ -263,6 +263,164 @@ function ChainRulesCore.rrule(::typeof(encode), op::GB300ExplicitOp, x)
         return NoTangent(), Tangent{typeof(op)}(; kspha=dk, fieldmap=ddf, t0=dt0), op' * ybar
     end
     return y, encode_pullback
+end
+
+# ---------------------------------------------------------------------------
+# recon_HOOp (src/Recon/recon_HOOp.jl:52-88) on the device: CGNR with an L2
+# regularizer runs as one CUDA graph (hoe_recon); any other solver or
+# regularizer goes through the generic RegularizedLeastSquares path, which
+# only needs prod!/ctprod!/normalOperator.
+
+struct HoeCgParams
+    iterations::Int32; use_graph::Int32; rel_tol::Float64; lambda::Float64
+end
+struct HoeCgStats
+    iterations::Int32; status::Int32; residual0::Float64; residual::Float64
+end
+
+function HighOrderMRI.recon_HOOp(op::GB300ExplicitOp{T}, Data::CuMatrix{Complex{T}},
+                                 weight::CuVector{Complex{T}}, recParams::Dict;
+                                 release_backend::Bool=true) where {T}
+    params = merge(HighOrderMRI.defaultRecoParams(), recParams)
+    reg = params[:reg]
+    reg = reg isa AbstractVector && length(reg) == 1 ? only(reg) : reg
+    if params[:solver] !== HighOrderMRI.CGNR || !(reg isa HighOrderMRI.L2Regularization)
+        return invoke(HighOrderMRI.recon_HOOp, Tuple{HighOrderMRI.HOOp{Complex{T}}, AbstractArray{Complex{T},2},
+                      AbstractVector{Complex{T}}, Dict}, op, Data, weight, recParams; release_backend)
+    end
+    size(Data, 1) == op.nSam && size(Data, 2) == op.nCha || throw(DimensionMismatch("Data and operator"))
+    h = activate(op)
+    x = CuVector{ComplexF32}(undef, op.ncol)
+    p = Ref(HoeCgParams(Int32(params[:iterations]), Int32(1),
+                        Float64(get(params, :relTol, eps(real(T)))), Float64(HighOrderMRI.λ(reg))))
+    st = Ref(HoeCgStats(0, 0, 0.0, 0.0))
+    check(ccall((:hoe_recon, libhoe), Cint,
+                (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, Ref{HoeCgParams},
+                 Ref{HoeCgStats}, CUDA.CUstream), h, Data, weight, x, p, st, stream_handle()), h)
+    return Array(reshape(x, params[:reconSize]))
+end
+
+# ---------------------------------------------------------------------------
+# Batches of slices (hoe_batch_*): every direction of all members in one
+# persistent launch; members are borrowed (close the batch first).
+
+mutable struct GB300Batch
+    handle::Ptr{Cvoid}
+    ops::Vector{GB300ExplicitOp}
+end
+
+function GB300Batch(ops::Vector{<:GB300ExplicitOp})
+    hs = Ptr{Cvoid}[activate(o) for o in ops]
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hoe_batch_create, libhoe), Cint, (Ref{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Int32),
+                out, hs, Int32(length(hs))))
+    b = GB300Batch(out[], collect(GB300ExplicitOp, ops))
+    finalizer(x -> ccall((:hoe_batch_free, libhoe), Cvoid, (Ptr{Cvoid},), x.handle), b)
+    return b
+end
+
+_ptrs(v) = Ptr{Cvoid}[reinterpret(Ptr{Cvoid}, pointer(a)) for a in v]
+
+function batch_check(rc::Cint, b::GB300Batch)
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:hoe_batch_last_error, libhoe), Cstring, (Ptr{Cvoid},), b.handle))
+    rc == -2 && throw(DimensionMismatch(msg))
+    rc in (-1, -6, -7) && throw(ArgumentError(msg))
+    rc == -3 && throw(OutOfMemoryError())
+    error(msg)
+end
+
+function forward(b::GB300Batch, xs::Vector{<:CuVector{ComplexF32}})
+    ys = [CuVector{ComplexF32}(undef, o.nrow) for o in b.ops]
+    batch_check(ccall((:hoe_batch_forward, libhoe), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, CUDA.CUstream),
+                      b.handle, _ptrs(xs), _ptrs(ys), stream_handle()), b)
+    return ys
+end
+
+function adjoint_apply(b::GB300Batch, ys::Vector{<:CuVector{ComplexF32}})
+    xs = [CuVector{ComplexF32}(undef, o.ncol) for o in b.ops]
+    batch_check(ccall((:hoe_batch_adjoint, libhoe), Cint, (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, CUDA.CUstream),
+                      b.handle, _ptrs(ys), _ptrs(xs), stream_handle()), b)
+    return xs
+end
+
+"""
+    recon(b::GB300Batch, datas, weights; iterations=10, relTol=eps(Float32), λ=0)
+
+`recon_HOOp`'s weighted CGNR for every member in lockstep (one CUDA graph);
+returns the images as device vectors.
+"""
+function recon(b::GB300Batch, datas::Vector{<:CuMatrix{ComplexF32}}, weights::Vector{<:CuVector{ComplexF32}};
+               iterations::Integer=10, relTol::Real=eps(Float32), λ::Real=0)
+    xs = [CuVector{ComplexF32}(undef, o.ncol) for o in b.ops]
+    p = Ref(HoeCgParams(Int32(iterations), Int32(1), Float64(relTol), Float64(λ)))
+    batch_check(ccall((:hoe_batch_recon, libhoe), Cint,
+                      (Ptr{Cvoid}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Ptr{Ptr{Cvoid}}, Ref{HoeCgParams},
+                       Ptr{HoeCgStats}, CUDA.CUstream),
+                      b.handle, _ptrs(datas), _ptrs(weights), _ptrs(xs), p, C_NULL, stream_handle()), b)
+    return xs
+end
+
+# ---------------------------------------------------------------------------
+# Delay synchronisation (src/Synchronization/FindDelay.jl:139-214) and
+# InterpTrajTime (InterpTraj.jl:18-40) on the device.
+
+"""
+    set_kspha!(op, kspha_dev, kspha_dt_dev=nothing)
+
+Replace the operator's coefficients on the device (hoe_set_kspha):
+`kspha_dev::CuMatrix{Float64}` (nTermEff, nSam) prepared as at construction.
+"""
+function set_kspha!(op::GB300ExplicitOp, k::CuMatrix{Float64}, kdt::Union{Nothing,CuMatrix{Float64}}=nothing)
+    h = activate(op)
+    check(ccall((:hoe_set_kspha, libhoe), Cint, (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{Float64}, CUDA.CUstream),
+                h, k, kdt === nothing ? CU_NULL : kdt, stream_handle()), h)
+    return op
+end
+
+function HighOrderMRI.InterpTrajTime(traj::CuMatrix{Float64}, dt::Real, delTime::Real,
+                                     datatime::CuVector{Float64}; kwargs...)
+    out = CuMatrix{Float64}(undef, length(datatime), size(traj, 2))
+    check(ccall((:hoe_interp_traj_time, libhoe), Cint,
+                (CuPtr{Float64}, Int64, Int32, Float64, Float64, CuPtr{Float64}, Int64, CuPtr{Float64}, Int32,
+                 CUDA.CUstream), traj, size(traj, 1), Int32(size(traj, 2)), Float64(dt), Float64(delTime),
+                datatime, length(datatime), out, Int32(0), stream_handle()))
+    return out
+end
+
+struct HoeDelayParams
+    start_time::Float64; dt::Float64; dtau_min::Float64; jump_fact::Float64; lambda::Float64
+    term_mask::Ptr{Float64}; iter_max::Int32; max_outer::Int32
+end
+struct HoeDelayResult
+    tau::Float64; tau_last::Float64; dtau::Float64; jump::Float64; iterations::Int32; status::Int32
+end
+
+"""
+    find_delay(op, data, kspha, StartTime, dt; weights=nothing, JumpFact=3, Δτ_min, iter_max=10,
+               λ=0, term_mask=nothing, max_outer=50)
+
+FindDelay for an operator built on the ADC times (`op.times == datatime`)
+without concomitant terms; `kspha::CuMatrix{Float64}` is the
+(nFieldSample, nTerm) coefficient series.  Returns the delay τ.
+"""
+function find_delay(op::GB300ExplicitOp, data::CuMatrix{ComplexF32}, kspha::CuMatrix{Float64},
+                    StartTime::Real, dt::Real; weights::Union{Nothing,CuVector{ComplexF32}}=nothing,
+                    JumpFact::Real=3, Δτ_min::Real, iter_max::Integer=10, λ::Real=0,
+                    term_mask::Union{Nothing,Vector{Float64}}=nothing, max_outer::Integer=50)
+    h = activate(op)
+    GC.@preserve term_mask begin
+        p = Ref(HoeDelayParams(Float64(StartTime), Float64(dt), Float64(Δτ_min), Float64(JumpFact), Float64(λ),
+                               term_mask === nothing ? Ptr{Float64}(C_NULL) : pointer(term_mask),
+                               Int32(iter_max), Int32(max_outer)))
+        res = Ref(HoeDelayResult(0, 0, 0, 0, 0, 0))
+        check(ccall((:hoe_find_delay, libhoe), Cint,
+                    (Ptr{Cvoid}, Ref{HoeDelayParams}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{Float64}, Int64,
+                     CuPtr{ComplexF32}, Ref{HoeDelayResult}, CUDA.CUstream),
+                    h, p, data, weights === nothing ? CU_NULL : weights, kspha, size(kspha, 1), CU_NULL, res,
+                    stream_handle()), h)
+    end
+    return res[].tau
 end
 
 end # module
