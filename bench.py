@@ -46,8 +46,8 @@ L2_FLUSH_BYTES = 256 << 20
 # the 200x200 / 12,000-sample / 16-coil workload (profiles/tc_engine_cfg2.md,
 # profiles/simt_engine_cfg2.md).  Other workloads report None.
 NCU_TRAFFIC_BYTES = {
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "forward"): 138_285_056,
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "adjoint"): 138_285_056,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "forward"): 138_285_056 + 4_443_136,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "adjoint"): 138_285_056 + 4_443_136,
     ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "forward"): 40_267_776 + 25_856,
     ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "adjoint"): 36_679_424 + 11_776,
 }
