@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the second engine")
     ap.add_argument("--no-recon", action="store_true", help="skip timing the device CGNR solve")
     ap.add_argument("--recon-iterations", type=int, default=20)
+    ap.add_argument("--autotune", action="store_true",
+                    help="time every execution plan on the workload and keep the fastest (always on for config 3)")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -406,6 +408,31 @@ def time_backward(op, x, y, flush, stream, reps):
             "engine": "fp32 (CUDA cores)"}
 
 
+def time_normal(op, w, x, flush, stream, reps):
+    """E^H D E (hoe_normal) with square-root-density-like weights squared:
+    2*nVox*nSam voxel.samples per application."""
+    import torch
+    from hoexplicit import normalOperator
+    kr = np.hypot(w.kspha[1], w.kspha[2])
+    D = normalOperator(op, np.tile(0.05 + kr / kr.max(), w.nCha))
+    out = torch.empty(op.ncol, dtype=torch.complex64, device=x.device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(3):
+        D.prod_(out, x)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        D.prod_(out, x)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms.append(ev0.elapsed_time(ev1))
+    m = statistics.mean(ms)
+    return {"ms_per_call": m, "value": 2.0 * w.nVox * w.nSam / (m / 1e3), "unit": UNIT}
+
+
 def run_gb300(a):
     import torch
     ws, rank, local = dist_env()
@@ -432,6 +459,10 @@ def run_gb300(a):
     if op is None:
         raise SystemExit("no engine available")
     engine = engines_avail[0]
+    tuned = None
+    if a.autotune or a.config == "3":
+        tuned = op.autotune(reps=3)
+        engine = tuned["engine"]
     op.set_timing(True)
     info = op.info()
     stream = torch.cuda.current_stream()
@@ -515,6 +546,12 @@ def run_gb300(a):
             out["backward"] = time_backward(op, x, y, flush, stream, max(3, a.steps // 4))
         except Exception as exc:  # report, do not substitute
             out["backward"] = {"error": str(exc)}
+    try:
+        out["normal"] = time_normal(op, w, x, flush, stream, max(3, a.steps // 2))
+    except Exception as exc:  # report, do not substitute
+        out["normal"] = {"error": str(exc)}
+    if tuned is not None:
+        out["autotune"] = tuned
 
     # end-to-end through the public API with host (pinned) buffers
     if not a.no_e2e:

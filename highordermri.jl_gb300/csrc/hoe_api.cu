@@ -791,6 +791,86 @@ int hoe_check(hoe_handle *h, void *stream) {
   return HOE_OK;
 }
 
+int hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *o, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  if (!o) return fail(h, HOE_ERR_ARG, "output must not be NULL");
+  if (reps < 1) return fail(h, HOE_ERR_ARG, "reps must be >= 1");
+  memset(o, 0, sizeof(*o));
+  DeviceGuard guard(h->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  const auto &t = h->t;
+  float2 *x = nullptr, *y = nullptr, *xo = nullptr, *yo = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&x, (size_t)t.nFull * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&xo, (size_t)t.nFull * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&y, (size_t)t.nSam * t.nCha * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&yo, (size_t)t.nSam * t.nCha * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemsetAsync(x, 0, (size_t)t.nFull * sizeof(float2), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(y, 0, (size_t)t.nSam * t.nCha * sizeof(float2), st);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const int savedTiming = h->timing;
+  h->timing = 0;
+  const int defF = h->splitF, defA = h->splitA, defEngine = h->engine;
+  struct Cand { int engine, sf, sa; };
+  std::vector<Cand> cands;
+  for (int div : {4, 2, 1}) {
+    Cand c{HOE_ENGINE_FP32_SIMT, std::max(1, defF / div), std::max(1, defA / div)};
+    bool dup = false;
+    for (auto &k : cands) dup = dup || (k.sf == c.sf && k.sa == c.sa);
+    if (!dup) cands.push_back(c);
+  }
+  std::string why;
+  if (hoe::tc_supported(h, &why)) {
+    if (!h->tc.ready && e == cudaSuccess) {
+      cudaError_t te = hoe::tc_prepare(h);
+      if (te != cudaSuccess) cudaGetLastError();
+    }
+    if (h->tc.ready) cands.push_back({HOE_ENGINE_TC_BF16X3, 0, 0});
+  }
+  float best = INFINITY;
+  Cand bestC{defEngine, defF, defA};
+  for (size_t i = 0; i < cands.size() && e == cudaSuccess && i < 8; ++i) {
+    const Cand &c = cands[i];
+    h->engine = c.engine;
+    if (c.engine == HOE_ENGINE_FP32_SIMT) { h->splitF = c.sf; h->splitA = c.sa; }
+    else { h->splitF = defF; h->splitA = defA; }
+    auto run = [&]() {
+      cudaError_t r = hoe::prep_Z(h, x, st);
+      if (r == cudaSuccess)
+        r = c.engine == HOE_ENGINE_TC_BF16X3 ? hoe::tc_forward(h, nullptr, yo, nullptr, hoe::FWD_TO_Y, st)
+                                             : hoe::simt_forward(h, nullptr, yo, nullptr, hoe::FWD_TO_Y, st);
+      if (r == cudaSuccess) r = hoe::apply_adjoint_weighted(h, y, nullptr, xo, st);
+      return r;
+    };
+    e = run();  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = run();
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    ms /= (float)reps;
+    o->cand_engine[i] = c.engine;
+    o->cand_split[i] = c.engine == HOE_ENGINE_FP32_SIMT ? c.sf : 0;
+    o->cand_ms[i] = ms;
+    o->candidates = (int)i + 1;
+    if (e == cudaSuccess && ms < best) { best = ms; bestC = {c.engine, h->splitF, h->splitA}; }
+  }
+  h->engine = bestC.engine;
+  h->splitF = bestC.sf;
+  h->splitA = bestC.sa;
+  h->timing = savedTiming;
+  o->engine = h->engine;
+  o->split_forward = h->splitF;
+  o->split_adjoint = h->splitA;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(x); cudaFree(xo); cudaFree(y); cudaFree(yo);
+  return finish(h, e, "hoe_autotune");
+}
+
 int hoe_forward(hoe_handle *h, const void *x, void *y, void *stream) {
   int rc = check_usable(h);
   if (rc) return rc;

@@ -37,7 +37,7 @@ EXPORTED = (
     "hoe_forward_noalloc", "hoe_check", "hoe_plan", "hoe_recon",
     "hoe_batch_create", "hoe_batch_free", "hoe_batch_last_error", "hoe_batch_get_info",
     "hoe_batch_forward", "hoe_batch_adjoint", "hoe_batch_normal", "hoe_batch_recon", "hoe_batch_check",
-    "hoe_set_kspha", "hoe_kdot_stencil", "hoe_interp_traj_time", "hoe_find_delay",
+    "hoe_set_kspha", "hoe_kdot_stencil", "hoe_interp_traj_time", "hoe_find_delay", "hoe_autotune",
 )
 
 HOE_CG_ITERATION_LIMIT = 0
@@ -127,6 +127,14 @@ class HoeDelayResult(ctypes.Structure):
     ]
 
 
+class HoeTuneResult(ctypes.Structure):
+    _fields_ = [
+        ("engine", ctypes.c_int32), ("split_forward", ctypes.c_int32), ("split_adjoint", ctypes.c_int32),
+        ("candidates", ctypes.c_int32), ("cand_engine", ctypes.c_int32 * 8), ("cand_split", ctypes.c_int32 * 8),
+        ("cand_ms", ctypes.c_float * 8),
+    ]
+
+
 class HoeBatchInfo(ctypes.Structure):
     _fields_ = [
         ("n", ctypes.c_int32), ("contraction_launches", ctypes.c_int32), ("launches", ctypes.c_int64),
@@ -196,6 +204,7 @@ def load():
     lib.hoe_batch_check.argtypes = [H, vp]
     I64 = ctypes.c_int64
     lib.hoe_set_kspha.argtypes = [H, vp, vp, vp]
+    lib.hoe_autotune.argtypes = [H, ctypes.c_int32, ctypes.POINTER(HoeTuneResult), vp]
     lib.hoe_kdot_stencil.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, vp, vp]
     lib.hoe_interp_traj_time.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, ctypes.c_double, vp, I64, vp,
                                          ctypes.c_int32, vp]

@@ -256,6 +256,17 @@ class ExplicitGB300Op:
         bounded-wait timeout (hoe_check)."""
         _lib.check(_lib.load().hoe_check(self._handle(), self._stream()), self._h)
 
+    def autotune(self, reps: int = 5) -> dict:
+        """Time forward+adjoint for each execution plan (FP32 engine at three
+        split-K factors, tensor-core engine) and keep the fastest (hoe_autotune)."""
+        r = _lib.HoeTuneResult()
+        _lib.check(_lib.load().hoe_autotune(self._handle(), int(reps), ctypes.byref(r), self._stream()), self._h)
+        names = {v: k for k, v in (("fp32", _lib.HOE_ENGINE_FP32_SIMT), ("tc", _lib.HOE_ENGINE_TC_BF16X3))}
+        self.engine = names[r.engine]
+        return {"engine": self.engine, "split_forward": r.split_forward, "split_adjoint": r.split_adjoint,
+                "candidates": [{"engine": names[r.cand_engine[i]], "split": r.cand_split[i], "ms": r.cand_ms[i]}
+                               for i in range(r.candidates)]}
+
     def set_engine(self, engine: str) -> None:
         if engine not in ENGINES:
             raise ArgumentError(f"unknown engine {engine!r}")

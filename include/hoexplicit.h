@@ -50,6 +50,8 @@
  *   hoe_interp_traj_time
  *                     InterpTrajTime, src/Synchronization/InterpTraj.jl:18-40 (Akima)
  *   hoe_find_delay    FindDelay, src/Synchronization/FindDelay.jl:139-214
+ *   hoe_autotune      no reference counterpart (the reference's backend and nBlock
+ *                     are chosen by the caller, HighOrderExplicitOp.jl:48-50)
  *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
  *   hoe_free          releases the host handle (Julia finalizer)
  *   hoe_set_timing / hoe_get_timings
@@ -174,6 +176,17 @@ typedef struct hoe_delay_result {
                                       2 stopped: ||B x|| = 0 or a non-finite update      */
 } hoe_delay_result;
 
+/* Result of hoe_autotune: the candidates tried, in order, and the choice. */
+typedef struct hoe_tune_result {
+    int32_t engine;                /* chosen engine                                       */
+    int32_t split_forward;         /* chosen split-K factors of the FP32 engine           */
+    int32_t split_adjoint;
+    int32_t candidates;            /* entries used below (<= 8)                           */
+    int32_t cand_engine[8];
+    int32_t cand_split[8];         /* forward split-K factor (FP32 engine), 0 otherwise   */
+    float   cand_ms[8];            /* mean forward+adjoint time of each candidate (ms)    */
+} hoe_tune_result;
+
 typedef struct hoe_batch_info {
     int32_t n;                     /* member operators                                   */
     int32_t contraction_launches;  /* contraction kernels per direction for all members  */
@@ -216,6 +229,13 @@ HOE_API int  hoe_get_timings(hoe_handle *h, hoe_timings *out);
  * HOE_ERR_TIMEOUT when a bounded wait inside a kernel ran out (the kernel
  * then skipped its remaining work).  The word is cleared after reporting. */
 HOE_API int  hoe_check(hoe_handle *h, void *stream);
+
+/* Times forward+adjoint of this operator for each available execution plan
+ * (the FP32 engine at split-K factors 1/4, 1/2 and 1 of its default, and the
+ * tensor-core engine) with CUDA events on `stream`, `reps` repetitions each,
+ * and keeps the fastest.  Waits for the stream.  Counterpart of choosing
+ * :array / :kernel / nBlock in the reference by hand. */
+HOE_API int  hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *out, void *stream);
 
 /* Operator applications (complex64 device vectors) */
 HOE_API int  hoe_forward(hoe_handle *h, const void *x_dev, void *y_dev, void *stream);

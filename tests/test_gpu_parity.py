@@ -292,3 +292,17 @@ def test_timing_trace():
     assert t["forward_kernel_ms"] > 0 and t["adjoint_kernel_ms"] > 0
     assert t["forward_total_ms"] >= t["forward_kernel_ms"]
     assert t["launches"] >= 6
+
+
+def test_autotune_keeps_results_correct():
+    w = workloads.small(seed=31, shape=(20, 17, 1), nSam=700, nCha=4)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    r = op.autotune(reps=2)
+    assert r["engine"] in ("fp32", "tc") and len(r["candidates"]) >= 2
+    assert all(c["ms"] > 0 for c in r["candidates"])
+    assert min(r["candidates"], key=lambda c: c["ms"])["engine"] == r["engine"]
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    assert dense.rel(host(op * dev(w.x)), oracle.forward(m, w.x[idx])) < TOL[r["engine"]]
+    op.check()
+    op.close()
