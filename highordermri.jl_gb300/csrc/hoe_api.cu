@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -789,6 +790,45 @@ int hoe_check(hoe_handle *h, void *stream) {
     }
   }
   return HOE_OK;
+}
+
+int hoe_coil_gram(const void *A, int32_t complex128, int64_t nObs, int32_t nCoil, int32_t center, double *G,
+                  void *stream) {
+  if (!A || !G) return fail(nullptr, HOE_ERR_ARG, "A must be a device pointer and G a host pointer");
+  if (nObs < 1 || nCoil < 1 || nCoil > 128) return fail(nullptr, HOE_ERR_ARG, "need nObs >= 1 and 1 <= nCoil <= 128");
+  std::vector<std::complex<double>> g;
+  cudaError_t e = hoe::coil_gram(A, complex128 != 0, nObs, nCoil, center != 0, g, (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "hoe_coil_gram");
+  for (int i = 0; i < nCoil; ++i)
+    for (int j = 0; j < nCoil; ++j) {
+      const std::complex<double> v = g[(size_t)i * nCoil + j];
+      G[2 * ((size_t)j * nCoil + i)] = v.real();
+      G[2 * ((size_t)j * nCoil + i) + 1] = v.imag();
+    }
+  return HOE_OK;
+}
+
+int hoe_coil_fit(const void *A, int32_t complex128, int64_t nObs, int32_t nCoil, int32_t nVirtual,
+                 double energyThreshold, const double *noiseCov, double scale, double *matrix, double *sv,
+                 int32_t *rank, double *retained, void *stream) {
+  if (!A || !matrix || !sv || !rank || !retained)
+    return fail(nullptr, HOE_ERR_ARG, "A must be a device pointer; matrix, sv, rank and retained host pointers");
+  std::string why;
+  int r = 0;
+  int rc = hoe::coil_fit(A, complex128 != 0, nObs, nCoil, nVirtual, energyThreshold, noiseCov, scale, matrix, sv, &r,
+                         retained, &why, (cudaStream_t)stream);
+  if (rc != HOE_OK) return fail(nullptr, rc, "%s", why.c_str());
+  *rank = r;
+  return HOE_OK;
+}
+
+int hoe_coil_apply(const void *a, int64_t n, int32_t nCoil, const void *M, int32_t nVirt, void *out, void *stream) {
+  if (!a || !M || !out) return fail(nullptr, HOE_ERR_ARG, "a, M and out must be device pointers");
+  if (n < 1 || nCoil < 1 || nCoil > 128 || nVirt < 1 || nVirt > nCoil)
+    return fail(nullptr, HOE_ERR_ARG, "need n >= 1, 1 <= nCoil <= 128 and 1 <= nVirt <= nCoil");
+  cudaError_t e = hoe::coil_apply((const float2 *)a, n, nCoil, (const float2 *)M, nVirt, (float2 *)out,
+                                  (cudaStream_t)stream);
+  return finish(nullptr, e, "hoe_coil_apply");
 }
 
 int hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *o, void *stream) {

@@ -34,6 +34,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <complex>
 #include <string>
 #include <vector>
 #include "hoexplicit.h"
@@ -229,6 +230,15 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
 // enqueues one complete solve without a graph of its own.
 cudaError_t cg_prepare(hoe_handle *h);
 cudaError_t cg_enqueue(hoe_handle *h, const float2 *data, const float2 *w, float2 *x, const CgRequest &r,
+                       cudaStream_t st);
+
+// SVD coil compression (hoe_coils.cu).  G is row-major complex128.
+cudaError_t coil_gram(const void *A, int doubleInput, int64_t nObs, int nCoil, int center,
+                      std::vector<std::complex<double>> &G, cudaStream_t st);
+int coil_fit(const void *A, int doubleInput, int64_t nObs, int nCoil, int nVirtual, double energyThreshold,
+             const double *noiseCov, double scale, double *matrixOut, double *svOut, int *rankOut,
+             double *retainedOut, std::string *why, cudaStream_t st);
+cudaError_t coil_apply(const float2 *a, int64_t n, int nCoil, const float2 *M, int nVirt, float2 *out,
                        cudaStream_t st);
 
 // Sets the thread's handle-less error message (hoe_last_error(NULL)).

@@ -14,6 +14,8 @@ from .operator import (AdjointOp, ExplicitGB300Op, HighOrderExplicitOp, NormalOp
 from .recon import CGNR, L2Regularization, recon_HOOp  # noqa: F401
 from .batch import OperatorBatch  # noqa: F401
 from .sync import FindDelay, InterpTrajTime, kspha_dt, set_kspha  # noqa: F401
+from .coils import (CoilCompressionTransform, apply_coil_compression, compress_coils,  # noqa: F401
+                    estimate_noise_covariance, fit_coil_compression, noise_prewhitening_scale_factor)
 
 __all__ = [
     "ArgumentError", "DimensionMismatch", "HoeError", "OutOfMemoryError", "Grid",
@@ -21,4 +23,6 @@ __all__ = [
     "AdjointOp", "NormalOp", "WeightingOp", "WeightedOp", "compose", "normalOperator",
     "explicit_gpu_normal", "close", "load", "CGNR", "L2Regularization", "recon_HOOp",
     "OperatorBatch", "FindDelay", "InterpTrajTime", "kspha_dt", "set_kspha",
+    "CoilCompressionTransform", "apply_coil_compression", "compress_coils", "estimate_noise_covariance",
+    "fit_coil_compression", "noise_prewhitening_scale_factor",
 ]

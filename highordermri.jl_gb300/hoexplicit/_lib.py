@@ -38,6 +38,7 @@ EXPORTED = (
     "hoe_batch_create", "hoe_batch_free", "hoe_batch_last_error", "hoe_batch_get_info",
     "hoe_batch_forward", "hoe_batch_adjoint", "hoe_batch_normal", "hoe_batch_recon", "hoe_batch_check",
     "hoe_set_kspha", "hoe_kdot_stencil", "hoe_interp_traj_time", "hoe_find_delay", "hoe_autotune",
+    "hoe_coil_gram", "hoe_coil_fit", "hoe_coil_apply",
 )
 
 HOE_CG_ITERATION_LIMIT = 0
@@ -205,6 +206,11 @@ def load():
     I64 = ctypes.c_int64
     lib.hoe_set_kspha.argtypes = [H, vp, vp, vp]
     lib.hoe_autotune.argtypes = [H, ctypes.c_int32, ctypes.POINTER(HoeTuneResult), vp]
+    DP = ctypes.POINTER(ctypes.c_double)
+    lib.hoe_coil_gram.argtypes = [vp, ctypes.c_int32, I64, ctypes.c_int32, ctypes.c_int32, DP, vp]
+    lib.hoe_coil_fit.argtypes = [vp, ctypes.c_int32, I64, ctypes.c_int32, ctypes.c_int32, ctypes.c_double, DP,
+                                 ctypes.c_double, DP, DP, ctypes.POINTER(ctypes.c_int32), DP, vp]
+    lib.hoe_coil_apply.argtypes = [vp, I64, ctypes.c_int32, vp, ctypes.c_int32, vp, vp]
     lib.hoe_kdot_stencil.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, vp, vp]
     lib.hoe_interp_traj_time.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, ctypes.c_double, vp, I64, vp,
                                          ctypes.c_int32, vp]

@@ -50,6 +50,9 @@
  *   hoe_interp_traj_time
  *                     InterpTrajTime, src/Synchronization/InterpTraj.jl:18-40 (Akima)
  *   hoe_find_delay    FindDelay, src/Synchronization/FindDelay.jl:139-214
+ *   hoe_coil_gram / hoe_coil_fit / hoe_coil_apply
+ *                     estimate_noise_covariance, fit_coil_compression and
+ *                     apply_coil_compression, src/Recon/CoilCompression.jl:127-301
  *   hoe_autotune      no reference counterpart (the reference's backend and nBlock
  *                     are chosen by the caller, HighOrderExplicitOp.jl:48-50)
  *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
@@ -299,6 +302,29 @@ HOE_API int  hoe_set_kspha(hoe_handle *h, const double *kspha_dev, const double 
 HOE_API int  hoe_find_delay(hoe_handle *h, const hoe_delay_params *params, const void *data_dev,
                             const void *weights_dev, const double *traj_dev, int64_t nField,
                             void *x_dev, hoe_delay_result *out, void *stream);
+
+/* SVD coil compression (src/Recon/CoilCompression.jl:150-353).  Matrices are
+ * column-major: A [nObs x nCoil] observations by coils on the device
+ * (complex64, or complex128 when complex128 != 0), host outputs complex128.
+ *   hoe_coil_gram   G = (A - 1 m^T)^H (A - 1 m^T) in FP64 (m the column means
+ *                   when center, else 0): estimate_noise_covariance divides
+ *                   by nObs - 1 (center) or nObs
+ *   hoe_coil_fit    fit_coil_compression: exactly one of n_virtual (> 0) and
+ *                   energy_threshold (in (0, 1]); noise_cov NULL or a host
+ *                   complex128 [nCoil x nCoil] covariance, scale the
+ *                   prewhitening scale factor.  matrix receives W*V[:, 1:rank]
+ *                   (room for nCoil x nCoil), sv the min(nObs, nCoil)
+ *                   singular values of A*W
+ *   hoe_coil_apply  apply_coil_compression: out [n x nVirt] = a [n x nCoil] * M
+ *                   (device complex64) */
+HOE_API int  hoe_coil_gram(const void *A_dev, int32_t complex128, int64_t nObs, int32_t nCoil, int32_t center,
+                           double *G_host, void *stream);
+HOE_API int  hoe_coil_fit(const void *A_dev, int32_t complex128, int64_t nObs, int32_t nCoil, int32_t n_virtual,
+                          double energy_threshold, const double *noise_cov_host, double scale,
+                          double *matrix_host, double *sv_host, int32_t *rank, double *retained_energy,
+                          void *stream);
+HOE_API int  hoe_coil_apply(const void *a_dev, int64_t n, int32_t nCoil, const void *M_dev, int32_t nVirt,
+                            void *out_dev, void *stream);
 
 /* Batches of operators on one device (e.g. the slices of a multi-slice scan).
  * A batch borrows its members: free the batch before freeing a member, and a
