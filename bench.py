@@ -502,6 +502,16 @@ def run_gb300(a):
                 "kernel_ms": dom_ms, "flops_per_launch": flops_per_launch,
                 "frac_of_split_peak": achieved / (bf16_peak / 3.0) if engine == "tc" else None,
                 "share_of_step": (fk + ak) / ms_per_step}
+    if engine == "tc":
+        # The phase generator's binding pipe: two MUFU ops (sin, cos) per pair,
+        # 16 per clock per SM (measured with a MUFU-only probe at 92% of it).
+        sm_mhz = clk.summary().get("sm_mhz") or 2070.0
+        sfu_peak = 16.0 * 152 * sm_mhz * 1e6                # sin/cos per second
+        sfu_achieved = 2.0 * w.nVox * w.nSam / (dom_ms / 1e3)
+        roofline["binding"] = {"pipe": "sfu (MUFU sin/cos)", "achieved": sfu_achieved / 1e12,
+                               "peak": sfu_peak / 1e12, "unit": "T sin-or-cos/s",
+                               "frac": sfu_achieved / sfu_peak,
+                               "note": "16 MUFU ops per clock per SM at the sampled SM clock"}
     if engine == "fp32":
         sm_mhz = clk.summary().get("sm_mhz") or 1900.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
