@@ -343,7 +343,7 @@ struct Tmem {
 //   RV  [2][hi,lo]    TF32 row residual tile, 128 x KP (one per row-tile parity)
 //   XR  [NS][data,0]  TF32 anchor k-step, row side: 128 rows x 4, then 128 x 4 zeros
 //   XC  [NS][data,0]  TF32 anchor k-step, column side: TV columns x 4, then zeros
-//   barriers: full[NS] empty[NS] afull[ABUF] aempty[ABUF] segdone[2]
+//   barriers: full[NS] empty[NS] afull[ABUF] segdone[2]
 //             tmemfree[2] pfull[PD] pfree[PD] rfull[2] rfree[2]
 // The residual-phase issuer runs up to PD stages ahead of the phase warps.
 template <int N, int KP, int NS>
@@ -361,7 +361,7 @@ struct Smem {
   static constexpr size_t XR_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
   static constexpr size_t XC_OFF = XR_OFF + (size_t)NS * 2 * XR_BYTES;
   static constexpr size_t BAR_OFF = (XC_OFF + (size_t)NS * 2 * XC_BYTES + 7) / 8 * 8;
-  static constexpr int NBAR = 2 * NS + 2 * ABUF + 8 + 2 * PD;
+  static constexpr int NBAR = 2 * NS + ABUF + 8 + 2 * PD;
   static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
@@ -389,8 +389,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
   uint64_t *empty = full + NS;        // B-ring stage consumed by the contraction MMAs
   uint64_t *afull = empty + NS;       // [ABUF] TMEM phase tile written (16 phase warps)
-  uint64_t *aempty = afull + ABUF;    // [ABUF] TMEM phase tile consumed by the MMAs
-  uint64_t *segdone = aempty + ABUF;  // [2] accumulator buffer complete (group of stages)
+  uint64_t *segdone = afull + ABUF;   // [2] accumulator buffer complete (group of stages)
   uint64_t *tmemfree = segdone + 2;   // [2] accumulator buffer read out
   uint64_t *pfull = tmemfree + 2;     // [PD] residual-phase TMEM tile computed
   uint64_t *pfree = pfull + PD;       // [PD] residual-phase TMEM tile read out
@@ -418,7 +417,6 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     }
     for (int i = 0; i < ABUF; ++i) {
       mbar_init(&afull[i], GROUP_WARPS);
-      mbar_init(&aempty[i], NISS);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&segdone[i], NISS);
@@ -553,8 +551,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         uint32_t hi[16], lo[16];
         tmem_ld16(pBase, d);
         phase16(d, hi, lo);
-        // TMEM phase tile buffer: free once the contraction of stage it-ABUF is done
-        if (ar > 0 && !wait_bar(&aempty[ab], (ar - 1) & 1, abort, p.err)) { ok = false; break; }
+        // TMEM phase tile buffer: free once the contraction of stage it-ABUF is
+        // done, which the stage's `empty` barrier records (the slot of stage
+        // it-ABUF cannot have been reused: that needs this stage's tile)
+        if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err)) { ok = false; break; }
         tc_fence_after();
         tmem_st16(aBase, hi);
         tmem_st16(aBase + TV, lo);
@@ -624,9 +624,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
           umma_ta(dt, aLo + ka, bHi + kb, idescC, 1u);
         }
         umma_commit(&empty[slot]);
-        umma_commit(&aempty[ab]);
-        lastBar = &aempty[ab];
-        lastPar = ar & 1;
+        lastBar = &empty[slot];
+        lastPar = round & 1;
         if (last) umma_commit(&segdone[grp & 1]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);  // MMAs done before TMEM is freed
