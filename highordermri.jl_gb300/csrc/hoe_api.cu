@@ -877,10 +877,7 @@ int hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *o, void *stream) 
     if (c.engine == HOE_ENGINE_FP32_SIMT) { h->splitF = c.sf; h->splitA = c.sa; }
     else { h->splitF = defF; h->splitA = defA; }
     auto run = [&]() {
-      cudaError_t r = hoe::prep_Z(h, x, st);
-      if (r == cudaSuccess)
-        r = c.engine == HOE_ENGINE_TC_BF16X3 ? hoe::tc_forward(h, nullptr, yo, nullptr, hoe::FWD_TO_Y, st)
-                                             : hoe::simt_forward(h, nullptr, yo, nullptr, hoe::FWD_TO_Y, st);
+      cudaError_t r = hoe::apply_forward(h, x, yo, st);
       if (r == cudaSuccess) r = hoe::apply_adjoint_weighted(h, y, nullptr, xo, st);
       return r;
     };
@@ -918,11 +915,7 @@ int hoe_forward(hoe_handle *h, const void *x, void *y, void *stream) {
   DeviceGuard guard(h->device);
   cudaStream_t st = (cudaStream_t)stream;
   hoe::trace(h, hoe::EV_F0, st);
-  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
-  if (e == cudaSuccess)
-    e = (h->engine == HOE_ENGINE_TC_BF16X3)
-            ? hoe::tc_forward(h, nullptr, (float2 *)y, nullptr, hoe::FWD_TO_Y, st)
-            : hoe::simt_forward(h, nullptr, (float2 *)y, nullptr, hoe::FWD_TO_Y, st);
+  cudaError_t e = hoe::apply_forward(h, (const float2 *)x, (float2 *)y, st);
   hoe::trace(h, hoe::EV_F1, st);
   return finish(h, e, "hoe_forward");
 }
@@ -934,10 +927,7 @@ int hoe_adjoint(hoe_handle *h, const void *y, void *x, void *stream) {
   DeviceGuard guard(h->device);
   cudaStream_t st = (cudaStream_t)stream;
   hoe::trace(h, hoe::EV_A0, st);
-  cudaError_t e = hoe::prep_Yt(h, (const float2 *)y, nullptr, st);
-  if (e == cudaSuccess)
-    e = (h->engine == HOE_ENGINE_TC_BF16X3) ? hoe::tc_adjoint_from_Yt(h, (float2 *)x, st)
-                                            : hoe::simt_adjoint_from_Yt(h, (float2 *)x, st);
+  cudaError_t e = hoe::apply_adjoint_weighted(h, (const float2 *)y, nullptr, (float2 *)x, st);
   hoe::trace(h, hoe::EV_A1, st);
   return finish(h, e, "hoe_adjoint");
 }
@@ -1055,23 +1045,26 @@ cudaError_t build_anchor_tables(const hoe_handle *h, cudaStream_t st) {
   return e;
 }
 
-cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {
+cudaError_t apply_forward(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st) {
+  if (h->engine == HOE_ENGINE_TC_BF16X3) return tc_forward(h, x, y, st);
   cudaError_t e = prep_Z(h, x, st);
-  if (h->engine == HOE_ENGINE_TC_BF16X3) {
-    if (e == cudaSuccess) e = tc_forward(h, nullptr, nullptr, D, FWD_TO_YT_WEIGHTED, st);
-    if (e == cudaSuccess) e = tc_adjoint_from_Yt(h, out, st);
-  } else {
-    if (e == cudaSuccess) e = simt_forward(h, nullptr, nullptr, D, FWD_TO_YT_WEIGHTED, st);
-    if (e == cudaSuccess) e = simt_adjoint_from_Yt(h, out, st);
-  }
+  if (e == cudaSuccess) e = simt_forward(h, nullptr, y, nullptr, FWD_TO_Y, st);
+  return e;
+}
+
+cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {
+  if (h->engine == HOE_ENGINE_TC_BF16X3) return tc_normal(h, D, x, out, st);
+  cudaError_t e = prep_Z(h, x, st);
+  if (e == cudaSuccess) e = simt_forward(h, nullptr, nullptr, D, FWD_TO_YT_WEIGHTED, st);
+  if (e == cudaSuccess) e = simt_adjoint_from_Yt(h, out, st);
   return e;
 }
 
 cudaError_t apply_adjoint_weighted(hoe_handle *h, const float2 *y, const float *D, float2 *x,
                                    cudaStream_t st) {
+  if (h->engine == HOE_ENGINE_TC_BF16X3) return tc_adjoint(h, y, D, x, st);
   cudaError_t e = prep_Yt(h, y, D, st);
-  if (e == cudaSuccess)
-    e = (h->engine == HOE_ENGINE_TC_BF16X3) ? tc_adjoint_from_Yt(h, x, st) : simt_adjoint_from_Yt(h, x, st);
+  if (e == cudaSuccess) e = simt_adjoint_from_Yt(h, x, st);
   return e;
 }
 

@@ -135,16 +135,11 @@ int hoe_batch_forward(hoe_batch *b, const void *const *x, void *const *y, void *
   cudaStream_t st = (cudaStream_t)stream;
   const int64_t l0 = member_launches(b);
   cudaError_t e = cudaSuccess;
-  for (size_t i = 0; i < n && e == cudaSuccess; ++i) e = hoe::prep_Z(b->hs[i], (const float2 *)x[i], st);
   if (b->tcplan) {
-    if (e == cudaSuccess) e = hoe::tc_batch_forward(b->tcplan, (float2 *const *)y, nullptr, hoe::FWD_TO_Y, st);
+    e = hoe::tc_batch_forward(b->tcplan, (const float2 *const *)x, (float2 *const *)y, st);
   } else {
-    for (size_t i = 0; i < n && e == cudaSuccess; ++i) {
-      hoe_handle *h = b->hs[i];
-      e = h->engine == HOE_ENGINE_TC_BF16X3
-              ? hoe::tc_forward(h, nullptr, (float2 *)y[i], nullptr, hoe::FWD_TO_Y, st)
-              : hoe::simt_forward(h, nullptr, (float2 *)y[i], nullptr, hoe::FWD_TO_Y, st);
-    }
+    for (size_t i = 0; i < n && e == cudaSuccess; ++i)
+      e = hoe::apply_forward(b->hs[i], (const float2 *)x[i], (float2 *)y[i], st);
   }
   b->launches += member_launches(b) - l0;
   if (e == cudaSuccess) e = cudaGetLastError();
@@ -161,8 +156,7 @@ int hoe_batch_adjoint(hoe_batch *b, const void *const *y, void *const *x, void *
   const int64_t l0 = member_launches(b);
   cudaError_t e = cudaSuccess;
   if (b->tcplan) {
-    for (size_t i = 0; i < n && e == cudaSuccess; ++i) e = hoe::prep_Yt(b->hs[i], (const float2 *)y[i], nullptr, st);
-    if (e == cudaSuccess) e = hoe::tc_batch_adjoint_from_Yt(b->tcplan, (float2 *const *)x, st);
+    e = hoe::tc_batch_adjoint(b->tcplan, (const float2 *const *)y, nullptr, (float2 *const *)x, st);
   } else {
     for (size_t i = 0; i < n && e == cudaSuccess; ++i)
       e = hoe::apply_adjoint_weighted(b->hs[i], (const float2 *)y[i], nullptr, (float2 *)x[i], st);
@@ -183,9 +177,7 @@ int hoe_batch_normal(hoe_batch *b, const float *const *D, const void *const *x, 
   const int64_t l0 = member_launches(b);
   cudaError_t e = cudaSuccess;
   if (b->tcplan) {
-    for (size_t i = 0; i < n && e == cudaSuccess; ++i) e = hoe::prep_Z(b->hs[i], (const float2 *)x[i], st);
-    if (e == cudaSuccess) e = hoe::tc_batch_forward(b->tcplan, nullptr, D, hoe::FWD_TO_YT_WEIGHTED, st);
-    if (e == cudaSuccess) e = hoe::tc_batch_adjoint_from_Yt(b->tcplan, (float2 *const *)out, st);
+    e = hoe::tc_batch_normal(b->tcplan, D, (const float2 *const *)x, (float2 *const *)out, st);
   } else {
     for (size_t i = 0; i < n && e == cudaSuccess; ++i)
       e = hoe::apply_normal(b->hs[i], D ? D[i] : nullptr, (const float2 *)x[i], (float2 *)out[i], st);

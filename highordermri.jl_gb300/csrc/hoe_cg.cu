@@ -247,13 +247,9 @@ cudaError_t normal_all(const Members &m, const std::vector<float2 *> &xs, const 
   cudaError_t e = cudaSuccess;
   if (m.tcplan) {
     std::vector<const float *> D(m.n);
-    for (int i = 0; i < m.n && e == cudaSuccess; ++i) {
-      D[i] = m.hs[i]->cg.D;
-      e = prep_Z(m.hs[i], xs[i], st);
-    }
-    if (e == cudaSuccess) e = tc_batch_forward(m.tcplan, nullptr, D.data(), FWD_TO_YT_WEIGHTED, st);
-    if (e == cudaSuccess) e = tc_batch_adjoint_from_Yt(m.tcplan, outs.data(), st);
-    return e;
+    std::vector<const float2 *> xc(xs.begin(), xs.end());
+    for (int i = 0; i < m.n; ++i) D[i] = m.hs[i]->cg.D;
+    return tc_batch_normal(m.tcplan, D.data(), xc.data(), outs.data(), st);
   }
   for (int i = 0; i < m.n && e == cudaSuccess; ++i) e = apply_normal(m.hs[i], m.hs[i]->cg.D, xs[i], outs[i], st);
   return e;
@@ -277,8 +273,9 @@ cudaError_t enqueue_solve(const Members &m, const float2 *const *data, const flo
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   // z₀ = HOOpᴴ (|w|² · Data)
   if (m.tcplan) {
-    for (int i = 0; i < n && e == cudaSuccess; ++i) e = prep_Yt(m.hs[i], data[i], m.hs[i]->cg.D, st);
-    if (e == cudaSuccess) e = tc_batch_adjoint_from_Yt(m.tcplan, zs.data(), st);
+    std::vector<const float *> D(n);
+    for (int i = 0; i < n; ++i) D[i] = m.hs[i]->cg.D;
+    e = tc_batch_adjoint(m.tcplan, data, D.data(), zs.data(), st);
   } else {
     for (int i = 0; i < n && e == cudaSuccess; ++i)
       e = apply_adjoint_weighted(m.hs[i], data[i], m.hs[i]->cg.D, zs[i], st);

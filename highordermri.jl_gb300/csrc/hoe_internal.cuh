@@ -191,8 +191,9 @@ cudaError_t simt_reduce_adjoint(const hoe_handle *h, const float2 *part, int spl
 cudaError_t simt_backward(const hoe_handle *h, const float2 *x, const float2 *r,
                           float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
 
-// Operator applications on the active engine (hoe_api.cu), used by the solver:
+// Operator applications on the active engine (hoe_api.cu): y = HOOp x,
 // out = HOOpᴴ diag(D) HOOp x, and x = HOOpᴴ (D · y) (D = NULL: ones).
+cudaError_t apply_forward(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st);
 cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st);
 cudaError_t apply_adjoint_weighted(hoe_handle *h, const float2 *y, const float *D, float2 *x,
                                    cudaStream_t st);
@@ -256,22 +257,28 @@ enum { FWD_TO_Y = 0, FWD_TO_YT_WEIGHTED = 1, FWD_DERIV_TO_Y = 2 };
 // Tensor-core kernels (hoe_tc.cu).
 cudaError_t tc_prepare(hoe_handle *h);
 void tc_release(hoe_handle *h);
-cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y,
-                       const float *D, int mode, cudaStream_t st);
-cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st);
+// Tensor-core applications; each builds its B operand straight from the
+// caller's vector (no Z / Yt staging): y = E x; x = E^H (D . y) (D may be
+// NULL); out = E^H diag(D) E x.
+cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st);
+cudaError_t tc_adjoint(const hoe_handle *h, const float2 *y, const float *D, float2 *x, cudaStream_t st);
+cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st);
 bool tc_supported(const hoe_handle *h, std::string *why);
 int *tc_error_word(const hoe_handle *h);   // device word set by a timed-out wait
 // Rebuilds the tensor-core anchor tables from Atab/Btab (no-op before tc_prepare).
 cudaError_t tc_anchor_tables(const hoe_handle *h, cudaStream_t st);
 // Several operators (tensor-core engine, equal coil counts) in one persistent
 // launch per direction and residual width.  The plan borrows the handles.
-// tc_batch_forward reads each handle's prepared Z; y/D may be NULL per the
-// forward mode as in tc_forward.  tc_batch_adjoint_from_Yt reads each Yt.
+// The batched applications take one device pointer per member; D may be NULL
+// (ones) as a whole or per member.
 void *tc_batch_plan(hoe_handle *const *hs, int n, std::string *why);
 void tc_batch_plan_free(void *plan);
 int *tc_batch_error_word(void *plan);
 int tc_batch_launches(void *plan);         // contraction launches per direction
-cudaError_t tc_batch_forward(void *plan, float2 *const *y, const float *const *D, int mode, cudaStream_t st);
-cudaError_t tc_batch_adjoint_from_Yt(void *plan, float2 *const *x, cudaStream_t st);
+cudaError_t tc_batch_forward(void *plan, const float2 *const *x, float2 *const *y, cudaStream_t st);
+cudaError_t tc_batch_adjoint(void *plan, const float2 *const *y, const float *const *D, float2 *const *x,
+                             cudaStream_t st);
+cudaError_t tc_batch_normal(void *plan, const float *const *D, const float2 *const *x, float2 *const *out,
+                            cudaStream_t st);
 
 }  // namespace hoe

@@ -336,10 +336,8 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
     h->launches += 2;
     if (err == cudaSuccess) err = replan_samples(h, ks, nTerm, kdt, nTerm, mask, s);
     if (err == cudaSuccess) err = cg_enqueue(h, data, weights, x, r, s);
-    if (err == cudaSuccess) err = prep_Z(h, x, s);
-    if (err == cudaSuccess)
-      err = h->engine == HOE_ENGINE_TC_BF16X3 ? tc_forward(h, nullptr, yf, nullptr, FWD_TO_Y, s)
-                                              : simt_forward(h, nullptr, yf, nullptr, FWD_TO_Y, s);
+    if (err == cudaSuccess) err = apply_forward(h, x, yf, s);
+    if (err == cudaSuccess) err = prep_Z(h, x, s);  // the derivative runs on the FP32 engine
     if (err == cudaSuccess) err = simt_forward(h, nullptr, yd, nullptr, FWD_DERIV_TO_Y, s);
     if (err == cudaSuccess) {
       k_delay_dots<<<G, kThreads, 0, s>>>(data, yf, yd, nD, S, part);

@@ -727,44 +727,126 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   }
 }
 
-// B operand of the forward: chunk i covers voxels [i*TV, (i+1)*TV); element
-// (n, k) with k = 2*v_local + r and n = 2*c + q.
-__global__ void k_tc_bop_forward(const float2 *__restrict__ Z, uint16_t *__restrict__ Bop,
-                                 int nChunks, int N, int nChaPad) {
+// One element of a B operand tile: val split into BF16 hi + lo.
+__device__ __forceinline__ void store_bop(uint16_t *tile, int64_t per, int n, int k, float val) {
+  __nv_bfloat16 h = __float2bfloat16_rn(val);
+  __nv_bfloat16 l = __float2bfloat16_rn(val - __bfloat162float(h));
+  uint32_t o = kmajor_off(n, k) / 2;
+  tile[o] = *reinterpret_cast<uint16_t *>(&h);
+  tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+}
+
+// B operand of the forward straight from the image: chunk i covers
+// tile-order voxels [i*TV, (i+1)*TV); element (n, k) with k = 2*v_local + r
+// and n = 2*c + q holds (re, im) of Z = x[perm[v]] * csm[v][c].
+__global__ void k_tc_bop_forward(const float2 *__restrict__ x, const int *__restrict__ perm,
+                                 const float2 *__restrict__ csm, uint16_t *__restrict__ Bop, int nChunks, int N,
+                                 int nChaPad) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t per = (int64_t)N * TK;
   if (i >= (int64_t)nChunks * per) return;
   int ch = (int)(i / per), e = (int)(i % per);
   int n = e / TK, k = e % TK;
   int v = ch * TV + k / 2, r = k & 1, c = n / 2, q = n & 1;
-  float2 z = c < nChaPad ? Z[(int64_t)v * nChaPad + c] : make_float2(0.f, 0.f);
-  float val = r == 0 ? (q == 0 ? z.x : z.y) : (q == 0 ? -z.y : z.x);
-  __nv_bfloat16 h = __float2bfloat16_rn(val);
-  __nv_bfloat16 l = __float2bfloat16_rn(val - __bfloat162float(h));
-  uint16_t *tile = Bop + (size_t)ch * 2 * per;
-  uint32_t o = kmajor_off(n, k) / 2;
-  tile[o] = *reinterpret_cast<uint16_t *>(&h);
-  tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+  float2 z = make_float2(0.f, 0.f);
+  const int g = perm[v];
+  if (c < nChaPad && g >= 0) {
+    const float2 xv = x[g], cv = csm[(int64_t)v * nChaPad + c];
+    z = make_float2(xv.x * cv.x - xv.y * cv.y, xv.x * cv.y + xv.y * cv.x);
+  }
+  store_bop(Bop + (size_t)ch * 2 * per, per, n, k, r == 0 ? (q == 0 ? z.x : z.y) : (q == 0 ? -z.y : z.x));
 }
 
-// B operand of the adjoint from Yt [nSamPad][nChaPad]: chunk i covers
-// samples [i*TV, (i+1)*TV).
-__global__ void k_tc_bop_adjoint(const float2 *__restrict__ Yt, uint16_t *__restrict__ Bop,
-                                 int nChunks, int N, int nChaPad) {
+// B operand of the adjoint straight from the data y (samples fastest, then
+// coils), weighted by D (NULL: ones): chunk i covers samples [i*TV, (i+1)*TV).
+__global__ void k_tc_bop_adjoint(const float2 *__restrict__ y, const float *__restrict__ D,
+                                 uint16_t *__restrict__ Bop, int nChunks, int N, int nSam, int nCha) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t per = (int64_t)N * TK;
   if (i >= (int64_t)nChunks * per) return;
   int ch = (int)(i / per), e = (int)(i % per);
   int n = e / TK, k = e % TK;
   int s = ch * TV + k / 2, r = k & 1, c = n / 2, q = n & 1;
-  float2 y = c < nChaPad ? Yt[(int64_t)s * nChaPad + c] : make_float2(0.f, 0.f);
-  float val = r == 0 ? (q == 0 ? y.x : y.y) : (q == 0 ? y.y : -y.x);
-  __nv_bfloat16 h = __float2bfloat16_rn(val);
-  __nv_bfloat16 l = __float2bfloat16_rn(val - __bfloat162float(h));
-  uint16_t *tile = Bop + (size_t)ch * 2 * per;
-  uint32_t o = kmajor_off(n, k) / 2;
-  tile[o] = *reinterpret_cast<uint16_t *>(&h);
-  tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+  float2 yv = make_float2(0.f, 0.f);
+  if (s < nSam && c < nCha) {
+    const int64_t o = (int64_t)c * nSam + s;
+    yv = y[o];
+    if (D) { const float w = D[o]; yv.x *= w; yv.y *= w; }
+  }
+  store_bop(Bop + (size_t)ch * 2 * per, per, n, k, r == 0 ? (q == 0 ? yv.x : yv.y) : (q == 0 ? yv.y : -yv.x));
+}
+
+// The slots a row tile's partial sums occupy: the CTAs that own any of its
+// work items, in schedule order (work items [first + r*C, first + (r+1)*C)).
+struct SlotMap {
+  int64_t first, W;
+  int C, G;
+  __device__ __forceinline__ int slots(int r) const {
+    return work_owner(first + (int64_t)(r + 1) * C - 1, W, G) - work_owner(first + (int64_t)r * C, W, G) + 1;
+  }
+};
+
+// Forward reduction over the written slots: y[c*nSam + s] = scale * sum, or
+// (bopA != NULL) the adjoint's B operand of D * (scale * sum) for the normal
+// operator.  Threads cover s < nSamPad and c < nChaTC.
+__global__ void k_tc_fwd_reduce(const float2 *__restrict__ part, int nSamPad, int nChaPad, int nChaTC, int nSam,
+                                int nCha, float scale, SlotMap m, float2 *__restrict__ y,
+                                const float *__restrict__ D, uint16_t *__restrict__ bopA, int N) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nSamPad * nChaTC) return;
+  const int s = (int)(i / nChaTC), c = (int)(i % nChaTC);
+  float sr = 0.f, si = 0.f;
+  if (c < nChaPad) {
+    const int ns = m.slots(s / TM);
+    for (int k = 0; k < ns; ++k) {
+      const float2 v = part[((int64_t)k * nSamPad + s) * nChaPad + c];
+      sr += v.x;
+      si += v.y;
+    }
+  }
+  sr *= scale;
+  si *= scale;
+  const bool valid = s < nSam && c < nCha;
+  const int64_t o = (int64_t)c * nSam + s;
+  if (!bopA) {
+    if (valid) y[o] = make_float2(sr, si);
+    return;
+  }
+  const float w = valid ? (D ? D[o] : 1.f) : 0.f;
+  sr *= w;
+  si *= w;
+  const int64_t per = (int64_t)N * TK;
+  uint16_t *tile = bopA + (size_t)(s / TV) * 2 * per;
+  const int sl = s % TV;
+  store_bop(tile, per, 2 * c, 2 * sl, sr);
+  store_bop(tile, per, 2 * c + 1, 2 * sl, si);
+  store_bop(tile, per, 2 * c, 2 * sl + 1, si);
+  store_bop(tile, per, 2 * c + 1, 2 * sl + 1, -sr);
+}
+
+// Adjoint reduction over the written slots: conj(csm), sum over coils,
+// scale, scatter into the full grid (zeroed beforehand).
+__global__ void k_tc_adj_reduce(const float2 *__restrict__ part, int nVoxPad, int nChaPad, int nCha,
+                                const float2 *__restrict__ csm, const int *__restrict__ perm, float scale,
+                                SlotMap m, float2 *__restrict__ x) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nVoxPad) return;
+  const int g = perm[p];
+  if (g < 0) return;
+  const int ns = m.slots(p / TM);
+  float xr = 0.f, xi = 0.f;
+  for (int c = 0; c < nCha; ++c) {
+    float qr = 0.f, qi = 0.f;
+    for (int k = 0; k < ns; ++k) {
+      const float2 v = part[((int64_t)k * nVoxPad + p) * nChaPad + c];
+      qr += v.x;
+      qi += v.y;
+    }
+    const float2 w = csm[(int64_t)p * nChaPad + c];
+    xr += w.x * qr + w.y * qi;   // conj(w) * q
+    xi += w.x * qi - w.y * qr;
+  }
+  x[g] = make_float2(xr * scale, xi * scale);
 }
 
 // Anchor tables of the anchor k-step: v = 2*pi*tab[i] (radians) split into
@@ -986,23 +1068,55 @@ TcSlice slice_adjoint(const hoe_handle *h, const TcBuffers &b) {
   return sl;
 }
 
-// B operand tiles and zeroed partial slots before a contraction launch.
-cudaError_t pre_forward(const hoe_handle *h, const TcBuffers &b, int slots, cudaStream_t st) {
+SlotMap slot_map(int64_t first, int C, int64_t W, int G) {
+  SlotMap m;
+  m.first = first;
+  m.W = W;
+  m.C = C;
+  m.G = G;
+  return m;
+}
+
+cudaError_t bop_forward(const hoe_handle *h, const TcBuffers &b, const float2 *x, cudaStream_t st) {
   const auto &t = h->t;
   const int chunks = t.nVoxPad / TV;
   int64_t n = (int64_t)chunks * b.N * TK;
-  k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Z, b.bopF, chunks, b.N, t.nChaPad);
+  k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, t.perm, t.csm, b.bopF, chunks, b.N, t.nChaPad);
   h->launches += 1;
-  return cudaMemsetAsync(b.part, 0, (size_t)slots * t.nSamPad * t.nChaPad * sizeof(float2), st);
+  return cudaGetLastError();
 }
 
-cudaError_t pre_adjoint(const hoe_handle *h, const TcBuffers &b, int slots, cudaStream_t st) {
+cudaError_t bop_adjoint(const hoe_handle *h, const TcBuffers &b, const float2 *y, const float *D, cudaStream_t st) {
   const auto &t = h->t;
   const int chunks = t.nSamPad / TV;
   int64_t n = (int64_t)chunks * b.N * TK;
-  k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(h->s.Yt, b.bopA, chunks, b.N, t.nChaPad);
+  k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, D, b.bopA, chunks, b.N, t.nSam, t.nCha);
   h->launches += 1;
-  return cudaMemsetAsync(b.part, 0, (size_t)slots * t.nVoxPad * t.nChaPad * sizeof(float2), st);
+  return cudaGetLastError();
+}
+
+// y = E x (toBop false), or the adjoint B operand of D * E x (toBop true).
+cudaError_t reduce_forward(const hoe_handle *h, const TcBuffers &b, const SlotMap &m, float2 *y, const float *D,
+                           bool toBop, cudaStream_t st) {
+  const auto &t = h->t;
+  const int64_t n = (int64_t)t.nSamPad * b.nChaTC;
+  const float scale = (float)(1.0 / sqrt((double)t.nVox));
+  k_tc_fwd_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b.part, t.nSamPad, t.nChaPad, b.nChaTC, t.nSam,
+                                                               t.nCha, scale, m, y, D, toBop ? b.bopA : nullptr,
+                                                               b.N);
+  h->launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t reduce_adjoint(const hoe_handle *h, const TcBuffers &b, const SlotMap &m, float2 *x, cudaStream_t st) {
+  const auto &t = h->t;
+  cudaError_t e = cudaMemsetAsync(x, 0, (size_t)t.nFull * sizeof(float2), st);
+  if (e != cudaSuccess) return e;
+  const float scale = (float)(1.0 / sqrt((double)t.nVox));
+  k_tc_adj_reduce<<<(t.nVoxPad + 255) / 256, 256, 0, st>>>(b.part, t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm,
+                                                           scale, m, x);
+  h->launches += 1;
+  return cudaGetLastError();
 }
 
 TcParams<1> single_params(const hoe_handle *h, const TcBuffers &b, const TcSlice &sl) {
@@ -1028,6 +1142,7 @@ struct TcBatchPlan {
   };
   std::vector<hoe_handle *> hs;
   std::vector<int> slotsF, slotsA;        // partial slots per slice
+  std::vector<SlotMap> mapF, mapA;        // each slice's place in its launch
   std::vector<Group> groups;
   int *err = nullptr;                     // device word shared by the batch's launches
 };
@@ -1043,29 +1158,60 @@ int slots_needed(int64_t first, int rowTiles, int C, int64_t W, int G) {
 
 }  // namespace
 
-cudaError_t tc_forward(const hoe_handle *h, const float2 *, float2 *y, const float *D, int mode,
-                       cudaStream_t st) {
-  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
-  cudaError_t e = pre_forward(h, b, b.slotsF, st);
-  if (e != cudaSuccess) return e;
+namespace {
+
+cudaError_t contract_forward(const hoe_handle *h, const TcBuffers &b, cudaStream_t st) {
   const TcParams<1> p = single_params(h, b, slice_forward(h, b));
   trace(h, EV_FK0, st);
-  e = launch(h, p, h->t.KP, b.N, b.gridF, st);
+  cudaError_t e = launch(h, p, h->t.KP, b.N, b.gridF, st);
   trace(h, EV_FK1, st);
-  if (e != cudaSuccess) return e;
-  return simt_reduce_forward(h, b.part, b.slotsF, y, D, mode, st);
+  return e;
 }
 
-cudaError_t tc_adjoint_from_Yt(const hoe_handle *h, float2 *x, cudaStream_t st) {
-  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
-  cudaError_t e = pre_adjoint(h, b, b.slotsA, st);
-  if (e != cudaSuccess) return e;
+cudaError_t contract_adjoint(const hoe_handle *h, const TcBuffers &b, cudaStream_t st) {
   const TcParams<1> p = single_params(h, b, slice_adjoint(h, b));
   trace(h, EV_AK0, st);
-  e = launch(h, p, h->t.KP, b.N, b.gridA, st);
+  cudaError_t e = launch(h, p, h->t.KP, b.N, b.gridA, st);
   trace(h, EV_AK1, st);
-  if (e != cudaSuccess) return e;
-  return simt_reduce_adjoint(h, b.part, b.slotsA, x, st);
+  return e;
+}
+
+SlotMap single_map_forward(const hoe_handle *h, const TcBuffers &b) {
+  const int C = h->t.nVoxPad / TV;
+  return slot_map(0, C, (int64_t)h->t.nSt * C, b.gridF);
+}
+
+SlotMap single_map_adjoint(const hoe_handle *h, const TcBuffers &b) {
+  const int C = h->t.nSamPad / TV;
+  return slot_map(0, C, (int64_t)h->t.nVt * C, b.gridA);
+}
+
+}  // namespace
+
+cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st) {
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  cudaError_t e = bop_forward(h, b, x, st);
+  if (e == cudaSuccess) e = contract_forward(h, b, st);
+  if (e == cudaSuccess) e = reduce_forward(h, b, single_map_forward(h, b), y, nullptr, false, st);
+  return e;
+}
+
+cudaError_t tc_adjoint(const hoe_handle *h, const float2 *y, const float *D, float2 *x, cudaStream_t st) {
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  cudaError_t e = bop_adjoint(h, b, y, D, st);
+  if (e == cudaSuccess) e = contract_adjoint(h, b, st);
+  if (e == cudaSuccess) e = reduce_adjoint(h, b, single_map_adjoint(h, b), x, st);
+  return e;
+}
+
+cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  cudaError_t e = bop_forward(h, b, x, st);
+  if (e == cudaSuccess) e = contract_forward(h, b, st);
+  if (e == cudaSuccess) e = reduce_forward(h, b, single_map_forward(h, b), nullptr, D, true, st);
+  if (e == cudaSuccess) e = contract_adjoint(h, b, st);
+  if (e == cudaSuccess) e = reduce_adjoint(h, b, single_map_adjoint(h, b), out, st);
+  return e;
 }
 
 void *tc_batch_plan(hoe_handle *const *hs, int n, std::string *why) {
@@ -1073,6 +1219,8 @@ void *tc_batch_plan(hoe_handle *const *hs, int n, std::string *why) {
   P->hs.assign(hs, hs + n);
   P->slotsF.assign(n, 1);
   P->slotsA.assign(n, 1);
+  P->mapF.assign(n, SlotMap{});
+  P->mapA.assign(n, SlotMap{});
   const TcBuffers &b0 = *(const TcBuffers *)hs[0]->tc_host;
   // group by KP, in input order, at most kBatchSlices per launch
   for (int KP : {8, 16, 24}) {
@@ -1108,6 +1256,7 @@ void *tc_batch_plan(hoe_handle *const *hs, int n, std::string *why) {
         const int i = g.idx[k];
         const hoe_handle *h = hs[i];
         const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+        (dir == 0 ? P->mapF : P->mapA)[i] = slot_map(p.s[k].first, p.s[k].nColChunks, W, G);
         const int J = slots_needed(p.s[k].first, p.s[k].nRowTiles, p.s[k].nColChunks, W, G);
         if ((size_t)J * p.s[k].nRowPad * h->t.nChaPad > b.partElems) {
           if (why) *why = "partial-sum buffer of a slice too small for the batched schedule";
@@ -1137,39 +1286,57 @@ void tc_batch_plan_free(void *plan) {
 
 int *tc_batch_error_word(void *plan) { return plan ? ((TcBatchPlan *)plan)->err : nullptr; }
 
-cudaError_t tc_batch_forward(void *plan, float2 *const *y, const float *const *D, int mode, cudaStream_t st) {
-  auto *P = (TcBatchPlan *)plan;
-  const int n = (int)P->hs.size();
+namespace {
+
+cudaError_t batch_contract(TcBatchPlan *P, bool forward, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < n && e == cudaSuccess; ++i)
-    e = pre_forward(P->hs[i], *(const TcBuffers *)P->hs[i]->tc_host, P->slotsF[i], st);
   for (size_t k = 0; k < P->groups.size() && e == cudaSuccess; ++k) {
     const auto &g = P->groups[k];
     const hoe_handle *h0 = P->hs[g.idx[0]];
-    e = launch(h0, g.pF, g.KP, ((const TcBuffers *)h0->tc_host)->N, g.G_F, st);
-  }
-  for (int i = 0; i < n && e == cudaSuccess; ++i) {
-    const TcBuffers &b = *(const TcBuffers *)P->hs[i]->tc_host;
-    e = simt_reduce_forward(P->hs[i], b.part, P->slotsF[i], y ? y[i] : nullptr, D ? D[i] : nullptr, mode, st);
+    e = launch(h0, forward ? g.pF : g.pA, g.KP, ((const TcBuffers *)h0->tc_host)->N, forward ? g.G_F : g.G_A, st);
   }
   return e;
 }
 
-cudaError_t tc_batch_adjoint_from_Yt(void *plan, float2 *const *x, cudaStream_t st) {
+const TcBuffers &buffers(const hoe_handle *h) { return *(const TcBuffers *)h->tc_host; }
+
+}  // namespace
+
+cudaError_t tc_batch_forward(void *plan, const float2 *const *x, float2 *const *y, cudaStream_t st) {
+  auto *P = (TcBatchPlan *)plan;
+  const int n = (int)P->hs.size();
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = bop_forward(P->hs[i], buffers(P->hs[i]), x[i], st);
+  if (e == cudaSuccess) e = batch_contract(P, true, st);
+  for (int i = 0; i < n && e == cudaSuccess; ++i)
+    e = reduce_forward(P->hs[i], buffers(P->hs[i]), P->mapF[i], y[i], nullptr, false, st);
+  return e;
+}
+
+cudaError_t tc_batch_adjoint(void *plan, const float2 *const *y, const float *const *D, float2 *const *x,
+                             cudaStream_t st) {
   auto *P = (TcBatchPlan *)plan;
   const int n = (int)P->hs.size();
   cudaError_t e = cudaSuccess;
   for (int i = 0; i < n && e == cudaSuccess; ++i)
-    e = pre_adjoint(P->hs[i], *(const TcBuffers *)P->hs[i]->tc_host, P->slotsA[i], st);
-  for (size_t k = 0; k < P->groups.size() && e == cudaSuccess; ++k) {
-    const auto &g = P->groups[k];
-    const hoe_handle *h0 = P->hs[g.idx[0]];
-    e = launch(h0, g.pA, g.KP, ((const TcBuffers *)h0->tc_host)->N, g.G_A, st);
-  }
-  for (int i = 0; i < n && e == cudaSuccess; ++i) {
-    const TcBuffers &b = *(const TcBuffers *)P->hs[i]->tc_host;
-    e = simt_reduce_adjoint(P->hs[i], b.part, P->slotsA[i], x[i], st);
-  }
+    e = bop_adjoint(P->hs[i], buffers(P->hs[i]), y[i], D ? D[i] : nullptr, st);
+  if (e == cudaSuccess) e = batch_contract(P, false, st);
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = reduce_adjoint(P->hs[i], buffers(P->hs[i]), P->mapA[i], x[i], st);
+  return e;
+}
+
+cudaError_t tc_batch_normal(void *plan, const float *const *D, const float2 *const *x, float2 *const *out,
+                            cudaStream_t st) {
+  auto *P = (TcBatchPlan *)plan;
+  const int n = (int)P->hs.size();
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < n && e == cudaSuccess; ++i) e = bop_forward(P->hs[i], buffers(P->hs[i]), x[i], st);
+  if (e == cudaSuccess) e = batch_contract(P, true, st);
+  for (int i = 0; i < n && e == cudaSuccess; ++i)
+    e = reduce_forward(P->hs[i], buffers(P->hs[i]), P->mapF[i], nullptr, D ? D[i] : nullptr, true, st);
+  if (e == cudaSuccess) e = batch_contract(P, false, st);
+  for (int i = 0; i < n && e == cudaSuccess; ++i)
+    e = reduce_adjoint(P->hs[i], buffers(P->hs[i]), P->mapA[i], out[i], st);
   return e;
 }
 
