@@ -57,9 +57,11 @@ class _Vec:
             raise ArgumentError(f"{name} must be a torch tensor or numpy array")
         if v.numel() != n:
             raise DimensionMismatch(f"{name} has length {v.numel()}, expected {n}")
+        self.pinned = False
         if v.device.type != "cuda":
             if self.host is None:
                 self.host = "cpu"
+                self.pinned = bool(v.is_pinned())
             v = v.to(device=op.torch_device, non_blocking=False)
         elif v.device.index != op.device:
             raise ArgumentError(f"{name} is on cuda:{v.device.index}, operator on cuda:{op.device}")
@@ -71,6 +73,10 @@ class _Vec:
         if self.host == "numpy":
             return result.cpu().numpy()
         if self.host == "cpu":
+            if self.pinned:  # page-locked in, page-locked out (direct DMA, no staging copy)
+                out = _torch().empty(result.shape, dtype=result.dtype, pin_memory=True)
+                out.copy_(result)
+                return out
             return result.cpu()
         return result
 

@@ -280,6 +280,11 @@ def test_host_round_trip_numpy():
     y = op * g["image"].astype(np.complex64)
     assert isinstance(y, np.ndarray)
     assert dense.rel(y, g["forward"]) < 1e-5
+    # page-locked host tensors come back page-locked
+    xp = torch.from_numpy(g["image"].astype(np.complex64)).pin_memory()
+    yp = op * xp
+    assert yp.device.type == "cpu" and yp.is_pinned()
+    assert dense.rel(yp.numpy(), g["forward"]) < 1e-5
 
 
 def test_timing_trace():
