@@ -250,7 +250,7 @@ int make_plan(const hoe_desc *d, Plan &P) {
     return fail(nullptr, HOE_ERR_ARG, "samples and coils must be positive");
   if ((int64_t)d->nSam * d->nCha > (1ll << 31) - 1)
     return fail(nullptr, HOE_ERR_DIM, "nSam*nCha too large");
-  if (d->engine != HOE_ENGINE_FP32_SIMT && d->engine != HOE_ENGINE_TC_BF16X3)
+  if (d->engine != HOE_ENGINE_FP32_SIMT && d->engine != HOE_ENGINE_TC_BF16X3 && d->engine != HOE_ENGINE_AUTO)
     return fail(nullptr, HOE_ERR_ARG, "unknown engine %d", d->engine);
   if (!d->mask_idx || !d->bf || !d->kspha || !d->times)
     return fail(nullptr, HOE_ERR_ARG, "mask_idx, bf, kspha and times are required");
@@ -656,6 +656,8 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
     return cuda_fail(nullptr, e, "hoe_create: model upload");
   }
   h->engine = d->engine;
+  if (h->engine == HOE_ENGINE_AUTO)
+    h->engine = hoe::tc_supported(h, nullptr) ? HOE_ENGINE_TC_BF16X3 : HOE_ENGINE_FP32_SIMT;
   if (h->engine == HOE_ENGINE_TC_BF16X3) {
     std::string why;
     if (!hoe::tc_supported(h, &why)) {
@@ -724,6 +726,8 @@ int hoe_get_info(const hoe_handle *h, hoe_info *o) {
 int hoe_set_engine(hoe_handle *h, int32_t engine) {
   int rc = check_usable(h);
   if (rc) return rc;
+  if (engine == HOE_ENGINE_AUTO)
+    engine = hoe::tc_supported(h, nullptr) ? HOE_ENGINE_TC_BF16X3 : HOE_ENGINE_FP32_SIMT;
   if (engine == HOE_ENGINE_FP32_SIMT) { h->engine = engine; return HOE_OK; }
   if (engine != HOE_ENGINE_TC_BF16X3) return fail(h, HOE_ERR_ARG, "unknown engine %d", engine);
   std::string why;

@@ -24,6 +24,7 @@ HOE_ERR_UNSUPPORTED = -7
 
 HOE_ENGINE_FP32_SIMT = 0
 HOE_ENGINE_TC_BF16X3 = 1
+HOE_ENGINE_AUTO = 2
 
 HOE_GRAD_KSPHA = 1
 HOE_GRAD_FIELDMAP = 2

@@ -27,8 +27,12 @@ from ._lib import ArgumentError, DimensionMismatch
 from .model import Grid, basisfunc_spha, prep_concomitant, prep_kspha
 
 ENGINES = {"fp32": _lib.HOE_ENGINE_FP32_SIMT, "simt": _lib.HOE_ENGINE_FP32_SIMT,
-           "tc": _lib.HOE_ENGINE_TC_BF16X3, "bf16x3": _lib.HOE_ENGINE_TC_BF16X3}
-DEFAULT_ENGINE = "fp32"
+           "tc": _lib.HOE_ENGINE_TC_BF16X3, "bf16x3": _lib.HOE_ENGINE_TC_BF16X3,
+           "auto": _lib.HOE_ENGINE_AUTO}
+# the tensor-core engine on a GB300, the FP32 engine where it is unavailable
+# (another device, more than 64 coils); ``op.engine`` reports the choice
+DEFAULT_ENGINE = "auto"
+_ENGINE_NAMES = {_lib.HOE_ENGINE_FP32_SIMT: "fp32", _lib.HOE_ENGINE_TC_BF16X3: "tc"}
 
 
 def _torch():
@@ -229,7 +233,7 @@ class ExplicitGB300Op:
         self.ncol = nFull
         self.shape = (self.nrow, self.ncol)
         self.mask = mask
-        self.engine = engine
+        self.engine = _ENGINE_NAMES[self.info()["engine"]]
         self.nprod = self.ntprod = self.nctprod = 0
         self.tprod = None
 
@@ -267,7 +271,7 @@ class ExplicitGB300Op:
         split-K factors, tensor-core engine) and keep the fastest (hoe_autotune)."""
         r = _lib.HoeTuneResult()
         _lib.check(_lib.load().hoe_autotune(self._handle(), int(reps), ctypes.byref(r), self._stream()), self._h)
-        names = {v: k for k, v in (("fp32", _lib.HOE_ENGINE_FP32_SIMT), ("tc", _lib.HOE_ENGINE_TC_BF16X3))}
+        names = _ENGINE_NAMES
         self.engine = names[r.engine]
         return {"engine": self.engine, "split_forward": r.split_forward, "split_adjoint": r.split_adjoint,
                 "candidates": [{"engine": names[r.cand_engine[i]], "split": r.cand_split[i], "ms": r.cand_ms[i]}
@@ -277,7 +281,7 @@ class ExplicitGB300Op:
         if engine not in ENGINES:
             raise ArgumentError(f"unknown engine {engine!r}")
         _lib.check(_lib.load().hoe_set_engine(self._handle(), ENGINES[engine]), self._h)
-        self.engine = engine
+        self.engine = _ENGINE_NAMES[self.info()["engine"]]
 
     def close(self) -> None:
         """Release device resources; idempotent (explicit_gpu_operator.jl:435-446)."""

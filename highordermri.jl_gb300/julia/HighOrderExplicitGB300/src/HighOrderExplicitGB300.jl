@@ -30,6 +30,7 @@ const libhoe = get(ENV, "HOE_LIBRARY",
 const HOE_ABI_VERSION = Int32(1)
 const HOE_ENGINE_FP32_SIMT = Int32(0)
 const HOE_ENGINE_TC_BF16X3 = Int32(1)
+const HOE_ENGINE_AUTO = Int32(2)
 const HOE_GRAD_KSPHA = Int32(1)
 const HOE_GRAD_FIELDMAP = Int32(2)
 const HOE_GRAD_T0_B0 = Int32(4)
@@ -115,19 +116,20 @@ end
 """
     GB300ExplicitOp(grid, kspha, times; fieldmap, csm, mask, concomitant=nothing,
         recon_terms=nothing, k_nominal=kspha[2:4,:], kspha_dt=nothing, gpus=nothing,
-        engine=:tc)
+        engine=:auto)
 
 The `:gb300` implementation of `HighOrderExplicitOp` (see
 HighOrderExplicitOp.jl:44-51).  `engine=:tc` uses the tcgen05 tensor-core
 contraction (split-BF16, FP32 accumulation), `engine=:fp32` the plain FP32
-CUDA-core kernel.  With `kspha_dt` the forward product evaluates the
+CUDA-core kernel, `engine=:auto` the tensor cores where the device and the
+coil count (at most 64) allow them, else the FP32 kernel.  With `kspha_dt` the forward product evaluates the
 derivative `B x` of the reference's kspha_dt mode and concomitant terms are
 ignored (array_operator.jl:139, 159-166).
 """
 function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::AbstractVector{T};
     fieldmap=zeros(T, grid.matrixSize...), csm=ones(Complex{T}, grid.matrixSize..., 1),
     mask=trues(grid.matrixSize...), concomitant=nothing, recon_terms=nothing,
-    k_nominal=kspha[2:4, :], kspha_dt=nothing, gpus=nothing, engine::Symbol=:tc,
+    k_nominal=kspha[2:4, :], kspha_dt=nothing, gpus=nothing, engine::Symbol=:auto,
 ) where {T<:AbstractFloat}
     if gpus !== nothing
         ids = Int.(collect(gpus))
@@ -135,7 +137,7 @@ function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::Abstrac
         0 <= only(ids) < length(collect(CUDA.devices())) || throw(ArgumentError("invalid visible GPU ID"))
         CUDA.device!(only(ids))
     end
-    engine in (:tc, :fp32) || throw(ArgumentError("engine must be :tc or :fp32"))
+    engine in (:tc, :fp32, :auto) || throw(ArgumentError("engine must be :tc, :fp32 or :auto"))
     nTerm, nSam = size(kspha)
     nTerm in (9, 16) || throw(ArgumentError("kspha requires 9 or 16 terms"))
     length(times) == nSam || throw(DimensionMismatch("times and kspha"))
@@ -165,7 +167,7 @@ function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::Abstrac
     GC.@preserve bf64 k64 t64 f64 c128 idx32 kd64 begin
         desc = Ref(HoeDesc(HOE_ABI_VERSION, grid.nX, grid.nY, grid.nZ, nSam, nCha, nTerm,
             Int32(size(k64, 1) != nTerm), nVox,
-            engine === :tc ? HOE_ENGINE_TC_BF16X3 : HOE_ENGINE_FP32_SIMT,
+            engine === :tc ? HOE_ENGINE_TC_BF16X3 : engine === :fp32 ? HOE_ENGINE_FP32_SIMT : HOE_ENGINE_AUTO,
             Int32(CUDA.deviceid(dev)), Int32(0), Int32(0), Int32(0),
             pointer(idx32), pointer(bf64), pointer(k64), pointer(t64), pointer(f64),
             Ptr{Float64}(pointer(c128)), kd64 === nothing ? Ptr{Float64}(C_NULL) : pointer(kd64)))

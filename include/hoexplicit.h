@@ -99,6 +99,8 @@ extern "C" {
 /* contraction engines (hoe_desc.engine, hoe_set_engine) */
 #define HOE_ENGINE_FP32_SIMT  0  /* plain FP32 CUDA-core direct kernel              */
 #define HOE_ENGINE_TC_BF16X3  1  /* tcgen05 tensor cores, split-BF16 3-product, FP32 accumulate */
+#define HOE_ENGINE_AUTO       2  /* hoe_create / hoe_set_engine: the tensor-core engine where the device
+                                    and coil count allow it, else FP32; hoe_get_info reports the choice */
 
 /* hoe_backward flags */
 #define HOE_GRAD_KSPHA     1     /* write dL/dkspha                                   */

@@ -301,7 +301,7 @@ def test_timing_trace():
 
 def test_autotune_keeps_results_correct():
     w = workloads.small(seed=31, shape=(20, 17, 1), nSam=700, nCha=4)
-    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
     r = op.autotune(reps=2)
     assert r["engine"] in ("fp32", "tc") and len(r["candidates"]) >= 2
     assert all(c["ms"] > 0 for c in r["candidates"])
@@ -310,4 +310,21 @@ def test_autotune_keeps_results_correct():
     m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
     assert dense.rel(host(op * dev(w.x)), oracle.forward(m, w.x[idx])) < TOL[r["engine"]]
     op.check()
+    op.close()
+
+
+def test_default_engine_is_chosen_by_the_device():
+    # engine="auto" (the default): the tensor-core engine on a GB300 with at
+    # most 64 coils, the FP32 engine otherwise; op.engine names the choice
+    w = workloads.small(seed=33, shape=(16, 12, 1), nSam=500, nCha=3)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    assert op.engine == ("tc" if have_tc() else "fp32")
+    assert op.info()["engine"] == (1 if op.engine == "tc" else 0)
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    assert dense.rel(host(op * dev(w.x)), oracle.forward(m, w.x[idx])) < TOL[op.engine]
+    op.set_engine("fp32")
+    assert op.engine == "fp32"
+    op.set_engine("auto")
+    assert op.engine == ("tc" if have_tc() else "fp32")
     op.close()

@@ -91,3 +91,19 @@ def test_workload_shapes():
     assert bf.shape == (4096, 16) and c.shape == (4096, 8)
     w3 = workloads.config3()
     assert w3.kspha.shape[1] == 12000 and w3.nCha == 16
+
+
+def test_host_plan_needs_no_device():
+    # hoe_plan validates the descriptor and reports the tiling and the reduced
+    # residual phase basis on the host; the default engine stays "auto" there
+    from hoexplicit import _lib
+    from hoexplicit.operator import plan
+    w = workloads.config1()
+    p = plan(w.grid, w.kspha, w.times, **w.op_kwargs())
+    assert p["engine"] == _lib.HOE_ENGINE_AUTO
+    assert (p["nSam"], p["nCha"], p["nVox"], p["nTermEff"]) == (4096, 8, 4096, 16)
+    assert 1 <= p["residual_rank"] <= p["residual_width"] <= 24
+    assert 0 < p["residual_phase_bound"] < 64 and p["device_bytes"] == 0
+    assert plan(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())["engine"] == _lib.HOE_ENGINE_FP32_SIMT
+    with pytest.raises(ArgumentError):
+        plan(w.grid, w.kspha, w.times, engine="fp16", **w.op_kwargs())

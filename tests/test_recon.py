@@ -136,7 +136,7 @@ def test_recon_docs_example_cartesian():
     kspha = np.zeros((9, nSam))
     kspha[1] = np.tile(np.arange(-4, 4) / (nX * 1e-3), nY)
     kspha[2] = np.repeat(np.arange(-4, 4) / (nY * 1e-3), nX)
-    op = HighOrderExplicitOp(grid, kspha, np.zeros(nSam))
+    op = HighOrderExplicitOp(grid, kspha, np.zeros(nSam), engine="fp32")
     reference = np.zeros((nX, nY, 1), dtype=np.complex64)
     reference[2:6, 2:6, 0] = 1
     samples = (op * reference.reshape(-1, order="F")).reshape(nSam, 1, order="F")
@@ -186,7 +186,7 @@ def test_recon_config1_vs_oracle_cgnr(engine):
 @pytest.mark.gpu
 def test_recon_graph_matches_direct_launches_bitwise():
     w, m, idx, y, weight = _config1_problem()
-    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
     data = y.reshape(w.nCha, w.nSam).T
     a, _ = hrecon.solve(op, data, weight, iterations=8, use_graph=False)
     a = a.clone()
@@ -202,7 +202,7 @@ def test_recon_graph_matches_direct_launches_bitwise():
 @pytest.mark.gpu
 def test_recon_early_convergence_and_regularisation():
     w, m, idx, y, weight = _config1_problem()
-    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
     data = y.reshape(w.nCha, w.nSam).T
     x, st = hrecon.solve(op, data, weight, iterations=50, rel_tol=0.3)
     assert st["status"] == "converged" and st["iterations"] < 50
