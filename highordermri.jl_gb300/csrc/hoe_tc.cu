@@ -23,9 +23,11 @@
 // into BF16 hi/lo and write both into a TMEM A tile with tcgen05.st (lane =
 // row, one 32-bit column = one (re, im) pair).  A loader warp streams the
 // pre-tiled B operand, the TF32 residual tiles and the anchors with
-// cp.async.bulk (TMA bulk copies) onto mbarriers; the MMA thread issues the
-// contraction with A from TMEM and B from shared memory (3 BF16 products)
-// into a double-buffered FP32 TMEM accumulator that is flushed every GROUP
+// cp.async.bulk (TMA bulk copies) onto mbarriers.  Two threads issue the
+// contraction with A from TMEM and B from shared memory: one the product
+// hi x [B_hi | B_lo] as a single MMA of twice the width, the other lo x B_hi
+// (up to 32 coils; beyond that the k-steps are split between them, 3
+// products each).  Their FP32 TMEM accumulators are flushed every GROUP
 // stages into FP32 register sums.  Every mbarrier wait is bounded in time: on
 // timeout the kernel records HOE_ERR_TIMEOUT in a device word, stops
 // issuing work, waits (bounded) for its own copies and MMAs and frees TMEM.
@@ -50,20 +52,22 @@ constexpr int TK = 2 * TV;          // real K per stage (128 BF16 = 8 UMMA k-ste
 // and half of the stage's columns ((warp >> 2) & 1).
 constexpr int PHASE_WARPS = 16;
 constexpr int GROUP_WARPS = PHASE_WARPS / 2;
-// Warp roles: 16 phase warps, two contraction issuers (each one tcgen05.mma
-// stream; issue from a single thread costs ~50 cycles per instruction, so
-// the stage's k-steps are split between them), one residual-phase issuer
-// (TF32 MMAs) that also owns the TMEM allocation, and one loader.
+// Warp roles: 16 phase warps, two contraction issuers, one residual-phase
+// issuer (TF32 MMAs) that also owns the TMEM allocation, and one loader.
+// The MMA instruction count bounds a stage: a thread issuing tcgen05.mma
+// back to back waits 80-200 cycles per instruction almost whatever N is, so
+// the contraction uses as few, wide MMAs as tensor memory allows and splits
+// them over two threads.
 constexpr int CISS_WARP = PHASE_WARPS;        // contraction issuers: warps 16, 17
 constexpr int PISS_WARP = PHASE_WARPS + 2;    // residual-phase issuer, TMEM owner
 constexpr int LOAD_WARP = PHASE_WARPS + 3;
 constexpr int THREADS = (PHASE_WARPS + 4) * 32;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
 
-// The tensor-core FP32 accumulator sums at most GROUP stages (GROUP*24 MMAs)
-// before it is added, in round-to-nearest FP32, into register sums: long
-// accumulation chains in TMEM lose accuracy on coherent sums.
-constexpr int GROUP = 8;
+// A tensor-core FP32 accumulator sums at most GROUP stages (Tmem<N>::GROUP,
+// at most 256 MMAs per accumulator) before it is added, in round-to-nearest
+// FP32, into register sums: long accumulation chains in TMEM lose accuracy
+// on coherent sums.
 
 // byte offset of element (r, k) in a no-swizzle K-major tile with K = TK:
 // core matrices of 8 rows x 16 B; cores adjacent in K are 128 B apart (LBO),
@@ -172,13 +176,6 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
           smem_u32(dst)),
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
-}
-__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                     uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 __device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
@@ -325,13 +322,24 @@ struct Cursor {
 
 // Tensor-memory plan (512 columns): BF16 phase tiles ABUF x [hi TV | lo TV]
 // columns (one 32-bit column per complex element), residual-phase tiles
-// PD x TV FP32 columns, accumulators 2 (groups) x NISS (issuers) x N FP32
-// columns.
+// PD x TV FP32 columns, ACCBUF accumulator sets of ACCW FP32 columns.
+//   PSPLIT (N <= 64): issuer 0 accumulates hi x [B_hi | B_lo] into 2N
+//     columns [hi.B_hi | hi.B_lo], issuer 1 lo x B_hi into N more; one set,
+//     flushed every 32 stages while the issuers pause (a second set would
+//     not leave room for two residual tiles).
+//   otherwise: one issuer, 3 products per k-step into N columns; two sets
+//     that alternate between groups of 8 stages.
 template <int N>
 struct Tmem {
-  static constexpr int NISS = N <= 64 ? 2 : 1;
+  static constexpr bool PSPLIT = N <= 64;
+  static constexpr int NISS = PSPLIT ? 2 : 1;
   static constexpr int ABUF = N <= 32 ? 2 : 1;
-  static constexpr int ACC = 2 * NISS * N;
+  static constexpr int ACCBUF = PSPLIT ? 1 : 2;
+  static constexpr int NPART = PSPLIT ? 3 : 1;   // N-wide parts of one set
+  static constexpr int ACCW = NPART * N;
+  static constexpr int QOFF = 2 * N;             // issuer 1's part of a set (PSPLIT)
+  static constexpr int GROUP = PSPLIT ? 32 : 8;
+  static constexpr int ACC = ACCBUF * ACCW;
   static constexpr int PD_MAX = (512 - ACC - ABUF * 2 * TV) / TV;
   static constexpr uint32_t A_COL = 0;
   static constexpr uint32_t P_COL = ABUF * 2 * TV;
@@ -344,7 +352,7 @@ struct Tmem {
 //   XR  [NS][data,0]  TF32 anchor k-step, row side: 128 rows x 4, then 128 x 4 zeros
 //   XC  [NS][data,0]  TF32 anchor k-step, column side: TV columns x 4, then zeros
 //   barriers: full[NS] empty[NS] afull[ABUF] segdone[2]
-//             tmemfree[2] pfull[PD] pfree[PD] rfull[2] rfree[2]
+//             tmemfree[2] pfull[PB] pfree[PB] rfull[2] rfree[2]
 // The residual-phase issuer runs up to PD stages ahead of the phase warps.
 template <int N, int KP, int NS>
 struct Smem {
@@ -361,7 +369,13 @@ struct Smem {
   static constexpr size_t XR_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
   static constexpr size_t XC_OFF = XR_OFF + (size_t)NS * 2 * XR_BYTES;
   static constexpr size_t BAR_OFF = (XC_OFF + (size_t)NS * 2 * XC_BYTES + 7) / 8 * 8;
-  static constexpr int NBAR = 2 * NS + ABUF + 8 + 2 * PD;
+  // pfull/pfree barriers: one per residual tile buffer, except that a single
+  // buffer gets two (by stage parity).  The two phase-warp groups take
+  // alternate stages, so no barrier is then shared by both groups: a group
+  // waiting for stage s on a barrier shared with stage s-1 could see the
+  // phase of stage s-2 and go ahead early.
+  static constexpr int PB = PD == 1 ? 2 : PD;
+  static constexpr int NBAR = 2 * NS + ABUF + 8 + 2 * PB;
   static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
@@ -377,7 +391,10 @@ constexpr int pick_stages() {
 template <int N, int KP, int NS, int MS>
 __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
   using S = Smem<N, KP, NS>;
-  constexpr int ABUF = S::ABUF, PD = S::PD, NISS = Tmem<N>::NISS;
+  constexpr int ABUF = S::ABUF, PD = S::PD, PB = S::PB, NISS = Tmem<N>::NISS;
+  constexpr int ACCBUF = Tmem<N>::ACCBUF, NPART = Tmem<N>::NPART, ACCW = Tmem<N>::ACCW;
+  constexpr int QOFF = Tmem<N>::QOFF, GROUP = Tmem<N>::GROUP;
+  constexpr bool PSPLIT = Tmem<N>::PSPLIT;
   static_assert(PD >= 1, "residual-phase look-ahead");
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -389,18 +406,18 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
   uint64_t *empty = full + NS;        // B-ring stage consumed by the contraction MMAs
   uint64_t *afull = empty + NS;       // [ABUF] TMEM phase tile written (16 phase warps)
-  uint64_t *segdone = afull + ABUF;   // [2] accumulator buffer complete (group of stages)
-  uint64_t *tmemfree = segdone + 2;   // [2] accumulator buffer read out
-  uint64_t *pfull = tmemfree + 2;     // [PD] residual-phase TMEM tile computed
-  uint64_t *pfree = pfull + PD;       // [PD] residual-phase TMEM tile read out
-  uint64_t *rfull = pfree + PD;       // [2] row residual tile loaded
+  uint64_t *segdone = afull + ABUF;   // [ACCBUF] accumulator set complete (group of stages)
+  uint64_t *tmemfree = segdone + 2;   // [ACCBUF] accumulator set read out
+  uint64_t *pfull = tmemfree + 2;     // [PB] residual-phase TMEM tile computed
+  uint64_t *pfree = pfull + PB;       // [PB] residual-phase TMEM tile read out
+  uint64_t *rfull = pfree + PB;       // [2] row residual tile loaded
   uint64_t *rfree = rfull + 2;        // [2] row residual tile no longer read by MMAs
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::MISC_OFF);
   volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
   constexpr uint32_t TMEM_COLS = 512;
   constexpr uint32_t A_COL = Tmem<N>::A_COL, P_COL = Tmem<N>::P_COL;
-  constexpr uint32_t ACC_COL = P_COL + PD * TV;   // group g, issuer q: ACC_COL + (g&1)*NISS*N + q*N
-  static_assert(ACC_COL + 2 * NISS * N <= TMEM_COLS, "tensor memory plan");
+  constexpr uint32_t ACC_COL = P_COL + PD * TV;   // group g, issuer q: ACC_COL + (g%ACCBUF)*ACCW + q*QOFF
+  static_assert(ACC_COL + ACCBUF * ACCW <= TMEM_COLS, "tensor memory plan");
   constexpr uint32_t SBO_TF32 = (KP / 4) * 128;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -424,7 +441,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       mbar_init(&rfull[i], 1);
       mbar_init(&rfree[i], 1);
     }
-    for (int i = 0; i < PD; ++i) {
+    for (int i = 0; i < PB; ++i) {
       mbar_init(&pfull[i], 1);
       mbar_init(&pfree[i], GROUP_WARPS);
     }
@@ -453,15 +470,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
 
   if (warp < PHASE_WARPS) {
     // ---------------- phase generator: one row x 32 columns of every other
-    // stage.  Two stages after a group of GROUP stages closes (or at the end),
-    // all 16 warps add its accumulator into register sums (columns split by
-    // warp >> 2) and, at the end of a row tile, write the sums to the partial slot.
+    // stage.  FLUSH_LAG stages after a group of GROUP stages closes (or at the
+    // end), all 16 warps add its accumulator set into register sums (columns
+    // split by warp >> 2) and, at the end of a row tile, write the sums to the
+    // partial slot.  With one set the issuers wait for this, so it comes right
+    // after the next stage's tile; with two it waits one stage more, so that
+    // the group's MMAs are normally done by then.
     const int row = (warp & 3) * 32 + lane;
     const int qcol = warp >> 2;          // accumulator quarter
     const int half = (warp >> 2) & 1;    // stage columns [half*32, half*32+32)
     const int par = warp >> 3;           // stages with it % 2 == par
     const uint32_t laneBase = (uint32_t)((warp & 3) * 32) << 16;
     constexpr int NA = N / 4;  // accumulator columns owned by this thread
+    constexpr int FLUSH_LAG = ACCBUF == 1 ? 1 : 2;
     float acc[NA];
 #pragma unroll
     for (int i = 0; i < NA; ++i) acc[i] = 0.f;
@@ -471,14 +492,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     bool ok = true;
     auto flush = [&]() {
       // add group pendGrp into acc; write acc out if it closed its row tile
-      const int g = pendGrp;
-      bool got = ok && wait_bar(&segdone[g & 1], (g >> 1) & 1, abort, p.err);
+      const int g = pendGrp, gb = g % ACCBUF, gr = g / ACCBUF;
+      bool got = ok && wait_bar(&segdone[gb], gr & 1, abort, p.err);
       tc_fence_after();
       if (got) {
 #pragma unroll
-        for (int q = 0; q < NISS; ++q) {
+        for (int q = 0; q < NPART; ++q) {
           const uint32_t base =
-              tmem + laneBase + ACC_COL + (uint32_t)((g & 1) * NISS * N + q * N + qcol * NA);
+              tmem + laneBase + ACC_COL + (uint32_t)(gb * ACCW + q * N + qcol * NA);
           if constexpr (NA % 16 == 0) {
 #pragma unroll
             for (int k0 = 0; k0 < NA; k0 += 16) {
@@ -503,7 +524,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&tmemfree[g & 1]);
+      if (lane == 0) mbar_arrive(&tmemfree[gb]);
       if (pendLast) {
         const TcSlice &ps = p.at(pendSI);
         const int slot = b - work_owner(ps.first + (int64_t)pendRT * ps.nColChunks, p.work, G);
@@ -523,16 +544,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     };
     // sincos of 16 phases (radians) -> BF16 hi/lo pairs.  The phase stays
     // within a few hundred radians, where the fast sincos keeps an absolute
-    // error near |phase| * 2^-24.
+    // error near |phase| * 2^-24.  A BF16 value is the upper half of the FP32
+    // with the same value, so the hi parts are unpacked with a shift and a mask.
     auto phase16 = [&](const float *d, uint32_t *hi, uint32_t *lo) {
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         float sn, cs;
         __sincosf(d[j], &sn, &cs);
-        __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);
-        float2 hf = __bfloat1622float2(h);
-        hi[j] = *reinterpret_cast<uint32_t *>(&h);
-        lo[j] = pack_bf16(cs - hf.x, sn - hf.y);
+        __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);  // .x (low half) = cos
+        const uint32_t hb = *reinterpret_cast<uint32_t *>(&h);
+        hi[j] = hb;
+        lo[j] = pack_bf16(cs - __uint_as_float(hb << 16), sn - __uint_as_float(hb & 0xffff0000u));
       }
     };
     Cursor<MS> c = c0;
@@ -541,8 +563,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       if (it == 0 || c.ch % GROUP == 0) ++grp;
       if ((it & 1) == par) {
         // phase of this stage in radians (TMEM), then release its buffer
-        const int pb = it % PD, pr = it / PD;
-        if (!wait_bar(&pfull[pb], pr & 1, abort, p.err)) { ok = false; break; }
+        const int pb = it % PD, pbar = it % PB, pr = it / PB;
+        if (!wait_bar(&pfull[pbar], pr & 1, abort, p.err)) { ok = false; break; }
         tc_fence_after();
         const uint32_t pBase = tmem + laneBase + P_COL + (uint32_t)(pb * TV + half * 32);
         const int ab = it % ABUF, ar = it / ABUF;
@@ -561,7 +583,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         tmem_ld16(pBase + 16, d);
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&pfree[pb]);
+        if (lane == 0) mbar_arrive(&pfree[pbar]);
         phase16(d, hi, lo);
         tmem_st16(aBase + 16, hi);
         tmem_st16(aBase + TV + 16, lo);
@@ -571,10 +593,10 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         if (lane == 0) mbar_arrive(&afull[ab]);
       }
       // a closed group is flushed two stages later, when its MMAs are done
-      if (pendGrp >= 0 && it >= pendIt + 2) flush();
+      if (pendGrp >= 0 && it >= pendIt + FLUSH_LAG) flush();
       const bool endRT = (it == nIter - 1) || (c.ch + 1 == c.C);
       if (endRT || (c.ch + 1) % GROUP == 0) {
-        if (pendGrp >= 0) flush();  // a short group closed within two stages of the previous one
+        if (pendGrp >= 0) flush();  // a short group closed within FLUSH_LAG stages of the previous one
         pendGrp = grp;
         pendRT = c.rt;
         pendSI = c.si;
@@ -584,8 +606,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     }
     if (pendGrp >= 0) flush();
   } else if (warp == CISS_WARP || warp == CISS_WARP + 1) {
-    // ---------------- contraction issuers: issuer q takes k-steps
-    // [q*KS, (q+1)*KS) of every stage into its own accumulator
+    // ---------------- contraction issuers: with PSPLIT issuer 0 takes
+    // hi x [B_hi | B_lo] and issuer 1 lo x B_hi over all k-steps, otherwise
+    // issuer q takes k-steps [q*KS, (q+1)*KS) with all 3 products
     const int q = warp - CISS_WARP;
     if (lane == 0 && q < NISS && nIter > 0) {
       constexpr int KS = (TK / 16) / NISS;
@@ -600,8 +623,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         const bool first = (it == 0) || (ch % GROUP == 0);
         if (first) {
           ++grp;
-          // accumulator buffer grp&1 was last used by group grp-2: wait until it was read out
-          if (grp >= 2 && !wait_bar(&tmemfree[grp & 1], ((grp >> 1) - 1) & 1, abort, p.err)) break;
+          // accumulator set grp%ACCBUF was last used by group grp-ACCBUF: wait until it was read out
+          if (grp >= ACCBUF &&
+              !wait_bar(&tmemfree[grp % ACCBUF], ((grp / ACCBUF) - 1) & 1, abort, p.err)) break;
         }
         const bool last = (it == nIter - 1) || (ch + 1 == c.C) || ((ch + 1) % GROUP == 0);
         const int slot = it % NS, round = it / NS;
@@ -609,24 +633,38 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
         if (!wait_bar(&afull[ab], ar & 1, abort, p.err)) break;
         tc_fence_after();
-        const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp & 1) * NISS * N + q * N);
+        const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp % ACCBUF) * ACCW + q * QOFF);
         const uint32_t aHi = tmem + A_COL + (uint32_t)(ab * 2 * TV);
         const uint32_t aLo = aHi + TV;
         const uint64_t bHi = umma_desc(smem_u32(sB + (size_t)slot * 2 * S::B_TILE));
         const uint64_t bLo = umma_desc(smem_u32(sB + (size_t)slot * 2 * S::B_TILE + S::B_TILE));
+        if constexpr (PSPLIT) {
+          // B_lo follows B_hi in shared memory as N more rows at the same
+          // stride, so [B_hi | B_lo] is one operand of width 2N
+          constexpr uint32_t idescW = idesc_bf16(TM, 2 * N);
+          const uint32_t aS = q == 0 ? aHi : aLo;
+          const uint32_t idS = q == 0 ? idescW : idescC;
 #pragma unroll
-        for (int kk = 0; kk < KS; ++kk) {
-          const int ks = q * KS + kk;
-          const uint32_t ka = ks * 8;                    // 16 BF16 = 8 TMEM columns
-          const uint64_t kb = (uint64_t)(ks * 2 * LBO) >> 4;  // two core matrices along K
-          umma_ta(dt, aHi + ka, bHi + kb, idescC, (first && kk == 0) ? 0u : 1u);
-          umma_ta(dt, aHi + ka, bLo + kb, idescC, 1u);
-          umma_ta(dt, aLo + ka, bHi + kb, idescC, 1u);
+          for (int ks = 0; ks < TK / 16; ++ks) {
+            const uint32_t ka = ks * 8;                          // 16 BF16 = 8 TMEM columns
+            const uint64_t kb = (uint64_t)(ks * 2 * LBO) >> 4;   // two core matrices along K
+            umma_ta(dt, aS + ka, bHi + kb, idS, (first && ks == 0) ? 0u : 1u);
+          }
+        } else {
+#pragma unroll
+          for (int kk = 0; kk < KS; ++kk) {
+            const int ks = q * KS + kk;
+            const uint32_t ka = ks * 8;
+            const uint64_t kb = (uint64_t)(ks * 2 * LBO) >> 4;
+            umma_ta(dt, aHi + ka, bHi + kb, idescC, (first && kk == 0) ? 0u : 1u);
+            umma_ta(dt, aHi + ka, bLo + kb, idescC, 1u);
+            umma_ta(dt, aLo + ka, bHi + kb, idescC, 1u);
+          }
         }
         umma_commit(&empty[slot]);
         lastBar = &empty[slot];
         lastPar = round & 1;
-        if (last) umma_commit(&segdone[grp & 1]);
+        if (last) umma_commit(&segdone[grp % ACCBUF]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);  // MMAs done before TMEM is freed
     }
@@ -649,8 +687,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         const int s = j % NS, r = j / NS;
         if (!wait_bar(&full[s], r & 1, abort, p.err)) break;
         if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
-        const int pb = j % PD, pr = j / PD;
-        if (j >= PD && !wait_bar(&pfree[pb], (pr - 1) & 1, abort, p.err)) break;
+        const int pb = j % PD, pbar = j % PB, pr = j / PB;
+        // tile buffer pb was last used by stage j - PD
+        if (j >= PD && !wait_bar(&pfree[(j - PD) % PB], ((j - PD) / PB) & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t dt = tmem + P_COL + (uint32_t)(pb * TV);
         const uint32_t rHi = smem_u32(sRV + (size_t)(kj & 1) * 2 * S::RV_TILE);
@@ -667,15 +706,15 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         // anchor k-step: [a_hi, a_lo, 1, 1 | 0] . [1, 1, c_hi, c_lo | 0] adds both anchors
         umma_tf32(dt, umma_desc(smem_u32(sXR + (size_t)s * 2 * S::XR_BYTES), 128, S::XR_BYTES),
                   umma_desc(smem_u32(sXC + (size_t)s * 2 * S::XC_BYTES), 128, S::XC_BYTES), idescP, 1u);
-        umma_commit(&pfull[pb]);
-        lastBar = &pfull[pb];
+        umma_commit(&pfull[pbar]);
+        lastBar = &pfull[pbar];
         lastPar = pr & 1;
         if (lastOfRow) umma_commit(&rfree[kj & 1]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);
     }
     __syncwarp();
-  } else {
+  } else if (warp == LOAD_WARP) {
     // ---------------- loader (one thread): row residual tiles per row tile,
     // per stage the B tiles, column residual tiles and column anchors
     if (lane == 0) {

@@ -173,6 +173,7 @@ SMALL = [
     dict(shape=(13, 11, 1), nSam=257, nCha=16, nTerm=16, conc=True),
     dict(shape=(17, 9, 2), nSam=200, nCha=1, nTerm=9),
     dict(shape=(12, 12, 1), nSam=131, nCha=33, nTerm=16),
+    dict(shape=(14, 13, 1), nSam=333, nCha=24, nTerm=16, conc=True),
     dict(shape=(16, 16, 1), nSam=640, nCha=8, nTerm=16, masked=False),
 ]
 
@@ -328,3 +329,21 @@ def test_default_engine_is_chosen_by_the_device():
     op.set_engine("auto")
     assert op.engine == ("tc" if have_tc() else "fp32")
     op.close()
+
+
+def test_tc_many_coils_long_pipeline():
+    # 40 coils use 64-coil MMA tiles; their shared-memory plan leaves a
+    # one-deep residual-phase ring, so both phase-warp groups hand the same
+    # tile buffer back and forth over ~8 stages per CTA in each direction
+    maybe_skip("tc")
+    w = workloads.small(seed=41, shape=(64, 48, 1), nSam=3000, nCha=40, nTerm=16)
+    a = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    b = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    x = dev(w.x)
+    assert dense.rel(host(a * x), host(b * x)) < TOL["tc"]
+    rng = np.random.default_rng(42)
+    y = dev(rng.standard_normal(a.nrow) + 1j * rng.standard_normal(a.nrow))
+    assert dense.rel(host(a.H * y), host(b.H * y)) < TOL["tc"]
+    a.check()
+    a.close()
+    b.close()
