@@ -174,6 +174,12 @@ SMALL = [
     dict(shape=(17, 9, 2), nSam=200, nCha=1, nTerm=9),
     dict(shape=(12, 12, 1), nSam=131, nCha=33, nTerm=16),
     dict(shape=(14, 13, 1), nSam=333, nCha=24, nTerm=16, conc=True),
+    # residual ranks 6 / 3 / 16 / 17: TF32 residual widths (tensor-core
+    # instances) 8, 8, 16 and 24
+    dict(shape=(9, 7, 1), nSam=300, nCha=3, nTerm=9),
+    dict(shape=(12, 1, 1), nSam=300, nCha=3, nTerm=9),
+    dict(shape=(6, 5, 4), nSam=300, nCha=3, nTerm=16),
+    dict(shape=(6, 5, 4), nSam=300, nCha=3, nTerm=16, conc=True),
     dict(shape=(16, 16, 1), nSam=640, nCha=8, nTerm=16, masked=False),
 ]
 
@@ -191,7 +197,8 @@ def run_small(engine, params, seed=11):
 
 
 @pytest.mark.parametrize("engine", ENGINE_PARAMS)
-@pytest.mark.parametrize("params", SMALL, ids=lambda p: "x".join(map(str, p["shape"])) + f"-{p['nSam']}s-{p['nCha']}c")
+@pytest.mark.parametrize("params", SMALL, ids=lambda p: "x".join(map(str, p["shape"])) + f"-{p['nSam']}s-{p['nCha']}c"
+                         + f"-{p['nTerm']}t" + ("-conc" if p.get("conc") else ""))
 def test_small_problems_vs_oracle(engine, params):
     maybe_skip(engine)
     op, m, mask, w, y0 = run_small(engine, params)
