@@ -94,6 +94,7 @@ void release_events(hoe_handle *h) {
 void release_device(hoe_handle *h) {
   release_events(h);
   hoe::cg_release(h);
+  hoe::tc_backward_release(h);
   hoe::tc_release(h);
   auto &t = h->t;
   dfree(t.dbeta); dfree(t.kappa); dfree(t.Atab); dfree(t.Btab); dfree(t.csm);
@@ -1100,9 +1101,14 @@ int hoe_backward(hoe_handle *h, const void *x, const void *r, float *dk, float *
   if ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) && !dt0) return fail(h, HOE_ERR_ARG, "dt0 must be given");
   DeviceGuard guard(h->device);
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
-  if (e == cudaSuccess)
-    e = hoe::simt_backward(h, (const float2 *)x, (const float2 *)r, dk, ddf, dt0, flags, st);
+  cudaError_t e = cudaSuccess;
+  if (h->engine == HOE_ENGINE_TC_BF16X3 && hoe::tc_backward_supported(h)) {
+    e = hoe::tc_backward(h, (const float2 *)x, (const float2 *)r, dk, ddf, dt0, flags, st);
+  } else {
+    e = hoe::prep_Z(h, (const float2 *)x, st);
+    if (e == cudaSuccess)
+      e = hoe::simt_backward(h, (const float2 *)x, (const float2 *)r, dk, ddf, dt0, flags, st);
+  }
   return finish(h, e, "hoe_backward");
 }
 

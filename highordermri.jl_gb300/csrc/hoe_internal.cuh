@@ -157,6 +157,7 @@ struct hoe_handle {
   hoe::Scratch s;
   hoe::TcState tc;
   void *tc_host = nullptr;   // tensor-core buffer table (hoe_tc.cu)
+  void *tcb_host = nullptr;  // tensor-core backward buffers (hoe_tc_bwd.cu), allocated on first use
   hoe::CgState cg;           // device-resident CGNR (hoe_cg.cu)
 };
 
@@ -257,6 +258,17 @@ enum { FWD_TO_Y = 0, FWD_TO_YT_WEIGHTED = 1, FWD_DERIV_TO_Y = 2 };
 // Tensor-core kernels (hoe_tc.cu).
 cudaError_t tc_prepare(hoe_handle *h);
 void tc_release(hoe_handle *h);
+// Backward pass on the tensor cores (hoe_tc_bwd.cu): up to 16 coils and a
+// residual width of at most 16; otherwise simt_backward.
+bool tc_backward_supported(const hoe_handle *h);
+cudaError_t tc_backward(hoe_handle *h, const float2 *x, const float2 *r, float *dk, float *ddf, double *dt0,
+                        int flags, cudaStream_t st);
+void tc_backward_release(hoe_handle *h);
+// The reductions after either backward kernel: dk from nSplit partial slots
+// [nSplit][nSamPad][kRF], dL/dfieldmap and the fieldmap part of dL/dt0 from
+// nRows partial rows [nRows][nVoxPad] of sum_s G and sum_s G t_s, and dL/dt0.
+cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const float *g1, const float *gt, int nRows,
+                       double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
 // Tensor-core applications; each builds its B operand straight from the
 // caller's vector (no Z / Yt staging): y = E x; x = E^H (D . y) (D may be
 // NULL); out = E^H diag(D) E x.

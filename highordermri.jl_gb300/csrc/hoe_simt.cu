@@ -588,25 +588,33 @@ cudaError_t simt_backward(const hoe_handle *hc, const float2 *, const float2 *r,
   if (t.nChaPad == 4) launch_bwd<4>(h, scaleG, st);
   else if (t.nChaPad == 8) launch_bwd<8>(h, scaleG, st);
   else launch_bwd<16>(h, scaleG, st);
-  h->launches += 2 + ((flags & HOE_GRAD_KSPHA) ? 1 : 0) +
-                 ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
+  h->launches += 1;
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   float *dkpart = h->s.gpart;
   float *g1 = dkpart + (size_t)h->splitF * t.nSamPad * kRF;
   float *gt = g1 + (size_t)t.nSt * t.nVoxPad;
+  return bwd_finish(h, dkpart, h->splitF, g1, gt, t.nSt, h->s.dred, dk, ddf, dt0, flags, st);
+}
+
+cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const float *g1, const float *gt, int nRows,
+                       double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st) {
+  const auto &t = h->t;
+  const int nVB = (t.nVoxPad + 255) / 256;
+  cudaError_t e = cudaSuccess;
+  h->launches += 1 + ((flags & HOE_GRAD_KSPHA) ? 1 : 0) + ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
   if (flags & HOE_GRAD_KSPHA) {
     int64_t n = (int64_t)t.nSam * t.R0;
-    k_bwd_dk<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dkpart, h->splitF, t.nSamPad, t.R0, t.nSam, dk);
+    k_bwd_dk<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dkpart, nSplit, t.nSamPad, t.R0, t.nSam, dk);
   }
   if (flags & HOE_GRAD_FIELDMAP) {
     e = cudaMemsetAsync(ddf, 0, (size_t)t.nFull * sizeof(float), st);
     if (e != cudaSuccess) return e;
   }
-  k_bwd_vox<<<nVB, 256, 0, st>>>(g1, gt, t.nSt, t.nVoxPad, t.perm, t.bfraw, t.R0,
-                                 (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr, h->s.dred);
+  k_bwd_vox<<<nVB, 256, 0, st>>>(g1, gt, nRows, t.nVoxPad, t.perm, t.bfraw, t.R0,
+                                 (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr, dred);
   if (flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF))
-    k_bwd_t0<<<1, 256, 0, st>>>(h->s.dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0, dkpart, h->splitF,
+    k_bwd_t0<<<1, 256, 0, st>>>(dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0, dkpart, nSplit,
                                 t.nSamPad, t.kdot, t.nSam, t.nTerm,
                                 (flags & HOE_GRAD_T0_COEF) ? 1 : 0, dt0);
   return cudaGetLastError();

@@ -1,0 +1,252 @@
+// hoe_tcgen05.cuh — tcgen05 building blocks shared by the tensor-core
+// kernels (hoe_tc.cu: forward/adjoint contraction, hoe_tc_bwd.cu: backward):
+// tile shapes, UMMA descriptors and no-swizzle K-major layouts, bounded
+// mbarrier waits, bulk copies, MMA and tensor-memory wrappers, the even split
+// of work items over CTAs and the engine's per-operator device buffers.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+
+#include "hoe_internal.cuh"
+
+namespace hoe {
+
+// Device buffers of the tensor-core engine for one operator (tc_prepare).
+struct TcBuffers {
+  uint16_t *bopF = nullptr, *bopA = nullptr;
+  float *AtabP = nullptr, *BtabQ = nullptr;   // anchors in radians, TF32 [hi, lo, 1, 1] / [1, 1, hi, lo]
+  float2 *part = nullptr;
+  int *err = nullptr;
+  int N = 0, nChaTC = 0;
+  int gridF = 1, gridA = 1, slotsF = 1, slotsA = 1;
+  size_t bopFElems = 0, bopAElems = 0, partElems = 0;
+};
+
+namespace {
+
+constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel tile)
+constexpr int TV = 64;              // complex columns per pipeline stage
+constexpr int TK = 2 * TV;          // real K per stage (128 BF16 = 8 UMMA k-steps)
+
+// Phase warps: two groups of 8 take alternate stages (group = warp >> 3), so
+// one group's barrier and tensor-memory latencies overlap the other's
+// arithmetic; within a group a warp covers one TMEM lane quarter (warp & 3)
+// and half of the stage's columns ((warp >> 2) & 1).
+constexpr int PHASE_WARPS = 16;
+constexpr int GROUP_WARPS = PHASE_WARPS / 2;
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
+
+// byte offset of element (r, k) in a no-swizzle K-major tile with K = TK:
+// core matrices of 8 rows x 16 B; cores adjacent in K are 128 B apart (LBO),
+// 8-row groups are (TK/8)*128 B apart (SBO)
+__host__ __device__ constexpr uint32_t kmajor_off(int r, int k) {
+  return (uint32_t)((r / 8) * (TK / 8) * 128 + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2);
+}
+constexpr uint32_t LBO = 128;                 // K-direction core stride (all tiles)
+constexpr uint32_t SBO = (TK / 8) * 128;      // 8-row group stride of the BF16 tiles
+
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  // D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12), K-major, N>>3 at 17, M>>4 at 24
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  // D = F32, A = B = TF32 (2 at bits 7-9, 10-12), K-major, N>>3 at 17, M>>4 at 24
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Shared-memory matrix descriptor, no swizzle: start address, LBO (K step of
+// core matrices), SBO (step of 8-row groups), descriptor version 1.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo = SBO, uint32_t lbo = LBO) {
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
+         ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// try_wait with a suspend-time hint: a waiting thread sleeps until the phase
+// completes (or the hint elapses) instead of spinning on issue slots.
+constexpr uint32_t kSuspendNs = 200000;
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false on timeout or when another role aborted.
+__device__ __noinline__ bool wait_bar_slow(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                           int *gerr) {
+  const uint64_t t0 = globaltimer();
+  for (;;) {
+    if (mbar_try_wait_sleep(bar, parity)) return true;
+    if (*abort) return false;
+    if (globaltimer() - t0 > kWaitNs) {
+      *abort = 1;
+      atomicExch(gerr, HOE_ERR_TIMEOUT);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                         int *gerr) {
+  if (mbar_try_wait(bar, parity)) return true;
+  return wait_bar_slow(bar, parity, abort, gerr);
+}
+
+// Bounded wait that ignores the abort flag (used to drain in-flight work).
+__device__ __noinline__ bool drain_bar(uint64_t *bar, uint32_t parity) {
+  uint64_t t0 = globaltimer();
+  while (!mbar_try_wait_sleep(bar, parity))
+    if (globaltimer() - t0 > kWaitNs) return false;
+  return true;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void umma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+// D += A(TMEM) * B(SMEM)^T, kind::f16
+__device__ __forceinline__ void umma_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(dtmem),
+      "r"(atmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t *w) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7]), "r"(w[8]),
+      "r"(w[9]), "r"(w[10]), "r"(w[11]), "r"(w[12]), "r"(w[13]), "r"(w[14]), "r"(w[15])
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                 "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x (low half) = lo_elem
+  return *reinterpret_cast<uint32_t *>(&v);
+}
+
+// CTA that owns work item w when W items are split into G contiguous ranges
+// [b*W/G, (b+1)*W/G).
+__host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
+  return (int)(((w + 1) * (int64_t)G - 1) / W);
+}
+
+// Largest number of CTAs that share one row tile when rowTiles*C work items
+// are split evenly over G CTAs.
+inline int max_slots(int rowTiles, int C, int G) {
+  const int64_t W = (int64_t)rowTiles * C;
+  int J = 1;
+  for (int r = 0; r < rowTiles; ++r) {
+    int b0 = work_owner((int64_t)r * C, W, G), b1 = work_owner((int64_t)(r + 1) * C - 1, W, G);
+    J = std::max(J, b1 - b0 + 1);
+  }
+  return J;
+}
+
+// D += A(SMEM) * B(SMEM)^T, kind::f16
+__device__ __forceinline__ void umma_ss(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                        uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+}  // namespace
+}  // namespace hoe
