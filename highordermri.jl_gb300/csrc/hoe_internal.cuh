@@ -268,7 +268,8 @@ void tc_backward_release(hoe_handle *h);
 // [nSplit][nSamPad][kRF], dL/dfieldmap and the fieldmap part of dL/dt0 from
 // nRows partial rows [nRows][nVoxPad] of sum_s G and sum_s G t_s, and dL/dt0.
 cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const float *g1, const float *gt, int nRows,
-                       double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
+                       double *vpart, double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
+constexpr int kBwdVoxSplit = 16;   // row ranges of the first voxel reduction pass (vpart: 2 x 16 x nVoxPad)
 // Tensor-core applications; each builds its B operand straight from the
 // caller's vector (no Z / Yt staging): y = E x; x = E^H (D . y) (D may be
 // NULL); out = E^H diag(D) E x.

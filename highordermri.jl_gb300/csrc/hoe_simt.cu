@@ -378,8 +378,26 @@ __global__ void k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamP
 }
 
 // Per voxel: dL/dfieldmap and the fieldmap part of dL/dt0 (block partials in FP64).
-__global__ void k_bwd_vox(const float *__restrict__ g1part, const float *__restrict__ gtpart,
-                          int nSt, int nVoxPad, const int *__restrict__ perm,
+// Sums of the partial rows [nRows][nVoxPad] per voxel in kBwdVoxSplit row
+// ranges (grid.y): vpart[0][split][p] (sum_s G), vpart[1][split][p] (sum_s G t).
+// A range holds a few dozen rows, summed in FP32 (GB300's FP64 add rate would
+// bound this pass); the ranges are added in FP64 by k_bwd_vox.
+__global__ void k_bwd_rows(const float *__restrict__ g1part, const float *__restrict__ gtpart, int nRows,
+                           int nVoxPad, double *__restrict__ vpart) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nVoxPad) return;
+  const int per = (nRows + kBwdVoxSplit - 1) / kBwdVoxSplit;
+  const int k0 = blockIdx.y * per, k1 = min(nRows, k0 + per);
+  float a1 = 0.f, at = 0.f;
+  for (int k = k0; k < k1; ++k) {
+    a1 += g1part[(int64_t)k * nVoxPad + p];
+    at += gtpart[(int64_t)k * nVoxPad + p];
+  }
+  vpart[(int64_t)blockIdx.y * nVoxPad + p] = (double)a1;
+  vpart[((int64_t)kBwdVoxSplit + blockIdx.y) * nVoxPad + p] = (double)at;
+}
+
+__global__ void k_bwd_vox(const double *__restrict__ vpart, int nVoxPad, const int *__restrict__ perm,
                           const float *__restrict__ bfraw, int R0, float *__restrict__ ddf,
                           double *__restrict__ blockAcc) {
   __shared__ double red[256];
@@ -387,9 +405,9 @@ __global__ void k_bwd_vox(const float *__restrict__ g1part, const float *__restr
   double contrib = 0.0;
   if (p < nVoxPad && perm[p] >= 0) {
     double g1 = 0.0, gt = 0.0;
-    for (int k = 0; k < nSt; ++k) {
-      g1 += g1part[(int64_t)k * nVoxPad + p];
-      gt += gtpart[(int64_t)k * nVoxPad + p];
+    for (int k = 0; k < kBwdVoxSplit; ++k) {
+      g1 += vpart[(int64_t)k * nVoxPad + p];
+      gt += vpart[((int64_t)kBwdVoxSplit + k) * nVoxPad + p];
     }
     if (ddf) ddf[perm[p]] = (float)gt;
     contrib = -(double)bfraw[(int64_t)p * kRF + R0] * g1;
@@ -568,8 +586,10 @@ cudaError_t simt_backward(const hoe_handle *hc, const float2 *, const float2 *r,
   hoe_handle *h = const_cast<hoe_handle *>(hc);
   const auto &t = h->t;
   if (t.nChaPad > 16) return cudaErrorNotSupported;
-  // scratch for the gradient partials, allocated on first use
-  size_t need = (size_t)h->splitF * t.nSamPad * kRF + 2 * (size_t)t.nSt * t.nVoxPad;
+  // scratch for the gradient partials, allocated on first use (the last
+  // 4 * kBwdVoxSplit * nVoxPad floats hold the FP64 voxel partial sums)
+  size_t need = (size_t)h->splitF * t.nSamPad * kRF + 2 * (size_t)t.nSt * t.nVoxPad +
+                4 * (size_t)kBwdVoxSplit * t.nVoxPad;
   int nVB = (t.nVoxPad + 255) / 256;
   if (h->s.gpartElems < need || !h->s.dred) {
     if (h->s.gpart) cudaFree(h->s.gpart);
@@ -594,15 +614,16 @@ cudaError_t simt_backward(const hoe_handle *hc, const float2 *, const float2 *r,
   float *dkpart = h->s.gpart;
   float *g1 = dkpart + (size_t)h->splitF * t.nSamPad * kRF;
   float *gt = g1 + (size_t)t.nSt * t.nVoxPad;
-  return bwd_finish(h, dkpart, h->splitF, g1, gt, t.nSt, h->s.dred, dk, ddf, dt0, flags, st);
+  double *vpart = reinterpret_cast<double *>(gt + (size_t)t.nSt * t.nVoxPad);
+  return bwd_finish(h, dkpart, h->splitF, g1, gt, t.nSt, vpart, h->s.dred, dk, ddf, dt0, flags, st);
 }
 
 cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const float *g1, const float *gt, int nRows,
-                       double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st) {
+                       double *vpart, double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st) {
   const auto &t = h->t;
   const int nVB = (t.nVoxPad + 255) / 256;
   cudaError_t e = cudaSuccess;
-  h->launches += 1 + ((flags & HOE_GRAD_KSPHA) ? 1 : 0) + ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
+  h->launches += 2 + ((flags & HOE_GRAD_KSPHA) ? 1 : 0) + ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
   if (flags & HOE_GRAD_KSPHA) {
     int64_t n = (int64_t)t.nSam * t.R0;
     k_bwd_dk<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dkpart, nSplit, t.nSamPad, t.R0, t.nSam, dk);
@@ -611,8 +632,9 @@ cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const flo
     e = cudaMemsetAsync(ddf, 0, (size_t)t.nFull * sizeof(float), st);
     if (e != cudaSuccess) return e;
   }
-  k_bwd_vox<<<nVB, 256, 0, st>>>(g1, gt, nRows, t.nVoxPad, t.perm, t.bfraw, t.R0,
-                                 (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr, dred);
+  k_bwd_rows<<<dim3(nVB, kBwdVoxSplit), 256, 0, st>>>(g1, gt, nRows, t.nVoxPad, vpart);
+  k_bwd_vox<<<nVB, 256, 0, st>>>(vpart, t.nVoxPad, t.perm, t.bfraw, t.R0, (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr,
+                                 dred);
   if (flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF))
     k_bwd_t0<<<1, 256, 0, st>>>(dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0, dkpart, nSplit,
                                 t.nSamPad, t.kdot, t.nSam, t.nTerm,

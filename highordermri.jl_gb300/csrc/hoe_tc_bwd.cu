@@ -23,6 +23,10 @@
 //   * the dk issuer contracts G with the basis tile: hi x [bf_hi | bf_lo] as
 //     one 64-wide MMA and lo x bf_hi, into one accumulator set that the phase
 //     warps add into FP32 registers every 32 stages.
+// The stage ring (Z tiles, residual column tiles, anchors) is released as
+// soon as the W and residual-phase MMAs have read it; the basis tiles, read
+// two or three stages later by the dk MMAs, have a ring of their own that the
+// dk issuer fills itself, NF - 1 stages ahead.
 // Every mbarrier wait is bounded as in hoe_tc.cu: on timeout the kernel sets
 // the engine's error word, stops, drains its own copies and MMAs and frees
 // tensor memory.
@@ -59,32 +63,35 @@ static_assert(BW_ACC_COL + 3 * BW_NF <= 512, "tensor memory plan");
 
 // Shared memory (dynamic, 1024-byte aligned base), KC = 2 * coils (BF16 K of
 // the W product), KP = residual width:
-//   stage ring [NS]: ZB [hi|lo] 128 x KC, FB [hi|lo] 32 x 64, CV [hi|lo] 64 x KP
-//                    (TF32), XR [data|0] 128 x 4, XC [data|0] 64 x 4
-//   row-tile ring [2]: RV [hi|lo] 128 x KP (TF32), RA [hi|lo] 128 x KC
+//   stage ring [NS]: ZB [hi|lo] 128 x KC, CV [hi|lo] 64 x KP (TF32),
+//                    XR [data|0] 128 x 4, XC [data|0] 64 x 4
+//   basis ring [NF]: FB [hi|lo] 32 x 64
+//   row-tile tables: RV [hi|lo] 128 x KP (TF32), RA [hi|lo] 128 x KC
 //   G tiles [2 parities]: [hi|lo] 128 x 64
+constexpr int BW_NFB = 4;
 template <int KC, int KP, int NS>
 struct BwSmem {
+  static constexpr int NF = BW_NFB;
   static constexpr int ZB = 128 * KC * 2, FB = BW_NF * TV * 2, CV = TV * KP * 4;
   static constexpr int XR = TM * 4 * 4, XC = TV * 4 * 4;
   static constexpr int RV = TM * KP * 4, RA = TM * KC * 2, GT = TM * TV * 2;
   static constexpr size_t ZB_OFF = 0;
-  static constexpr size_t FB_OFF = ZB_OFF + (size_t)NS * 2 * ZB;
-  static constexpr size_t CV_OFF = FB_OFF + (size_t)NS * 2 * FB;
+  static constexpr size_t CV_OFF = ZB_OFF + (size_t)NS * 2 * ZB;
   static constexpr size_t XR_OFF = CV_OFF + (size_t)NS * 2 * CV;
   static constexpr size_t XC_OFF = XR_OFF + (size_t)NS * 2 * XR;
-  static constexpr size_t RV_OFF = XC_OFF + (size_t)NS * 2 * XC;
-  static constexpr size_t RA_OFF = RV_OFF + (size_t)2 * 2 * RV;
-  static constexpr size_t G_OFF = RA_OFF + (size_t)2 * 2 * RA;
+  static constexpr size_t FB_OFF = XC_OFF + (size_t)NS * 2 * XC;
+  static constexpr size_t RV_OFF = FB_OFF + (size_t)NF * 2 * FB;
+  static constexpr size_t RA_OFF = RV_OFF + (size_t)2 * RV;
+  static constexpr size_t G_OFF = RA_OFF + (size_t)2 * RA;
   static constexpr size_t BAR_OFF = G_OFF + (size_t)2 * 2 * GT;
-  static constexpr int NBAR = 2 * NS + 18;
+  static constexpr int NBAR = 2 * NS + 2 * NF + 16;
   static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;
 };
 
 template <int KC, int KP>
 constexpr int bw_stages() {
-  return BwSmem<KC, KP, 3>::BYTES <= 227 * 1024 ? 3 : 2;
+  return BwSmem<KC, KP, 4>::BYTES <= 227 * 1024 ? 4 : BwSmem<KC, KP, 3>::BYTES <= 227 * 1024 ? 3 : 2;
 }
 
 struct BwParams {
@@ -122,11 +129,14 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
   using S = BwSmem<KC, KP, NS>;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int NF = S::NF;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
-  uint64_t *empty = full + NS;        // [NS] stage consumed (dk MMAs done, hence all of its MMAs)
-  uint64_t *rfull = empty + NS;       // [2] row-tile tables loaded
-  uint64_t *rfree = rfull + 2;        // [2] row-tile tables no longer read (residual and W issuers)
-  uint64_t *pfull = rfree + 2;        // [2] residual phase of the stage in TMEM
+  uint64_t *empty = full + NS;        // [NS] stage read by the W and residual-phase MMAs
+  uint64_t *ffull = empty + NS;       // [NF] basis tile loaded
+  uint64_t *fempty = ffull + NF;      // [NF] basis tile read by the dk MMAs
+  uint64_t *rfull = fempty + NF;      // [1] row-tile tables loaded
+  uint64_t *rfree = rfull + 1;        // [1] row-tile tables no longer read (residual and W issuers)
+  uint64_t *pfull = rfree + 1;        // [2] residual phase of the stage in TMEM
   uint64_t *pfree = pfull + 2;        // [2] ... read by the phase warps
   uint64_t *wfull = pfree + 2;        // [2] W of the stage in TMEM
   uint64_t *wfree = wfull + 2;        // [2] ... read by the phase warps
@@ -148,11 +158,15 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
   if (threadIdx.x == 0) {
     for (int i = 0; i < NS; ++i) {
       mbar_init(&full[i], 1);
-      mbar_init(&empty[i], 1);
+      mbar_init(&empty[i], 2);
     }
+    for (int i = 0; i < NF; ++i) {
+      mbar_init(&ffull[i], 1);
+      mbar_init(&fempty[i], 1);
+    }
+    mbar_init(&rfull[0], 1);
+    mbar_init(&rfree[0], 2);
     for (int i = 0; i < 2; ++i) {
-      mbar_init(&rfull[i], 1);
-      mbar_init(&rfree[i], 2);
       mbar_init(&pfull[i], 1);
       mbar_init(&pfree[i], GROUP_WARPS);
       mbar_init(&wfull[i], 1);
@@ -226,8 +240,10 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
       pendGrp = -1;
     };
     int rt = rt0, ch = ch0;
+    float ts = 0.f;   // sample time of this thread's row in the current row tile
     for (int it = 0; it < nIter && ok; ++it) {
       if (it > 0 && ++ch == p.nChunks) { ch = 0; ++rt; }
+      if (it == 0 || ch == 0) ts = p.times[(int64_t)rt * TM + row];
       if (it == 0 || ch % BW_GROUP == 0) ++grp;
       if ((it & 1) == par) {
         const int pb = it & 1, pr = (it >> 1) & 1;
@@ -237,15 +253,18 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         const uint32_t wBase = tmem + laneBase + BW_W_COL + (uint32_t)(pb * 2 * TV + half * 64);
         float g[32];
 #pragma unroll
-        for (int j0 = 0; j0 < 32; j0 += 8) {
-          float d[8], w[16];
-          tmem_ld8(pBase + j0, d);
-          tmem_ld16(wBase + 2 * j0, w);
+        for (int j0 = 0; j0 < 32; j0 += 16) {
+          // 16 voxels: their phases and (Re W, Im W), three loads and one wait
+          uint32_t d[16], w[32];
+          tmem_ld16_async(pBase + j0, d);
+          tmem_ld16_async(wBase + 2 * j0, w);
+          tmem_ld16_async(wBase + 2 * j0 + 16, w + 16);
+          tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
+          for (int j = 0; j < 16; ++j) {
             float sn, cs;
-            __sincosf(d[j], &sn, &cs);
-            g[j0 + j] = -p.scaleG * (cs * w[2 * j + 1] + sn * w[2 * j]);
+            __sincosf(__uint_as_float(d[j]), &sn, &cs);
+            g[j0 + j] = -p.scaleG * (cs * __uint_as_float(w[2 * j + 1]) + sn * __uint_as_float(w[2 * j]));
           }
         }
         tc_fence_before();
@@ -277,7 +296,6 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         __syncwarp();
         if (lane == 0) mbar_arrive(&gfull[pb]);
         // column sums of G and G*t over the tile's 128 rows
-        const float ts = p.times[(int64_t)rt * TM + row];
         float gt[32];
 #pragma unroll
         for (int j = 0; j < 32; ++j) gt[j] = g[j] * ts;
@@ -309,7 +327,7 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         if (it > 0 && ++ch == p.nChunks) ch = 0;
         if (it == 0 || ch == 0) {
           ++kj;
-          if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
+          if (!wait_bar(&rfull[0], kj & 1, abort, p.err)) break;
         }
         const bool lastOfRow = (it == nIter - 1) || (ch + 1 == p.nChunks);
         const int slot = it % NS, pb = it & 1;
@@ -317,7 +335,7 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         if (it >= 2 && !wait_bar(&wfree[pb], ((it >> 1) - 1) & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t dt = tmem + BW_W_COL + (uint32_t)(pb * 2 * TV);
-        const uint32_t aHi = smem_u32(smem + S::RA_OFF + (size_t)(kj & 1) * 2 * S::RA), aLo = aHi + S::RA;
+        const uint32_t aHi = smem_u32(smem + S::RA_OFF), aLo = aHi + S::RA;
         const uint32_t bHi = smem_u32(smem + S::ZB_OFF + (size_t)slot * 2 * S::ZB), bLo = bHi + S::ZB;
 #pragma unroll
         for (int ks = 0; ks < KC / 16; ++ks) {
@@ -327,9 +345,10 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
           umma_ss(dt, umma_desc(aLo + ko, SBO_KC), umma_desc(bHi + ko, SBO_KC), idescW, 1u);
         }
         umma_commit(&wfull[pb]);
+        umma_commit(&empty[slot]);
         lastBar = &wfull[pb];
         lastPar = (it >> 1) & 1;
-        if (lastOfRow) umma_commit(&rfree[kj & 1]);
+        if (lastOfRow) umma_commit(&rfree[0]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);
     }
@@ -345,7 +364,7 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         if (it > 0 && ++ch == p.nChunks) { ch = 0; ++rt; }
         if (it == 0 || ch == 0) {
           ++kj;
-          if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
+          if (!wait_bar(&rfull[0], kj & 1, abort, p.err)) break;
         }
         const bool lastOfRow = (it == nIter - 1) || (ch + 1 == p.nChunks);
         const int s = it % NS, pb = it & 1;
@@ -353,7 +372,7 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         if (it >= 2 && !wait_bar(&pfree[pb], ((it >> 1) - 1) & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t dt = tmem + BW_P_COL + (uint32_t)(pb * TV);
-        const uint32_t rHi = smem_u32(smem + S::RV_OFF + (size_t)(kj & 1) * 2 * S::RV), rLo = rHi + S::RV;
+        const uint32_t rHi = smem_u32(smem + S::RV_OFF), rLo = rHi + S::RV;
         const uint32_t cHi = smem_u32(smem + S::CV_OFF + (size_t)s * 2 * S::CV), cLo = cHi + S::CV;
 #pragma unroll
         for (int ks = 0; ks < KP / 8; ++ks) {
@@ -365,21 +384,36 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         umma_tf32(dt, umma_desc(smem_u32(smem + S::XR_OFF + (size_t)s * 2 * S::XR), 128, S::XR),
                   umma_desc(smem_u32(smem + S::XC_OFF + (size_t)s * 2 * S::XC), 128, S::XC), idescP, 1u);
         umma_commit(&pfull[pb]);
+        umma_commit(&empty[s]);
         lastBar = &pfull[pb];
         lastPar = (it >> 1) & 1;
-        if (lastOfRow) umma_commit(&rfree[kj & 1]);
+        if (lastOfRow) umma_commit(&rfree[0]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);
     }
     __syncwarp();
   } else if (warp == BW_KISS) {
-    // ---------------- dk issuer: D0 += G_hi x [bf_hi | bf_lo], D1 += G_lo x bf_hi
+    // ---------------- dk issuer: D0 += G_hi x [bf_hi | bf_lo], D1 += G_lo x bf_hi.
+    // It also loads the basis tiles, NF - 1 stages ahead of its own MMAs.
     if (lane == 0 && nIter > 0) {
       constexpr uint32_t idescW = idesc_bf16(TM, 2 * BW_NF), idescN = idesc_bf16(TM, BW_NF);
       uint64_t *lastBar = nullptr;
       uint32_t lastPar = 0;
+      int fIssued = 0, fch = ch0;   // basis tiles requested for stages [0, fIssued); chunk of stage fIssued
+      auto load_fb = [&]() -> bool {
+        // stage j into slot j % NF, last read by the dk MMAs of stage j - NF
+        const int j = fIssued, fs = j % NF;
+        if (j >= NF && !wait_bar(&fempty[fs], ((j - NF) / NF) & 1, abort, p.err)) return false;
+        mbar_expect_tx(&ffull[fs], 2 * S::FB);
+        bulk_g2s(smem + S::FB_OFF + (size_t)fs * 2 * S::FB, p.fb + (size_t)fch * 2 * BW_NF * TV, 2 * S::FB, &ffull[fs]);
+        ++fIssued;
+        if (++fch == p.nChunks) fch = 0;
+        return true;
+      };
+      bool ok = true;
+      while (ok && fIssued < NF - 1 && fIssued < nIter) ok = load_fb();
       int grp = -1, ch = ch0;
-      for (int it = 0; it < nIter; ++it) {
+      for (int it = 0; it < nIter && ok; ++it) {
         if (it > 0 && ++ch == p.nChunks) ch = 0;
         const bool first = (it == 0) || (ch % BW_GROUP == 0);
         if (first) {
@@ -388,12 +422,12 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
           if (grp >= 1 && !wait_bar(&tmemfree[0], (grp - 1) & 1, abort, p.err)) break;
         }
         const bool last = (it == nIter - 1) || (ch + 1 == p.nChunks) || ((ch + 1) % BW_GROUP == 0);
-        const int slot = it % NS, pb = it & 1;
-        if (!wait_bar(&full[slot], (it / NS) & 1, abort, p.err)) break;
+        const int fs = it % NF, pb = it & 1;
+        if (!wait_bar(&ffull[fs], (it / NF) & 1, abort, p.err)) break;
         if (!wait_bar(&gfull[pb], (it >> 1) & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t gHi = smem_u32(smem + S::G_OFF + (size_t)pb * 2 * S::GT), gLo = gHi + S::GT;
-        const uint32_t fHi = smem_u32(smem + S::FB_OFF + (size_t)slot * 2 * S::FB);
+        const uint32_t fHi = smem_u32(smem + S::FB_OFF + (size_t)fs * 2 * S::FB);
 #pragma unroll
         for (int ks = 0; ks < TV / 16; ++ks) {
           const uint32_t ko = ks * 2 * LBO;
@@ -403,38 +437,40 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
                   acc);
         }
         umma_commit(&gfree[pb]);
-        umma_commit(&empty[slot]);
-        lastBar = &empty[slot];
-        lastPar = (it / NS) & 1;
+        umma_commit(&fempty[fs]);
+        lastBar = &fempty[fs];
+        lastPar = (it / NF) & 1;
         if (last) umma_commit(&segdone[0]);
+        if (fIssued < nIter && !load_fb()) break;
       }
-      if (*abort && lastBar) drain_bar(lastBar, lastPar);
+      if (*abort) {
+        if (lastBar) drain_bar(lastBar, lastPar);   // MMAs done before TMEM is freed
+        for (int j = max(0, fIssued - NF); j < fIssued; ++j) drain_bar(&ffull[j % NF], (j / NF) & 1);
+      }
     }
     __syncwarp();
   } else if (warp == BW_LOAD) {
     // ---------------- loader: row-tile tables per row tile, stage operands per stage
     if (lane == 0) {
-      const uint32_t stageBytes = 2 * S::ZB + 2 * S::FB + 2 * S::CV + S::XR + S::XC;
+      const uint32_t stageBytes = 2 * S::ZB + 2 * S::CV + S::XR + S::XC;
       int issued = 0, kcount = -1, rowIssued = -1, rt = rt0, ch = ch0;
       for (int it = 0; it < nIter; ++it) {
         if (it > 0 && ++ch == p.nChunks) { ch = 0; ++rt; }
         if (it == 0 || ch == 0) {
+          // one buffer: the previous row tile's W and residual MMAs must be done
           ++kcount;
-          const int rb = kcount & 1;
-          if (kcount >= 2 && !wait_bar(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err)) break;
-          mbar_expect_tx(&rfull[rb], 2 * S::RV + 2 * S::RA);
+          if (kcount >= 1 && !wait_bar(&rfree[0], (kcount - 1) & 1, abort, p.err)) break;
+          mbar_expect_tx(&rfull[0], 2 * S::RV + 2 * S::RA);
           const size_t ro = (size_t)rt * TM * KP;
-          unsigned char *rv = smem + S::RV_OFF + (size_t)rb * 2 * S::RV;
-          bulk_g2s(rv, p.kpHi + ro, S::RV, &rfull[rb]);
-          bulk_g2s(rv + S::RV, p.kpLo + ro, S::RV, &rfull[rb]);
-          bulk_g2s(smem + S::RA_OFF + (size_t)rb * 2 * S::RA, p.ra + (size_t)rt * 2 * TM * KC, 2 * S::RA, &rfull[rb]);
+          bulk_g2s(smem + S::RV_OFF, p.kpHi + ro, S::RV, &rfull[0]);
+          bulk_g2s(smem + S::RV_OFF + S::RV, p.kpLo + ro, S::RV, &rfull[0]);
+          bulk_g2s(smem + S::RA_OFF, p.ra + (size_t)rt * 2 * TM * KC, 2 * S::RA, &rfull[0]);
           rowIssued = kcount;
         }
         const int slot = it % NS, round = it / NS;
         if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
         mbar_expect_tx(&full[slot], stageBytes);
         bulk_g2s(smem + S::ZB_OFF + (size_t)slot * 2 * S::ZB, p.zb + (size_t)ch * 2 * TM * KC, 2 * S::ZB, &full[slot]);
-        bulk_g2s(smem + S::FB_OFF + (size_t)slot * 2 * S::FB, p.fb + (size_t)ch * 2 * BW_NF * TV, 2 * S::FB, &full[slot]);
         const size_t co = (size_t)ch * TV * KP;
         unsigned char *cv = smem + S::CV_OFF + (size_t)slot * 2 * S::CV;
         bulk_g2s(cv, p.dbHi + co, S::CV, &full[slot]);
@@ -447,7 +483,7 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
       }
       if (*abort) {
         for (int it = max(0, issued - NS); it < issued; ++it) drain_bar(&full[it % NS], (it / NS) & 1);
-        if (rowIssued >= 0) drain_bar(&rfull[rowIssued & 1], (rowIssued >> 1) & 1);
+        if (rowIssued >= 0) drain_bar(&rfull[0], rowIssued & 1);
       }
     }
     __syncwarp();
@@ -520,7 +556,7 @@ __global__ void k_bw_fb(const float *__restrict__ bfraw, int nChunks, uint16_t *
 struct BwBuffers {
   uint16_t *ra = nullptr, *zb = nullptr, *fb = nullptr;
   float *dkpart = nullptr, *g1 = nullptr, *gt = nullptr;
-  double *dred = nullptr;
+  double *vpart = nullptr, *dred = nullptr;
   void *mem = nullptr;
   size_t bytes = 0;
   int KC = 0, grid = 0, slots = 0;
@@ -568,9 +604,9 @@ cudaError_t bw_prepare(hoe_handle *h) {
   const size_t raB = (size_t)t.nSamPad * b.KC * 2 * 2, zbB = (size_t)t.nVoxPad * 2 * b.KC * 2 * 2;
   const size_t fbB = (size_t)t.nVoxPad * BW_NF * 2 * 2;
   const size_t dkB = (size_t)b.slots * t.nSamPad * kRF * 4, gB = (size_t)t.nSt * 4 * t.nVoxPad * 4;
-  const size_t redB = (size_t)(nVB + 1) * 8;
+  const size_t redB = (size_t)(nVB + 1) * 8, vpB = (size_t)2 * kBwdVoxSplit * t.nVoxPad * 8;
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
-  b.bytes = al(raB) + al(zbB) + al(fbB) + al(dkB) + 2 * al(gB) + al(redB);
+  b.bytes = al(raB) + al(zbB) + al(fbB) + al(dkB) + 2 * al(gB) + al(vpB) + al(redB);
   cudaError_t e = cudaMalloc(&b.mem, b.bytes);
   if (e != cudaSuccess) return e;
   char *m = (char *)b.mem;
@@ -580,6 +616,7 @@ cudaError_t bw_prepare(hoe_handle *h) {
   b.dkpart = (float *)m; m += al(dkB);
   b.g1 = (float *)m; m += al(gB);
   b.gt = (float *)m; m += al(gB);
+  b.vpart = (double *)m; m += al(vpB);
   b.dred = (double *)m;
   const int64_t nF = (int64_t)nChunks * BW_NF * TV;
   k_bw_fb<<<(unsigned)((nF + 255) / 256), 256>>>(t.bfraw, nChunks, b.fb);
@@ -626,7 +663,7 @@ cudaError_t tc_backward(hoe_handle *h, const float2 *x, const float2 *r, float *
   e = bw_dispatch(b.KC, t.KP, p, b.grid, st);
   h->launches += 3;
   if (e != cudaSuccess) return e;
-  return bwd_finish(h, b.dkpart, b.slots, b.g1, b.gt, t.nSt * 4, b.dred, dk, ddf, dt0, flags, st);
+  return bwd_finish(h, b.dkpart, b.slots, b.g1, b.gt, t.nSt * 4, b.vpart, b.dred, dk, ddf, dt0, flags, st);
 }
 
 void tc_backward_release(hoe_handle *h) {
