@@ -150,11 +150,15 @@ def backward(m: Model, xm, r, kspha_dt=None):
     """Returns (dk (R, nSam), ddf (nVox,), dt0_b0, dt0_coef)."""
     xm, r = _c128(xm), _c128(r)
     kd = None if kspha_dt is None else np.asfortranarray(kspha_dt, dtype=np.float64)
+    # the coefficient part of dL/dt0 runs over the rows of kspha_dt (no concomitant rows)
+    nT = m.nTerm if kd is None else kd.shape[0]
+    if kd is not None and (kd.ndim != 2 or kd.shape[1] != m.nSam or nT > m.R):
+        raise ValueError(f"kspha_dt must be (nTerm <= {m.R}, {m.nSam}), got {kd.shape}")
     dk = np.zeros((m.R, m.nSam), order="F")
     ddf = np.zeros(m.nVox)
     parts = np.zeros(2)
     bf, k, t, f, c = m._args()
-    lib().oracle_backward(m.nVox, m.nSam, m.nCha, m.R, m.nTerm, bf, k, _p(kd), t, f, c,
+    lib().oracle_backward(m.nVox, m.nSam, m.nCha, m.R, nT, bf, k, _p(kd), t, f, c,
                           xm.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                           r.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                           _p(dk), _p(ddf), _p(parts))

@@ -254,13 +254,23 @@ def test_derivative_mode_vs_oracle():
 BWD_TOL = {"fp32": 1e-4, "tc": 1e-3}
 
 
+BWD_CASES = [
+    dict(shape=(10, 9, 1), nSam=300, nCha=4, nTerm=16),            # residual width 16, 4 coils
+    dict(shape=(11, 9, 1), nSam=300, nCha=8, nTerm=9),             # width 8, 8 coils
+    dict(shape=(9, 8, 1), nSam=280, nCha=12, nTerm=9),             # width 8, 12 coils
+    dict(shape=(7, 6, 3), nSam=260, nCha=6, nTerm=16, conc=True),  # width 24: FP32 kernel under "tc"
+]
+
+
 @pytest.mark.parametrize("engine", ENGINE_PARAMS)
-def test_backward_vs_oracle_and_fd(engine):
+@pytest.mark.parametrize("case", range(len(BWD_CASES)))
+def test_backward_vs_oracle_and_fd(engine, case):
     maybe_skip(engine)
-    w = workloads.small(seed=4, shape=(10, 9, 1), nSam=300, nCha=4, nTerm=16)
+    w = workloads.small(seed=4, **BWD_CASES[case])
     op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=w.kspha_dt, engine=engine, **w.op_kwargs())
     bf, k, t, f, c, idx = workloads.prepared_model(w)
-    m = oracle.Model(bf, k, t, f, c)
+    # kspha_dt has the nTerm rows of kspha (no concomitant rows)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
     rng = np.random.default_rng(9)
     y = oracle.forward(m, w.x[idx]) * 0.9 + 0.05 * (rng.standard_normal(w.nSam * w.nCha) + 1j * rng.standard_normal(w.nSam * w.nCha))
     r = oracle.forward(m, w.x[idx]) - y
