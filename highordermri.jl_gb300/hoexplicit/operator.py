@@ -66,7 +66,10 @@ class _Vec:
             if self.host is None:
                 self.host = "cpu"
                 self.pinned = bool(v.is_pinned())
-            v = v.to(device=op.torch_device, non_blocking=False)
+            # a page-locked source is copied on the current stream without a
+            # host wait: the call's kernels follow on the same stream, and the
+            # call waits for its result before returning
+            v = v.to(device=op.torch_device, non_blocking=self.pinned)
         elif v.device.index != op.device:
             raise ArgumentError(f"{name} is on cuda:{v.device.index}, operator on cuda:{op.device}")
         if v.dtype != torch.complex64:
