@@ -234,7 +234,7 @@ def check(rc: int, handle=None, batch=None) -> None:
         msg = load().hoe_batch_last_error(batch).decode(errors="replace")
     else:
         msg = load().hoe_last_error(handle).decode(errors="replace")
-    if rc in (HOE_ERR_ARG, HOE_ERR_CLOSED):
+    if rc in (HOE_ERR_ARG, HOE_ERR_CLOSED, HOE_ERR_UNSUPPORTED):
         raise ArgumentError(msg)
     if rc == HOE_ERR_DIM:
         raise DimensionMismatch(msg)

@@ -87,3 +87,7 @@ def test_error_mapping():
         _lib.check(_lib.HOE_ERR_DIM)
     with pytest.raises(_lib.OutOfMemoryError):
         _lib.check(_lib.HOE_ERR_OOM)
+    with pytest.raises(_lib.ArgumentError):
+        _lib.check(_lib.HOE_ERR_UNSUPPORTED)   # engine unavailable for this operator
+    with pytest.raises(_lib.HoeError):
+        _lib.check(_lib.HOE_ERR_TIMEOUT)

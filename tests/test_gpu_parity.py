@@ -376,6 +376,16 @@ def test_default_engine_is_chosen_by_the_device():
     op.set_engine("auto")
     assert op.engine == ("tc" if have_tc() else "fp32")
     op.close()
+    # more than 64 coils: the tensor-core engine is unavailable, AUTO takes FP32
+    w = workloads.small(seed=34, shape=(6, 5, 1), nSam=140, nCha=66, nTerm=9)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    assert op.engine == "fp32"
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    assert dense.rel(host(op * dev(w.x)), oracle.forward(m, w.x[idx])) < TOL["fp32"]
+    with pytest.raises(ArgumentError):
+        op.set_engine("tc")
+    op.close()
 
 
 def test_tc_many_coils_long_pipeline():
