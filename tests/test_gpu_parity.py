@@ -404,3 +404,24 @@ def test_tc_many_coils_long_pipeline():
     a.check()
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("n,nSam,nCha", [(160, 9000, 8), (160, 9000, 24), (96, 6000, 40)],
+                         ids=["8c-ring3", "24c-oneAbuf", "40c-twoAccSets"])
+def test_tc_long_pipelines_match_fp32_engine(n, nSam, nCha):
+    # each coil tile width has its own tensor-memory plan: 8 coils a three-deep
+    # residual ring; 24 coils one A buffer and the 2N-wide product; 40 coils one
+    # issuer, two alternating accumulator sets and a one-deep residual ring.
+    # 40-190 stages per CTA run through many accumulator groups.
+    maybe_skip("tc")
+    w = workloads.spiral_slice(17, n, nSam, nCha, d=200e-3 / n)
+    a = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    b = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    x = dev(w.x)
+    ya, yb = host(a * x), host(b * x)
+    assert dense.rel(ya, yb) < TOL["tc"]
+    y = dev(yb)
+    assert dense.rel(host(a.H * y), host(b.H * y)) < TOL["tc"]
+    a.check()
+    a.close()
+    b.close()
