@@ -337,7 +337,9 @@ class ExplicitGB300Op:
         Returns (dL/dkspha (nTermEff, nSam) float32 tensor, dL/dfieldmap
         (nFull,) float32 tensor zero outside the mask, dL/dt0 float64 tensor of
         one element); unrequested outputs are None.  ``t0_coef`` needs
-        ``kspha_dt`` or ``kdot`` at construction.
+        ``kspha_dt`` or ``kdot`` at construction.  The tensor-core engine forms
+        the gradient on the tensor cores for up to 16 coils and residual widths
+        up to 16 (``info()["residual_width"]``), otherwise the FP32 kernel does.
         """
         torch = _torch()
         xv = _Vec(self, x, self.ncol, "x")
