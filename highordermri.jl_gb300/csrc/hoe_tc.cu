@@ -413,7 +413,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     // hi x [B_hi | B_lo] and issuer 1 lo x B_hi over all k-steps, otherwise
     // issuer q takes k-steps [q*KS, (q+1)*KS) with all 3 products
     const int q = warp - CISS_WARP;
-    if (lane == 0 && q < NISS && nIter > 0) {
+    if (q < NISS && nIter > 0) {
+      // the whole warp walks the loop and waits; the elected lane issues
+      const bool leader = elect_one();
       constexpr int KS = (TK / 16) / NISS;
       constexpr uint32_t idescC = idesc_bf16(TM, N);
       uint64_t *lastBar = nullptr;
@@ -428,19 +430,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
           ++grp;
           // accumulator set grp%ACCBUF was last used by group grp-ACCBUF: wait until it was read out
           if (grp >= ACCBUF &&
-              !wait_bar(&tmemfree[grp % ACCBUF], ((grp / ACCBUF) - 1) & 1, abort, p.err)) break;
+              !wait_bar_warp(&tmemfree[grp % ACCBUF], ((grp / ACCBUF) - 1) & 1, abort, p.err)) break;
         }
         const bool last = (it == nIter - 1) || (ch + 1 == c.C) || ((ch + 1) % GROUP == 0);
         const int slot = it % NS, round = it / NS;
         const int ab = it % ABUF, ar = it / ABUF;
-        if (!wait_bar(&full[slot], round & 1, abort, p.err)) break;
-        if (!wait_bar(&afull[ab], ar & 1, abort, p.err)) break;
+        if (!wait_bar_warp(&full[slot], round & 1, abort, p.err)) break;
+        if (!wait_bar_warp(&afull[ab], ar & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp % ACCBUF) * ACCW + q * QOFF);
         const uint32_t aHi = tmem + A_COL + (uint32_t)(ab * 2 * TV);
         const uint32_t aLo = aHi + TV;
         const uint64_t bHi = umma_desc(smem_u32(sB + (size_t)slot * 2 * S::B_TILE));
         const uint64_t bLo = umma_desc(smem_u32(sB + (size_t)slot * 2 * S::B_TILE + S::B_TILE));
+        if (leader) {
         if constexpr (PSPLIT) {
           // B_lo follows B_hi in shared memory as N more rows at the same
           // stride, so [B_hi | B_lo] is one operand of width 2N
@@ -465,17 +468,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
           }
         }
         umma_commit(&empty[slot]);
+        if (last) umma_commit(&segdone[grp % ACCBUF]);
+        }
+        __syncwarp();
         lastBar = &empty[slot];
         lastPar = round & 1;
-        if (last) umma_commit(&segdone[grp % ACCBUF]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);  // MMAs done before TMEM is freed
     }
     __syncwarp();
   } else if (warp == PISS_WARP) {
     // ---------------- residual-phase issuer: TF32 tile of stage j, up to PD
-    // stages ahead of the phase warps
-    if (lane == 0 && nIter > 0) {
+    // stages ahead of the phase warps (whole warp, elected lane issues)
+    if (nIter > 0) {
+      const bool leader = elect_one();
       constexpr uint32_t idescP = idesc_tf32(TM, TV);
       uint64_t *lastBar = nullptr;
       uint32_t lastPar = 0;
@@ -488,39 +494,44 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         }
         const bool lastOfRow = (j == nIter - 1) || (c.ch + 1 == c.C);
         const int s = j % NS, r = j / NS;
-        if (!wait_bar(&full[s], r & 1, abort, p.err)) break;
-        if (!wait_bar(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
+        if (!wait_bar_warp(&full[s], r & 1, abort, p.err)) break;
+        if (!wait_bar_warp(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
         const int pb = j % PD, pbar = j % PB, pr = j / PB;
         // tile buffer pb was last used by stage j - PD
-        if (j >= PD && !wait_bar(&pfree[(j - PD) % PB], ((j - PD) / PB) & 1, abort, p.err)) break;
+        if (j >= PD && !wait_bar_warp(&pfree[(j - PD) % PB], ((j - PD) / PB) & 1, abort, p.err)) break;
         tc_fence_after();
         const uint32_t dt = tmem + P_COL + (uint32_t)(pb * TV);
         const uint32_t rHi = smem_u32(sRV + (size_t)(kj & 1) * 2 * S::RV_TILE);
         const uint32_t rLo = rHi + S::RV_TILE;
         const uint32_t cHi = smem_u32(sCV + (size_t)s * 2 * S::CV_TILE);
         const uint32_t cLo = cHi + S::CV_TILE;
+        if (leader) {
 #pragma unroll
-        for (int ks = 0; ks < KP / 8; ++ks) {
-          const uint32_t ko = ks * 2 * LBO;  // 8 TF32 = two core matrices along K
-          umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, ks ? 1u : 0u);
-          umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
-          umma_tf32(dt, umma_desc(rLo + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
+          for (int ks = 0; ks < KP / 8; ++ks) {
+            const uint32_t ko = ks * 2 * LBO;  // 8 TF32 = two core matrices along K
+            umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, ks ? 1u : 0u);
+            umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
+            umma_tf32(dt, umma_desc(rLo + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
+          }
+          // anchor k-step: [a_hi, a_lo, 1, 1 | 0] . [1, 1, c_hi, c_lo | 0] adds both anchors
+          umma_tf32(dt, umma_desc(smem_u32(sXR + (size_t)s * 2 * S::XR_BYTES), 128, S::XR_BYTES),
+                    umma_desc(smem_u32(sXC + (size_t)s * 2 * S::XC_BYTES), 128, S::XC_BYTES), idescP, 1u);
+          umma_commit(&pfull[pbar]);
+          if (lastOfRow) umma_commit(&rfree[kj & 1]);
         }
-        // anchor k-step: [a_hi, a_lo, 1, 1 | 0] . [1, 1, c_hi, c_lo | 0] adds both anchors
-        umma_tf32(dt, umma_desc(smem_u32(sXR + (size_t)s * 2 * S::XR_BYTES), 128, S::XR_BYTES),
-                  umma_desc(smem_u32(sXC + (size_t)s * 2 * S::XC_BYTES), 128, S::XC_BYTES), idescP, 1u);
-        umma_commit(&pfull[pbar]);
+        __syncwarp();
         lastBar = &pfull[pbar];
         lastPar = pr & 1;
-        if (lastOfRow) umma_commit(&rfree[kj & 1]);
       }
       if (*abort && lastBar) drain_bar(lastBar, lastPar);
     }
     __syncwarp();
   } else if (warp == LOAD_WARP) {
-    // ---------------- loader (one thread): row residual tiles per row tile,
-    // per stage the B tiles, column residual tiles and column anchors
-    if (lane == 0) {
+    // ---------------- loader: row residual tiles per row tile, per stage the
+    // B tiles, column residual tiles and column anchors (whole warp, elected
+    // lane issues the copies)
+    {
+      const bool leader = elect_one();
       const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + S::XR_BYTES + S::XC_BYTES;
       int issued = 0, kcount = -1, rowIssued = -1;
       Cursor<MS> c = c0;
@@ -531,24 +542,30 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         if (it == 0 || ch == 0) {
           ++kcount;
           const int rb = kcount & 1;
-          if (kcount >= 2 && !wait_bar(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err)) break;
-          mbar_expect_tx(&rfull[rb], 2 * S::RV_TILE);
-          const size_t ro = (size_t)rt * TM * KP;
-          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE, sl.rowHi + ro, S::RV_TILE, &rfull[rb]);
-          bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE + S::RV_TILE, sl.rowLo + ro, S::RV_TILE, &rfull[rb]);
+          if (kcount >= 2 && !wait_bar_warp(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err)) break;
+          if (leader) {
+            mbar_expect_tx(&rfull[rb], 2 * S::RV_TILE);
+            const size_t ro = (size_t)rt * TM * KP;
+            bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE, sl.rowHi + ro, S::RV_TILE, &rfull[rb]);
+            bulk_g2s(sRV + (size_t)rb * 2 * S::RV_TILE + S::RV_TILE, sl.rowLo + ro, S::RV_TILE, &rfull[rb]);
+          }
+          __syncwarp();
           rowIssued = kcount;
         }
         const int slot = it % NS, round = it / NS;
-        if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
-        const size_t co = (size_t)ch * TV * KP;
-        mbar_expect_tx(&full[slot], stageBytes);
-        bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, sl.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
-        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, sl.colHi + co, S::CV_TILE, &full[slot]);
-        bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, sl.colLo + co, S::CV_TILE, &full[slot]);
-        bulk_g2s(sXR + (size_t)slot * 2 * S::XR_BYTES,
-                 sl.rowX + ((int64_t)(ch * TV / 128) * sl.rowXStride + (int64_t)rt * TM) * 4, S::XR_BYTES, &full[slot]);
-        bulk_g2s(sXC + (size_t)slot * 2 * S::XC_BYTES,
-                 sl.colX + ((int64_t)rt * sl.colXStride + (int64_t)ch * TV) * 4, S::XC_BYTES, &full[slot]);
+        if (round > 0 && !wait_bar_warp(&empty[slot], (round - 1) & 1, abort, p.err)) break;
+        if (leader) {
+          const size_t co = (size_t)ch * TV * KP;
+          mbar_expect_tx(&full[slot], stageBytes);
+          bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, sl.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
+          bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, sl.colHi + co, S::CV_TILE, &full[slot]);
+          bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, sl.colLo + co, S::CV_TILE, &full[slot]);
+          bulk_g2s(sXR + (size_t)slot * 2 * S::XR_BYTES,
+                   sl.rowX + ((int64_t)(ch * TV / 128) * sl.rowXStride + (int64_t)rt * TM) * 4, S::XR_BYTES, &full[slot]);
+          bulk_g2s(sXC + (size_t)slot * 2 * S::XC_BYTES,
+                   sl.colX + ((int64_t)rt * sl.colXStride + (int64_t)ch * TV) * 4, S::XC_BYTES, &full[slot]);
+        }
+        __syncwarp();
         issued = it + 1;
       }
       if (*abort) {

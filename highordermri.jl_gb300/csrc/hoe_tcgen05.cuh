@@ -121,6 +121,24 @@ __device__ __forceinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatil
   return wait_bar_slow(bar, parity, abort, gerr);
 }
 
+// Bounded wait made by every lane of a converged warp; the result is the same
+// in all lanes (any lane's failure counts), so the warp stays converged.
+__device__ __forceinline__ bool wait_bar_warp(uint64_t *bar, uint32_t parity, volatile int *abort, int *gerr) {
+  return __all_sync(0xffffffffu, wait_bar(bar, parity, abort, gerr));
+}
+
+// One lane of a converged warp (elect.sync).  MMA issuers run their loop with
+// the whole warp and let the elected lane issue: issuing back to back from a
+// lone active lane costs ~83 cycles per tcgen05.mma, from an elected lane of
+// a converged warp ~32 (measured on GB300).
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred = 0;
+  asm volatile(
+      "{\n .reg .pred p;\n .reg .b32 r;\n elect.sync r|p, 0xffffffff;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(pred));
+  return pred != 0;
+}
+
 // Bounded wait that ignores the abort flag (used to drain in-flight work).
 __device__ __noinline__ bool drain_bar(uint64_t *bar, uint32_t parity) {
   uint64_t t0 = globaltimer();
