@@ -160,7 +160,14 @@ struct Tmem {
 template <int N, int KP, int NS>
 struct Smem {
   static constexpr int ABUF = Tmem<N>::ABUF;
-  static constexpr int PD = (NS - 1) < Tmem<N>::PD_MAX ? (NS - 1) : (Tmem<N>::PD_MAX < 3 ? Tmem<N>::PD_MAX : 3);
+  // Residual widths up to 16: the row tile's TF32 residual vectors (hi, lo)
+  // also sit in tensor memory, 2*KP columns after the accumulators, as the A
+  // operand of the residual MMAs (written by phase warps 0-3 once per row
+  // tile), so that those MMAs read only the column tile from shared memory.
+  static constexpr bool RT = KP <= 16;
+  static constexpr int R_COLS = RT ? 2 * KP : 0;
+  static constexpr int PD_CAP = (512 - Tmem<N>::ACC - ABUF * 2 * TV - R_COLS) / TV;
+  static constexpr int PD = (NS - 1) < PD_CAP ? (NS - 1) : (PD_CAP < 3 ? PD_CAP : 3);
   static constexpr int B_TILE = N * TK * 2;
   static constexpr int CV_TILE = TV * KP * 4;
   static constexpr int RV_TILE = TM * KP * 4;
@@ -178,7 +185,7 @@ struct Smem {
   // waiting for stage s on a barrier shared with stage s-1 could see the
   // phase of stage s-2 and go ahead early.
   static constexpr int PB = PD == 1 ? 2 : PD;
-  static constexpr int NBAR = 2 * NS + ABUF + 8 + 2 * PB;
+  static constexpr int NBAR = 2 * NS + ABUF + 10 + 2 * PB;
   static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
@@ -215,12 +222,16 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   uint64_t *pfree = pfull + PB;       // [PB] residual-phase TMEM tile read out
   uint64_t *rfull = pfree + PB;       // [2] row residual tile loaded
   uint64_t *rfree = rfull + 2;        // [2] row residual tile no longer read by MMAs
+  uint64_t *rtfull = rfree + 2;       // [1] row residual vectors written to TMEM (4 warps)
+  uint64_t *rtfree = rtfull + 1;      // [1] ... no longer read by the residual MMAs
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::MISC_OFF);
   volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
   constexpr uint32_t TMEM_COLS = 512;
   constexpr uint32_t A_COL = Tmem<N>::A_COL, P_COL = Tmem<N>::P_COL;
   constexpr uint32_t ACC_COL = P_COL + PD * TV;   // group g, issuer q: ACC_COL + (g%ACCBUF)*ACCW + q*QOFF
-  static_assert(ACC_COL + ACCBUF * ACCW <= TMEM_COLS, "tensor memory plan");
+  constexpr bool RT = S::RT;
+  constexpr uint32_t R_COL = ACC_COL + ACCBUF * ACCW;   // [hi KP | lo KP] when RT
+  static_assert(R_COL + S::R_COLS <= TMEM_COLS, "tensor memory plan");
   constexpr uint32_t SBO_TF32 = (KP / 4) * 128;
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -248,6 +259,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       mbar_init(&pfull[i], 1);
       mbar_init(&pfree[i], GROUP_WARPS);
     }
+    mbar_init(&rtfull[0], 4);
+    mbar_init(&rtfree[0], 1);
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -361,8 +374,42 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       }
     };
     Cursor<MS> c = c0;
+    int kt = -1;   // row tiles whose residual vectors warps 0-3 wrote to TMEM
     for (int it = 0; it < nIter && ok; ++it) {
       if (it > 0) c.next(p);
+      if constexpr (RT) {
+        if (warp < 4 && (it == 0 || c.ch == 0)) {
+          // the new row tile's residual vectors, hi and lo, from the shared
+          // tile into TMEM once the previous row tile's residual MMAs are done
+          ++kt;
+          if ((kt > 0 && !wait_bar_warp(&rtfree[0], (kt - 1) & 1, abort, p.err)) ||
+              !wait_bar_warp(&rfull[kt & 1], (kt >> 1) & 1, abort, p.err)) { ok = false; break; }
+          tc_fence_after();
+          const float4 *rv = reinterpret_cast<const float4 *>(sRV + (size_t)(kt & 1) * 2 * S::RV_TILE);
+          uint32_t hv[KP], lv[KP];
+#pragma unroll
+          for (int kc = 0; kc < KP / 4; ++kc) {
+            const int o = ((row / 8) * (KP / 4) + kc) * 8 + (row % 8);   // float4 index
+            const float4 h = rv[o], l = rv[S::RV_TILE / 16 + o];
+            hv[4 * kc] = __float_as_uint(h.x); hv[4 * kc + 1] = __float_as_uint(h.y);
+            hv[4 * kc + 2] = __float_as_uint(h.z); hv[4 * kc + 3] = __float_as_uint(h.w);
+            lv[4 * kc] = __float_as_uint(l.x); lv[4 * kc + 1] = __float_as_uint(l.y);
+            lv[4 * kc + 2] = __float_as_uint(l.z); lv[4 * kc + 3] = __float_as_uint(l.w);
+          }
+          const uint32_t rbase = tmem + laneBase + R_COL;
+          if constexpr (KP == 16) {
+            tmem_st16(rbase, hv);
+            tmem_st16(rbase + KP, lv);
+          } else {
+            tmem_st8(rbase, hv);
+            tmem_st8(rbase + KP, lv);
+          }
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&rtfull[0]);
+        }
+      }
       if (it == 0 || c.ch % GROUP == 0) ++grp;
       if ((it & 1) == par) {
         // phase of this stage in radians (TMEM), then release its buffer
@@ -496,6 +543,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         const int s = j % NS, r = j / NS;
         if (!wait_bar_warp(&full[s], r & 1, abort, p.err)) break;
         if (!wait_bar_warp(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
+        if (RT && (j == 0 || c.ch == 0) && !wait_bar_warp(&rtfull[0], kj & 1, abort, p.err)) break;
         const int pb = j % PD, pbar = j % PB, pr = j / PB;
         // tile buffer pb was last used by stage j - PD
         if (j >= PD && !wait_bar_warp(&pfree[(j - PD) % PB], ((j - PD) / PB) & 1, abort, p.err)) break;
@@ -509,15 +557,26 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
 #pragma unroll
           for (int ks = 0; ks < KP / 8; ++ks) {
             const uint32_t ko = ks * 2 * LBO;  // 8 TF32 = two core matrices along K
-            umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, ks ? 1u : 0u);
-            umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
-            umma_tf32(dt, umma_desc(rLo + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
+            if constexpr (RT) {
+              // A from TMEM: 8 TF32 columns per k-step, hi at R_COL, lo KP further
+              const uint32_t ra = tmem + R_COL + (uint32_t)(ks * 8);
+              umma_ta_tf32(dt, ra, umma_desc(cHi + ko, SBO_TF32), idescP, ks ? 1u : 0u);
+              umma_ta_tf32(dt, ra, umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
+              umma_ta_tf32(dt, ra + KP, umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
+            } else {
+              umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, ks ? 1u : 0u);
+              umma_tf32(dt, umma_desc(rHi + ko, SBO_TF32), umma_desc(cLo + ko, SBO_TF32), idescP, 1u);
+              umma_tf32(dt, umma_desc(rLo + ko, SBO_TF32), umma_desc(cHi + ko, SBO_TF32), idescP, 1u);
+            }
           }
           // anchor k-step: [a_hi, a_lo, 1, 1 | 0] . [1, 1, c_hi, c_lo | 0] adds both anchors
           umma_tf32(dt, umma_desc(smem_u32(sXR + (size_t)s * 2 * S::XR_BYTES), 128, S::XR_BYTES),
                     umma_desc(smem_u32(sXC + (size_t)s * 2 * S::XC_BYTES), 128, S::XC_BYTES), idescP, 1u);
           umma_commit(&pfull[pbar]);
-          if (lastOfRow) umma_commit(&rfree[kj & 1]);
+          if (lastOfRow) {
+            umma_commit(&rfree[kj & 1]);
+            if (RT) umma_commit(&rtfree[0]);
+          }
         }
         __syncwarp();
         lastBar = &pfull[pbar];

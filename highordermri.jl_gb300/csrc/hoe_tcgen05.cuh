@@ -267,6 +267,20 @@ inline int max_slots(int rowTiles, int C, int G) {
   return J;
 }
 
+// D += A(TMEM) * B(SMEM)^T, kind::tf32 (one TF32 element per TMEM column)
+__device__ __forceinline__ void umma_ta_tf32(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                             uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n" ::"r"(dtmem),
+      "r"(atmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t *w) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(w[0]),
+               "r"(w[1]), "r"(w[2]), "r"(w[3]), "r"(w[4]), "r"(w[5]), "r"(w[6]), "r"(w[7])
+               : "memory");
+}
+
 // D += A(SMEM) * B(SMEM)^T, kind::f16
 __device__ __forceinline__ void umma_ss(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                         uint32_t accumulate) {
