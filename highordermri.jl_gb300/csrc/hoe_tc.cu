@@ -360,17 +360,14 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     };
     // sincos of 16 phases (radians) -> BF16 hi/lo pairs.  The phase stays
     // within a few hundred radians, where the fast sincos keeps an absolute
-    // error near |phase| * 2^-24.  A BF16 value is the upper half of the FP32
-    // with the same value, so the hi parts are unpacked with a shift and a mask.
+    // error near |phase| * 2^-24.  Each (cos, sin) pair becomes one BF16 hi
+    // word and one BF16 lo word (low half = cos).
     auto phase16 = [&](const float *d, uint32_t *hi, uint32_t *lo) {
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         float sn, cs;
         __sincosf(d[j], &sn, &cs);
-        __nv_bfloat162 h = __floats2bfloat162_rn(cs, sn);  // .x (low half) = cos
-        const uint32_t hb = *reinterpret_cast<uint32_t *>(&h);
-        hi[j] = hb;
-        lo[j] = pack_bf16(cs - __uint_as_float(hb << 16), sn - __uint_as_float(hb & 0xffff0000u));
+        split_bf16x2(cs, sn, hi[j], lo[j]);
       }
     };
     Cursor<MS> c = c0;

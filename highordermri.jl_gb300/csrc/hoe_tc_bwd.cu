@@ -281,13 +281,8 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         for (int c8 = 0; c8 < 4; ++c8) {
           uint32_t hw[4], lw[4];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const float a0 = g[c8 * 8 + 2 * i], a1 = g[c8 * 8 + 2 * i + 1];
-            __nv_bfloat162 h = __floats2bfloat162_rn(a0, a1);
-            const uint32_t hb = *reinterpret_cast<uint32_t *>(&h);
-            hw[i] = hb;
-            lw[i] = pack_bf16(a0 - __uint_as_float(hb << 16), a1 - __uint_as_float(hb & 0xffff0000u));
-          }
+          for (int i = 0; i < 4; ++i)
+            split_bf16x2(g[c8 * 8 + 2 * i], g[c8 * 8 + 2 * i + 1], hw[i], lw[i]);
           const uint32_t off = kmaj(row, half * 32 + c8 * 8, TV);
           *reinterpret_cast<uint4 *>(gHi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
           *reinterpret_cast<uint4 *>(gHi + S::GT + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);

@@ -249,6 +249,23 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem) {
   return *reinterpret_cast<uint32_t *>(&v);
 }
 
+// Two FP32 values -> BF16 hi pair (round to nearest) and BF16 lo pair of the
+// residuals (a - hi(a), b - hi(b)).  A BF16 value is the upper half of the FP32
+// with the same value, so the hi parts are unpacked with a shift and a mask;
+// both residuals come from one packed FP32x2 subtraction.
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t &hi, uint32_t &lo) {
+  __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // .x (low half) = a
+  const uint32_t hb = *reinterpret_cast<uint32_t *>(&h);
+  uint64_t v, u, d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(a), "f"(b));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(u) : "r"(hb << 16), "r"(hb & 0xffff0000u));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(v), "l"(u));
+  float ra, rb;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(ra), "=f"(rb) : "l"(d));
+  hi = hb;
+  lo = pack_bf16(ra, rb);
+}
+
 // CTA that owns work item w when W items are split into G contiguous ranges
 // [b*W/G, (b+1)*W/G).
 __host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
