@@ -19,7 +19,7 @@
 // stages ahead: the residual dbeta.kappa (TF32, 3 products of hi/lo splits
 // made at create time, K = reduced rank) plus one more k-step that adds the
 // row and column anchors (see hoe_internal.cuh) as [a_hi, a_lo, 1, 1] .
-// [1, 1, c_hi, c_lo].  16 "phase" warps read it, take the FP32 sincos, split the result
+// [1, 1, c_hi, c_lo].  12 or 16 "phase" warps read it, take the FP32 sincos, split the result
 // into BF16 hi/lo and write both into a TMEM A tile with tcgen05.st (lane =
 // row, one 32-bit column = one (re, im) pair).  A loader warp streams the
 // pre-tiled B operand, the TF32 residual tiles and the anchors with
@@ -44,16 +44,30 @@
 namespace hoe {
 namespace {
 
-// Warp roles: 16 phase warps, two contraction issuers, one residual-phase
+// Warp roles: PW phase warps, two contraction issuers, one residual-phase
 // issuer (TF32 MMAs) that also owns the TMEM allocation, and one loader.
-// The MMA instruction count bounds a stage: a thread issuing tcgen05.mma
-// back to back waits 80-200 cycles per instruction almost whatever N is, so
-// the contraction uses as few, wide MMAs as tensor memory allows and splits
-// them over two threads.
-constexpr int CISS_WARP = PHASE_WARPS;        // contraction issuers: warps 16, 17
-constexpr int PISS_WARP = PHASE_WARPS + 2;    // residual-phase issuer, TMEM owner
-constexpr int LOAD_WARP = PHASE_WARPS + 3;
-constexpr int THREADS = (PHASE_WARPS + 4) * 32;
+// Phase warps form NG groups of GW that take the stages in turn (group
+// it % NG), so one group's barrier and tensor-memory latencies overlap the
+// others' arithmetic; warp w covers TMEM lane quarter w & 3.
+//   N <= 32: 3 groups of 4 (12 warps, 16 in all, 128 registers a thread); a
+//     warp covers all 64 columns of its stages.  The role warps then share an
+//     SM sub-partition with 3 phase warps instead of 4, which shortens the
+//     residual-phase issuer's loop, the chain that sets the stage time.
+//   N >= 64: 2 groups of 8 (16 warps, 20 in all, 96 registers, which the
+//     wider accumulators need); a warp covers half of the columns.
+template <int N>
+struct Warps {
+  static constexpr int NG = N <= 32 ? 3 : 2;
+  static constexpr int GW = N <= 32 ? 4 : 8;
+  static constexpr int PW = NG * GW;
+  static constexpr bool WIDE = GW == 4;
+  // warps that read out the accumulators: 2 or 4 per lane quarter
+  static constexpr int FLW = NG == 3 ? 8 : PW;
+  static constexpr int CISS = PW;        // contraction issuers: PW, PW + 1
+  static constexpr int PISS = PW + 2;    // residual-phase issuer, TMEM owner
+  static constexpr int LOAD = PW + 3;
+  static constexpr int THREADS = (PW + 4) * 32;
+};
 
 // A tensor-core FP32 accumulator sums at most GROUP stages (Tmem<N>::GROUP,
 // at most 256 MMAs per accumulator) before it is added, in round-to-nearest
@@ -179,12 +193,16 @@ struct Smem {
   static constexpr size_t XR_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
   static constexpr size_t XC_OFF = XR_OFF + (size_t)NS * 2 * XR_BYTES;
   static constexpr size_t BAR_OFF = (XC_OFF + (size_t)NS * 2 * XC_BYTES + 7) / 8 * 8;
-  // pfull/pfree barriers: one per residual tile buffer, except that a single
-  // buffer gets two (by stage parity).  The two phase-warp groups take
-  // alternate stages, so no barrier is then shared by both groups: a group
-  // waiting for stage s on a barrier shared with stage s-1 could see the
-  // phase of stage s-2 and go ahead early.
-  static constexpr int PB = PD == 1 ? 2 : PD;
+  // pfull/pfree barriers: stage s uses barrier s % PB.  A parity wait for s
+  // on a barrier whose previous phase (stage s - PB) were still open would
+  // see the phase before that and go ahead early.  With PB >= NG that cannot
+  // happen: the waiting group has already seen stage s - NG >= s - PB done,
+  // and the residual tiles complete in stage order.  With PB >= PD the
+  // residual issuer has seen all arrivals for stage s before it writes stage
+  // s + PD, so the arrivals for s and s + PB never mix.
+  static constexpr int NG = Warps<N>::NG;
+  static constexpr int PB = PD > NG ? PD : NG;
+  static_assert(PB >= NG && PB >= PD, "residual-tile barriers");
   static constexpr int NBAR = 2 * NS + ABUF + 10 + 2 * PB;
   static constexpr size_t MISC_OFF = BAR_OFF + (size_t)NBAR * 8;
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
@@ -199,12 +217,15 @@ constexpr int pick_stages() {
 }
 
 template <int N, int KP, int NS, int MS>
-__global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
+__global__ void __launch_bounds__(Warps<N>::THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
   using S = Smem<N, KP, NS>;
   constexpr int ABUF = S::ABUF, PD = S::PD, PB = S::PB, NISS = Tmem<N>::NISS;
   constexpr int ACCBUF = Tmem<N>::ACCBUF, NPART = Tmem<N>::NPART, ACCW = Tmem<N>::ACCW;
   constexpr int QOFF = Tmem<N>::QOFF, GROUP = Tmem<N>::GROUP;
   constexpr bool PSPLIT = Tmem<N>::PSPLIT;
+  using W = Warps<N>;
+  constexpr int NG = W::NG, GW = W::GW, PW = W::PW, FLW = W::FLW;
+  constexpr int CISS_WARP = W::CISS, PISS_WARP = W::PISS, LOAD_WARP = W::LOAD;
   static_assert(PD >= 1, "residual-phase look-ahead");
   extern __shared__ unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -215,7 +236,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   unsigned char *sXC = smem + S::XC_OFF;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
   uint64_t *empty = full + NS;        // B-ring stage consumed by the contraction MMAs
-  uint64_t *afull = empty + NS;       // [ABUF] TMEM phase tile written (16 phase warps)
+  uint64_t *afull = empty + NS;       // [ABUF] TMEM phase tile written (one phase-warp group)
   uint64_t *segdone = afull + ABUF;   // [ACCBUF] accumulator set complete (group of stages)
   uint64_t *tmemfree = segdone + 2;   // [ACCBUF] accumulator set read out
   uint64_t *pfull = tmemfree + 2;     // [PB] residual-phase TMEM tile computed
@@ -247,17 +268,17 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
       mbar_init(&empty[i], NISS);
     }
     for (int i = 0; i < ABUF; ++i) {
-      mbar_init(&afull[i], GROUP_WARPS);
+      mbar_init(&afull[i], GW);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&segdone[i], NISS);
-      mbar_init(&tmemfree[i], PHASE_WARPS);
+      mbar_init(&tmemfree[i], FLW);
       mbar_init(&rfull[i], 1);
       mbar_init(&rfree[i], 1);
     }
     for (int i = 0; i < PB; ++i) {
       mbar_init(&pfull[i], 1);
-      mbar_init(&pfree[i], GROUP_WARPS);
+      mbar_init(&pfree[i], GW);
     }
     mbar_init(&rtfull[0], 4);
     mbar_init(&rtfree[0], 1);
@@ -265,7 +286,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // the second core-matrix column of every anchor k-step operand is zero
-  for (int i = threadIdx.x; i < NS * (S::XR_BYTES + S::XC_BYTES) / 16; i += THREADS) {
+  for (int i = threadIdx.x; i < NS * (S::XR_BYTES + S::XC_BYTES) / 16; i += W::THREADS) {
     const int nr = NS * S::XR_BYTES / 16;
     float4 *dst = i < nr
         ? reinterpret_cast<float4 *>(sXR + (size_t)(i / (S::XR_BYTES / 16)) * 2 * S::XR_BYTES + S::XR_BYTES) + i % (S::XR_BYTES / 16)
@@ -284,20 +305,20 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp < PHASE_WARPS) {
-    // ---------------- phase generator: one row x 32 columns of every other
-    // stage.  FLUSH_LAG stages after a group of GROUP stages closes (or at the
-    // end), all 16 warps add its accumulator set into register sums (columns
-    // split by warp >> 2) and, at the end of a row tile, write the sums to the
-    // partial slot.  With one set the issuers wait for this, so it comes right
-    // after the next stage's tile; with two it waits one stage more, so that
-    // the group's MMAs are normally done by then.
+  if (warp < PW) {
+    // ---------------- phase generator: one row x 64 (N <= 32) or 32 columns
+    // of every NG-th stage.  FLUSH_LAG stages after a group of GROUP stages
+    // closes (or at the end), the first FLW warps add its accumulator set into
+    // register sums (columns split by warp >> 2) and, at the end of a row
+    // tile, write the sums to the partial slot.  With one set the issuers wait
+    // for this, so it comes right after the next stage's tile; with two it
+    // waits one stage more, so that the group's MMAs are normally done by then.
     const int row = (warp & 3) * 32 + lane;
-    const int qcol = warp >> 2;          // accumulator quarter
-    const int half = (warp >> 2) & 1;    // stage columns [half*32, half*32+32)
-    const int par = warp >> 3;           // stages with it % 2 == par
+    const int qcol = warp >> 2;          // accumulator part (FLW / 4 of them)
+    const int half = W::WIDE ? 0 : (warp >> 2) & 1;   // stage columns [half*32, half*32+32) when not WIDE
+    const int par = warp / GW;           // stages with it % NG == par
     const uint32_t laneBase = (uint32_t)((warp & 3) * 32) << 16;
-    constexpr int NA = N / 4;  // accumulator columns owned by this thread
+    constexpr int NA = N / (FLW / 4);  // accumulator columns owned by this thread
     constexpr int FLUSH_LAG = ACCBUF == 1 ? 1 : 2;
     float acc[NA];
 #pragma unroll
@@ -308,6 +329,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
     bool ok = true;
     auto flush = [&]() {
       // add group pendGrp into acc; write acc out if it closed its row tile
+      if (warp >= FLW) { pendGrp = -1; return; }
       const int g = pendGrp, gb = g % ACCBUF, gr = g / ACCBUF;
       bool got = ok && wait_bar(&segdone[gb], gr & 1, abort, p.err);
       tc_fence_after();
@@ -408,7 +430,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         }
       }
       if (it == 0 || c.ch % GROUP == 0) ++grp;
-      if ((it & 1) == par) {
+      if (it % NG == par) {
         // phase of this stage in radians (TMEM), then release its buffer
         const int pb = it % PD, pbar = it % PB, pr = it / PB;
         if (!wait_bar(&pfull[pbar], pr & 1, abort, p.err)) { ok = false; break; }
@@ -416,24 +438,37 @@ __global__ void __launch_bounds__(THREADS, 1) k_tc_contract(const __grid_constan
         const uint32_t pBase = tmem + laneBase + P_COL + (uint32_t)(pb * TV + half * 32);
         const int ab = it % ABUF, ar = it / ABUF;
         const uint32_t aBase = tmem + laneBase + A_COL + (uint32_t)(ab * 2 * TV + half * 32);
+        // H blocks of 32 columns, 16 at a time; the residual tile is released
+        // once its last 16 columns are in registers
+        constexpr int H = W::WIDE ? 2 : 1;
         float d[16];
         uint32_t hi[16], lo[16];
-        tmem_ld16(pBase, d);
-        phase16(d, hi, lo);
-        // TMEM phase tile buffer: free once the contraction of stage it-ABUF is
-        // done, which the stage's `empty` barrier records (the slot of stage
-        // it-ABUF cannot have been reused: that needs this stage's tile)
-        if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err)) { ok = false; break; }
-        tc_fence_after();
-        tmem_st16(aBase, hi);
-        tmem_st16(aBase + TV, lo);
-        tmem_ld16(pBase + 16, d);
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&pfree[pbar]);
-        phase16(d, hi, lo);
-        tmem_st16(aBase + 16, hi);
-        tmem_st16(aBase + TV + 16, lo);
+#pragma unroll
+        for (int h = 0; h < H; ++h) {
+          const uint32_t ph = pBase + (uint32_t)(h * 32), ah = aBase + (uint32_t)(h * 32);
+          tmem_ld16(ph, d);
+          phase16(d, hi, lo);
+          if (h == 0) {
+            // TMEM phase tile buffer: free once the contraction of stage
+            // it-ABUF is done, which the stage's `empty` barrier records (the
+            // slot of stage it-ABUF cannot have been reused: that needs this
+            // stage's tile)
+            if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err)) { ok = false; break; }
+            tc_fence_after();
+          }
+          tmem_st16(ah, hi);
+          tmem_st16(ah + TV, lo);
+          tmem_ld16(ph + 16, d);
+          if (h == H - 1) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&pfree[pbar]);
+          }
+          phase16(d, hi, lo);
+          tmem_st16(ah + 16, hi);
+          tmem_st16(ah + TV + 16, lo);
+        }
+        if (!ok) break;
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         tc_fence_before();
         __syncwarp();
@@ -802,7 +837,7 @@ template <int N, int KP, int MS>
 cudaError_t launch_contract(const hoe_handle *h, const TcParams<MS> &p, int G, cudaStream_t st) {
   using K = Kern<N, KP>;
   auto kern = k_tc_contract<N, KP, K::NS, MS>;
-  kern<<<G, THREADS, K::S::BYTES, st>>>(p);
+  kern<<<G, Warps<N>::THREADS, K::S::BYTES, st>>>(p);
   h->launches += 1;
   return cudaGetLastError();
 }
@@ -816,7 +851,7 @@ int configure() {
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES) != cudaSuccess)
     return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, THREADS, K::S::BYTES) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, Warps<N>::THREADS, K::S::BYTES) != cudaSuccess) return 0;
   return nb;
 }
 
