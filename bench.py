@@ -46,17 +46,21 @@ L2_FLUSH_BYTES = 256 << 20
 # the 200x200 / 12,000-sample / 16-coil workload (profiles/tc_engine_cfg2.md,
 # profiles/simt_engine_cfg2.md).  Other workloads report None.
 NCU_TRAFFIC_BYTES = {
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "forward"): 138_283_008 + 4_270_080,
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "adjoint"): 138_283_008 + 4_270_080,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "forward"): 138_284_032 + 4_328_448,
+    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "adjoint"): 138_284_032 + 4_328_448,
     ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "forward"): 40_267_776 + 25_856,
     ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "adjoint"): 36_679_424 + 11_776,
 }
 # Warp instructions issued by one tensor-core contraction launch at the
 # 200x200 spiral workload (ncu smsp__inst_executed.sum, same capture).
-NCU_TC_WARP_INST = {"cfg2-vdspiral-200x200-12000s-16c-16t+conc": 248_053_836}
-# Cycles a thread waits per tcgen05.mma issued back to back (kind::f16,
-# M = 128, N <= 128, A from TMEM), measured in isolation on this GPU.
-MMA_ISSUE_CYCLES = 83.0
+NCU_TC_WARP_INST = {"cfg2-vdspiral-200x200-12000s-16c-16t+conc": 201_034_673}
+# Cycles a converged warp's elected lane waits per tcgen05.mma issued back to
+# back (kind::f16, M = 128, N = 64, A from TMEM), measured in isolation on
+# this GPU (N = 32: 32 cycles).
+MMA_ISSUE_CYCLES = 40.0
+# Tensor-pipe cycles per SM of one M = 128 MMA: BF16 K = 16 and TF32 K = 8
+# both run at N / 2 cycles for N >= 32 (4,096 BF16 MACs per clock per SM),
+# from the same isolated probe and the ncu op counts of the capture above.
 
 
 def parse_args():
@@ -538,29 +542,38 @@ def run_gb300(a):
         hz = sm_mhz * 1e6
         nsm = torch.cuda.get_device_properties(dev).multi_processor_count
         stages = -(-info["n_sample_tiles"] * info["n_voxel_tiles"] * 2 // nsm)   # 64-column stages per CTA
-        mma_per_thread = 8 if w.nCha <= 32 else 24                              # per stage, busiest issuer
-        t_mma = stages * mma_per_thread * MMA_ISSUE_CYCLES / hz
+        nc = 2 * max(8, 1 << (w.nCha - 1).bit_length())   # N: coils padded to 8/16/32/64, re/im
+        rk = info["residual_rank"]
+        kp = 8 if rk <= 8 else (16 if rk <= 16 else 24)     # residual k-width
+        if nc <= 64:   # hi x [B_hi | B_lo] (2N wide) and lo x B_hi, 8 k-steps each
+            mma_contract, mma_busiest, pipe_contract = 16, 8, 8 * (2 * nc // 2) + 8 * max(16, nc // 2)
+        else:          # 3 products of width N per k-step
+            mma_contract, mma_busiest, pipe_contract = 24, 24, 24 * nc // 2
+        mma_resid = 3 * (kp // 8) + 1
+        pipe_cycles = pipe_contract + mma_resid * 32
+        t_mma = stages * mma_busiest * MMA_ISSUE_CYCLES / hz
+        t_pipe = stages * pipe_cycles / hz
         t_sfu = 2.0 * w.nVox * w.nSam / (16.0 * nsm * hz)
         inst = NCU_TC_WARP_INST.get(w.name)
         t_issue = inst / (4.0 * nsm * hz) if inst else None
-        t_tensor = flops_per_launch * 3.0 / (bf16_peak * 1e12)
         dom_s = dom_ms / 1e3
         roofline["ceilings"] = [
-            {"pipe": "tcgen05.mma issue", "ms": t_mma * 1e3, "frac": t_mma / dom_s,
-             "note": f"{mma_per_thread} MMAs per 64-column stage from the busiest of 3 issuing threads, "
-                     f"{MMA_ISSUE_CYCLES:.0f} cycles each (isolated issue cost), {stages} stages per SM"},
+            {"pipe": "sfu (MUFU sin/cos)", "ms": t_sfu * 1e3, "frac": t_sfu / dom_s,
+             "note": "2 MUFU ops per (voxel, sample), 16 per clock per SM"},
             {"pipe": "warp instruction issue", "ms": t_issue * 1e3 if t_issue else None,
              "frac": t_issue / dom_s if t_issue else None,
              "note": "ncu warp instructions of one launch / (4 per clock per SM)"},
-            {"pipe": "sfu (MUFU sin/cos)", "ms": t_sfu * 1e3, "frac": t_sfu / dom_s,
-             "note": "2 MUFU ops per element, 16 per clock per SM; not binding: the kernel "
-                     "with sin/cos removed runs in the same time"},
-            {"pipe": "tensor (3 BF16 products)", "ms": t_tensor * 1e3, "frac": t_tensor / dom_s,
-             "note": "measured dense BF16 peak / 3"},
+            {"pipe": "tensor pipe (all MMAs)", "ms": t_pipe * 1e3, "frac": t_pipe / dom_s,
+             "note": f"{pipe_cycles} cycles per 64-column stage: contraction (3 BF16 products, "
+                     f"{mma_contract} MMAs) + {mma_resid} TF32 residual-phase MMAs, {stages} stages per SM"},
+            {"pipe": "tcgen05.mma issue", "ms": t_mma * 1e3, "frac": t_mma / dom_s,
+             "note": f"{mma_busiest} MMAs per stage on the busiest issuer x {MMA_ISSUE_CYCLES:.0f} cycles "
+                     "(converged warp, elected lane, isolated)"},
         ]
-        roofline["binding"] = {"pipe": "tcgen05.mma issue", "frac": t_mma / dom_s,
-                               "note": "24 -> 16 contraction MMAs per stage cut the kernel time 14%; "
-                                       "removing sin/cos or 10% of the instructions changed it by < 2%"}
+        roofline["binding"] = {"pipe": "phase generator (sfu + issue, latency-bound)", "frac": t_sfu / dom_s,
+                               "note": "timing variants: sin/cos removed or the lo split removed each cut the "
+                                       "kernel 11%; with the phase work removed it runs at 0.23 ms, and the "
+                                       "residual-phase MMA count then matters, not before"}
     if engine == "fp32":
         sm_mhz = clk.summary().get("sm_mhz") or 1900.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
