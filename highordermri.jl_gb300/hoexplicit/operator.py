@@ -13,7 +13,10 @@ Reference surface mirrored (paths inside HighOrderMRI.jl):
 Solver vectors are torch CUDA complex64 tensors on the operator's device
 (the counterpart of ``CuVector{ComplexF32}``, storage_type at
 explicit_gpu_operator.jl:115).  numpy arrays are also accepted: they are
-copied to the device and the result is copied back (host round trip).
+copied to the device and the result is copied back (host round trip).  The
+in-place products ``prod_``/``ctprod_`` (the reference's ``mul!``) also take
+host tensors: with page-locked memory they queue the copies and kernels on
+the current stream and return without waiting.
 """
 from __future__ import annotations
 
@@ -239,6 +242,7 @@ class ExplicitGB300Op:
         self.engine = _ENGINE_NAMES[self.info()["engine"]]
         self.nprod = self.ntprod = self.nctprod = 0
         self.tprod = None
+        self._stage = {}   # device buffers for host operands of prod_/ctprod_, per (stream, role)
 
     # ------------------------------------------------------------------ misc
     def _handle(self):
@@ -296,19 +300,55 @@ class ExplicitGB300Op:
         return self._h is None or bool(_lib.load().hoe_is_closed(self._h))
 
     # ------------------------------------------------------------ products
-    def prod_(self, out, x):
-        """In-place forward: out = E x (or B x in the kspha_dt mode)."""
-        fn = _lib.load().hoe_derivative if self.derivative_mode else _lib.load().hoe_forward
-        _lib.check(fn(self._handle(), x.data_ptr(), out.data_ptr(), self._stream()), self._h)
-        self.nprod += 1
+    def _io(self, t, n, name, role):
+        """Device view of an in-place product operand.  A CUDA tensor is used
+        as is; a host tensor goes through a device buffer that the operator
+        keeps per (stream, role), reused in stream order.  Returns (device
+        tensor, host tensor to copy the result into or None, pinned)."""
+        torch = _torch()
+        if not isinstance(t, torch.Tensor) or t.dtype != torch.complex64 or not t.is_contiguous():
+            raise ArgumentError(f"{name} must be a contiguous complex64 torch tensor")
+        if t.numel() != n:
+            raise DimensionMismatch(f"{name} has length {t.numel()}, expected {n}")
+        if t.device.type == "cuda":
+            if t.device.index != self.device:
+                raise ArgumentError(f"{name} is on cuda:{t.device.index}, operator on cuda:{self.device}")
+            return t, None, False
+        key = (self._stream(), role)
+        buf = self._stage.get(key)
+        if buf is None or buf.numel() != n:
+            buf = torch.empty(n, dtype=torch.complex64, device=self.torch_device)
+            self._stage[key] = buf
+        return buf, t, bool(t.is_pinned())
+
+    def _product(self, fn, out, v, nout, nin, counter):
+        """Queue out = op(v) on the current stream.  Host operands are copied
+        in and out around the kernels; with page-locked host memory nothing
+        waits, so `out` holds the result once the stream has been synchronised
+        (as with torch's non_blocking copies).  Other host memory is copied
+        synchronously."""
+        dv, hv, pv = self._io(v, nin, "input", 0)
+        dout, hout, pout = self._io(out, nout, "out", 1)
+        if hv is not None:
+            dv.copy_(hv, non_blocking=pv)
+        _lib.check(fn(self._handle(), dv.data_ptr(), dout.data_ptr(), self._stream()), self._h)
+        if hout is not None:
+            hout.copy_(dout, non_blocking=pout)
+        setattr(self, counter, getattr(self, counter) + 1)
         return out
 
+    def prod_(self, out, x):
+        """In-place forward: out = E x (or B x in the kspha_dt mode), the
+        reference's mul!(out, op, x).  CUDA or host tensors (complex64,
+        contiguous); queued on the current stream."""
+        fn = _lib.load().hoe_derivative if self.derivative_mode else _lib.load().hoe_forward
+        return self._product(fn, out, x, self.nrow, self.ncol, "nprod")
+
     def ctprod_(self, out, y):
-        """In-place adjoint: out = E^H y (zeros outside the mask)."""
-        _lib.check(_lib.load().hoe_adjoint(self._handle(), y.data_ptr(), out.data_ptr(),
-                                           self._stream()), self._h)
-        self.nctprod += 1
-        return out
+        """In-place adjoint: out = E^H y (zeros outside the mask), the
+        reference's mul!(out, adjoint(op), y).  CUDA or host tensors
+        (complex64, contiguous); queued on the current stream."""
+        return self._product(_lib.load().hoe_adjoint, out, y, self.ncol, self.nrow, "nctprod")
 
     def forward(self, x):
         v = _Vec(self, x, self.ncol, "x")

@@ -16,8 +16,9 @@ import pytest
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
-from hoexplicit import (ArgumentError, Grid, HighOrderExplicitOp, OutOfMemoryError, WeightingOp,  # noqa: E402
-                        compose, explicit_gpu_normal, normalOperator, workloads)
+from hoexplicit import (ArgumentError, DimensionMismatch, Grid, HighOrderExplicitOp,  # noqa: E402
+                        OutOfMemoryError, WeightingOp, compose, explicit_gpu_normal, normalOperator,
+                        workloads)
 from oracle import dense, oracle  # noqa: E402
 from tests.golden_util import load, model_from_golden  # noqa: E402
 
@@ -333,6 +334,45 @@ def test_host_round_trip_numpy():
     yp = op * xp
     assert yp.device.type == "cpu" and yp.is_pinned()
     assert dense.rel(yp.numpy(), g["forward"]) < 1e-5
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_in_place_products_with_host_buffers(engine):
+    # mul!(y, op, x) / mul!(x, adjoint(op), y) with host tensors: page-locked
+    # operands are queued without a host wait (valid after a synchronise);
+    # back-to-back calls reuse the operator's device buffers in stream order
+    maybe_skip(engine)
+    g = load("gpu_case_2")
+    op = op_from_golden(g, engine)
+    tol = TOL[engine]
+    x0 = torch.from_numpy(g["image"].astype(np.complex64))
+    y0 = torch.from_numpy(g["probe"].astype(np.complex64))
+    xs = [x0.pin_memory(), (x0 * (0.5 - 0.25j)).pin_memory()]
+    yo = [torch.empty(op.nrow, dtype=torch.complex64, pin_memory=True) for _ in xs]
+    for x, y in zip(xs, yo):
+        assert op.prod_(y, x) is y
+    xo = torch.empty(op.ncol, dtype=torch.complex64, pin_memory=True)
+    op.H.prod_(xo, y0.pin_memory())
+    torch.cuda.synchronize()
+    assert dense.rel(yo[0].numpy(), g["forward"]) < tol
+    assert dense.rel(yo[1].numpy(), (0.5 - 0.25j) * g["forward"]) < tol
+    assert dense.rel(xo.numpy(), g["adjoint"]) < tol
+    # pageable host memory: copied synchronously, same results
+    yp = torch.empty(op.nrow, dtype=torch.complex64)
+    op.prod_(yp, x0)
+    assert dense.rel(yp.numpy(), g["forward"]) < tol
+    # device output from a host input, host output from a device input
+    yd = torch.empty(op.nrow, dtype=torch.complex64, device="cuda")
+    op.prod_(yd, xs[0])
+    xh = torch.empty(op.ncol, dtype=torch.complex64, pin_memory=True)
+    op.ctprod_(xh, yd)
+    torch.cuda.synchronize()
+    assert dense.rel(host(yd), g["forward"]) < tol
+    assert dense.rel(xh.numpy(), (op.H * dev(g["forward"])).cpu().numpy()) < tol
+    with pytest.raises(DimensionMismatch):
+        op.prod_(torch.empty(op.nrow + 1, dtype=torch.complex64), x0)
+    with pytest.raises(ArgumentError):
+        op.prod_(yp, x0.to(torch.complex128))
 
 
 def test_timing_trace():
