@@ -678,53 +678,96 @@ __global__ void __launch_bounds__(Warps<N>::THREADS, 1) k_tc_contract(const __gr
   }
 }
 
-// One element of a B operand tile: val split into BF16 hi + lo.
-__device__ __forceinline__ void store_bop(uint16_t *tile, int64_t per, int n, int k, float val) {
-  __nv_bfloat16 h = __float2bfloat16_rn(val);
-  __nv_bfloat16 l = __float2bfloat16_rn(val - __bfloat162float(h));
-  uint32_t o = kmajor_off(n, k) / 2;
-  tile[o] = *reinterpret_cast<uint16_t *>(&h);
-  tile[per + o] = *reinterpret_cast<uint16_t *>(&l);
+// B operand tiles are written in 16-byte units: unit u of a hi tile holds
+// row n, k = 8*kg .. 8*kg+7 (kmajor_off), and consecutive units are
+// consecutive addresses, so consecutive threads store contiguously.
+__device__ __forceinline__ void bop_unit(int u, int &n, int &kg) {
+  n = (u / (8 * (TK / 8))) * 8 + u % 8;
+  kg = (u / 8) % (TK / 8);
+}
+__device__ __forceinline__ int bop_unit_of(int n, int kg) { return ((n / 8) * (TK / 8) + kg) * 8 + n % 8; }
+
+// Eight values of one unit split into BF16 hi + lo (the lo tile follows the
+// hi tile, per elements further on).
+__device__ __forceinline__ void store_bop8(uint16_t *tile, int64_t per, int u, const float *v) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) split_bf16x2(v[2 * j], v[2 * j + 1], h[j], l[j]);
+  reinterpret_cast<uint4 *>(tile)[u] = make_uint4(h[0], h[1], h[2], h[3]);
+  reinterpret_cast<uint4 *>(tile + per)[u] = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// (re, im) of a complex value v in row n = 2*c + q at k = 2*j + r of the
+// forward B operand: [Re, Im; -Im, Re] (r = 0, 1) by q.
+__device__ __forceinline__ void bop_fwd_pair(float2 z, int q, float *v) {
+  v[0] = q == 0 ? z.x : z.y;
+  v[1] = q == 0 ? -z.y : z.x;
+}
+// ... and of the adjoint B operand: [Re, Im; Im, -Re].
+__device__ __forceinline__ void bop_adj_pair(float2 z, int q, float *v) {
+  v[0] = q == 0 ? z.x : z.y;
+  v[1] = q == 0 ? z.y : -z.x;
 }
 
 // B operand of the forward straight from the image: chunk i covers
 // tile-order voxels [i*TV, (i+1)*TV); element (n, k) with k = 2*v_local + r
-// and n = 2*c + q holds (re, im) of Z = x[perm[v]] * csm[v][c].
+// and n = 2*c + q holds (re, im) of Z = x[perm[v]] * csm[v][c].  One thread
+// per 16-byte unit (4 voxels of one row n).
 __global__ void k_tc_bop_forward(const float2 *__restrict__ x, const int *__restrict__ perm,
                                  const float2 *__restrict__ csm, uint16_t *__restrict__ Bop, int nChunks, int N,
                                  int nChaPad) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t per = (int64_t)N * TK;
-  if (i >= (int64_t)nChunks * per) return;
-  int ch = (int)(i / per), e = (int)(i % per);
-  int n = e / TK, k = e % TK;
-  int v = ch * TV + k / 2, r = k & 1, c = n / 2, q = n & 1;
-  float2 z = make_float2(0.f, 0.f);
-  const int g = perm[v];
-  if (c < nChaPad && g >= 0) {
-    const float2 xv = x[g], cv = csm[(int64_t)v * nChaPad + c];
-    z = make_float2(xv.x * cv.x - xv.y * cv.y, xv.x * cv.y + xv.y * cv.x);
+  const int units = N * (TK / 8);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nChunks * units) return;
+  const int ch = (int)(i / units), u = (int)(i % units);
+  int n, kg;
+  bop_unit(u, n, kg);
+  const int c = n / 2, q = n & 1;
+  float v[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int vx = ch * TV + kg * 4 + j;
+    float2 z = make_float2(0.f, 0.f);
+    const int g = perm[vx];
+    // csm rows exist for every tile-order voxel (zero padding), so its load
+    // does not wait for perm
+    const float2 cv = c < nChaPad ? csm[(int64_t)vx * nChaPad + c] : make_float2(0.f, 0.f);
+    if (g >= 0) {
+      const float2 xv = x[g];
+      z = make_float2(xv.x * cv.x - xv.y * cv.y, xv.x * cv.y + xv.y * cv.x);
+    }
+    bop_fwd_pair(z, q, v + 2 * j);
   }
-  store_bop(Bop + (size_t)ch * 2 * per, per, n, k, r == 0 ? (q == 0 ? z.x : z.y) : (q == 0 ? -z.y : z.x));
+  const int64_t per = (int64_t)N * TK;
+  store_bop8(Bop + (size_t)ch * 2 * per, per, u, v);
 }
 
 // B operand of the adjoint straight from the data y (samples fastest, then
 // coils), weighted by D (NULL: ones): chunk i covers samples [i*TV, (i+1)*TV).
+// One thread per 16-byte unit (4 samples of one row n).
 __global__ void k_tc_bop_adjoint(const float2 *__restrict__ y, const float *__restrict__ D,
                                  uint16_t *__restrict__ Bop, int nChunks, int N, int nSam, int nCha) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t per = (int64_t)N * TK;
-  if (i >= (int64_t)nChunks * per) return;
-  int ch = (int)(i / per), e = (int)(i % per);
-  int n = e / TK, k = e % TK;
-  int s = ch * TV + k / 2, r = k & 1, c = n / 2, q = n & 1;
-  float2 yv = make_float2(0.f, 0.f);
-  if (s < nSam && c < nCha) {
-    const int64_t o = (int64_t)c * nSam + s;
-    yv = y[o];
-    if (D) { const float w = D[o]; yv.x *= w; yv.y *= w; }
+  const int units = N * (TK / 8);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nChunks * units) return;
+  const int ch = (int)(i / units), u = (int)(i % units);
+  int n, kg;
+  bop_unit(u, n, kg);
+  const int c = n / 2, q = n & 1;
+  float v[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int s = ch * TV + kg * 4 + j;
+    float2 yv = make_float2(0.f, 0.f);
+    if (s < nSam && c < nCha) {
+      const int64_t o = (int64_t)c * nSam + s;
+      yv = y[o];
+      if (D) { const float w = D[o]; yv.x *= w; yv.y *= w; }
+    }
+    bop_adj_pair(yv, q, v + 2 * j);
   }
-  store_bop(Bop + (size_t)ch * 2 * per, per, n, k, r == 0 ? (q == 0 ? yv.x : yv.y) : (q == 0 ? yv.y : -yv.x));
+  const int64_t per = (int64_t)N * TK;
+  store_bop8(Bop + (size_t)ch * 2 * per, per, u, v);
 }
 
 // The slots a row tile's partial sums occupy: the CTAs that own any of its
@@ -739,65 +782,104 @@ struct SlotMap {
 
 // Forward reduction over the written slots: y[c*nSam + s] = scale * sum, or
 // (bopA != NULL) the adjoint's B operand of D * (scale * sum) for the normal
-// operator.  Threads cover s < nSamPad and c < nChaTC.
-__global__ void k_tc_fwd_reduce(const float2 *__restrict__ part, int nSamPad, int nChaPad, int nChaTC, int nSam,
-                                int nCha, float scale, SlotMap m, float2 *__restrict__ y,
-                                const float *__restrict__ D, uint16_t *__restrict__ bopA, int N) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)nSamPad * nChaTC) return;
-  const int s = (int)(i / nChaTC), c = (int)(i % nChaTC);
-  float sr = 0.f, si = 0.f;
-  if (c < nChaPad) {
-    const int ns = m.slots(s / TM);
-    for (int k = 0; k < ns; ++k) {
-      const float2 v = part[((int64_t)k * nSamPad + s) * nChaPad + c];
-      sr += v.x;
-      si += v.y;
+// operator.  A block takes FR_S samples and all nChaTC coils (one row tile:
+// FR_S divides TM): it reads the
+// slots with coils fastest, transposes through shared memory and writes y
+// with samples fastest (or whole 16-byte units of the B operand).
+constexpr int FR_S = 16;
+__global__ void __launch_bounds__(256) k_tc_fwd_reduce(const float2 *__restrict__ part, int nSamPad, int nChaPad,
+                                                       int nChaTC, int nSam, int nCha, float scale, SlotMap m,
+                                                       float2 *__restrict__ y, const float *__restrict__ D,
+                                                       uint16_t *__restrict__ bopA, int N) {
+  __shared__ float2 tile[64][FR_S + 1];
+  const int s0 = blockIdx.x * FR_S;
+  __shared__ int sns;
+  if (threadIdx.x == 0) sns = m.slots(s0 / TM);
+  __syncthreads();
+  const int ns = sns;
+  for (int e = threadIdx.x; e < FR_S * nChaTC; e += blockDim.x) {
+    const int sl = e / nChaTC, c = e % nChaTC, s = s0 + sl;
+    float sr = 0.f, si = 0.f;
+    if (c < nChaPad) {
+      for (int k = 0; k < ns; ++k) {
+        const float2 v = part[((int64_t)k * nSamPad + s) * nChaPad + c];
+        sr += v.x;
+        si += v.y;
+      }
     }
+    tile[c][sl] = make_float2(sr * scale, si * scale);
   }
-  sr *= scale;
-  si *= scale;
-  const bool valid = s < nSam && c < nCha;
-  const int64_t o = (int64_t)c * nSam + s;
+  __syncthreads();
   if (!bopA) {
-    if (valid) y[o] = make_float2(sr, si);
+    for (int e = threadIdx.x; e < FR_S * nChaTC; e += blockDim.x) {
+      const int c = e / FR_S, sl = e % FR_S, s = s0 + sl;
+      if (s < nSam && c < nCha) y[(int64_t)c * nSam + s] = tile[c][sl];
+    }
     return;
   }
-  const float w = valid ? (D ? D[o] : 1.f) : 0.f;
-  sr *= w;
-  si *= w;
+  // B operand units of these samples: rows n < N, k-groups of 4 samples
   const int64_t per = (int64_t)N * TK;
-  uint16_t *tile = bopA + (size_t)(s / TV) * 2 * per;
-  const int sl = s % TV;
-  store_bop(tile, per, 2 * c, 2 * sl, sr);
-  store_bop(tile, per, 2 * c + 1, 2 * sl, si);
-  store_bop(tile, per, 2 * c, 2 * sl + 1, si);
-  store_bop(tile, per, 2 * c + 1, 2 * sl + 1, -sr);
+  uint16_t *t = bopA + (size_t)(s0 / TV) * 2 * per;
+  const int kg0 = (s0 % TV) / 4;
+  for (int e = threadIdx.x; e < N * (FR_S / 4); e += blockDim.x) {
+    const int n = (e / (8 * (FR_S / 4))) * 8 + e % 8, kgl = (e / 8) % (FR_S / 4);
+    const int c = n / 2, q = n & 1;
+    float v[8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int sl = kgl * 4 + j, s = s0 + sl;
+      float2 z = tile[c][sl];
+      const float w = (s < nSam && c < nCha) ? (D ? D[(int64_t)c * nSam + s] : 1.f) : 0.f;
+      z.x *= w;
+      z.y *= w;
+      bop_adj_pair(z, q, v + 2 * j);
+    }
+    store_bop8(t, per, bop_unit_of(n, kg0 + kgl), v);
+  }
 }
 
 // Adjoint reduction over the written slots: conj(csm), sum over coils,
-// scale, scatter into the full grid (zeroed beforehand).
-__global__ void k_tc_adj_reduce(const float2 *__restrict__ part, int nVoxPad, int nChaPad, int nCha,
-                                const float2 *__restrict__ csm, const int *__restrict__ perm, float scale,
-                                SlotMap m, float2 *__restrict__ x) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nVoxPad) return;
-  const int g = perm[p];
-  if (g < 0) return;
-  const int ns = m.slots(p / TM);
-  float xr = 0.f, xi = 0.f;
-  for (int c = 0; c < nCha; ++c) {
-    float qr = 0.f, qi = 0.f;
-    for (int k = 0; k < ns; ++k) {
-      const float2 v = part[((int64_t)k * nVoxPad + p) * nChaPad + c];
-      qr += v.x;
-      qi += v.y;
-    }
-    const float2 w = csm[(int64_t)p * nChaPad + c];
-    xr += w.x * qr + w.y * qi;   // conj(w) * q
-    xi += w.x * qi - w.y * qr;
+// scale, scatter into the full grid (zeroed beforehand).  L = min(nChaPad,
+// 32) consecutive lanes take one voxel, coils innermost, so that the slot
+// and csm loads are coalesced; the coil sum is a shuffle reduction over the
+// L lanes (every lane of the warp takes part).  A block of 256 threads
+// covers 256 / L voxels of one row tile (L divides 32, TM = 128), so the
+// slot count is computed once per block.  Padding voxels have slot and csm
+// rows too, so those loads do not wait for perm.
+__global__ void __launch_bounds__(256) k_tc_adj_reduce(const float2 *__restrict__ part, int nVoxPad, int nChaPad,
+                                                       int nCha, const float2 *__restrict__ csm,
+                                                       const int *__restrict__ perm, float scale, SlotMap m,
+                                                       float2 *__restrict__ x) {
+  const int L = nChaPad < 32 ? nChaPad : 32;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (int)(i / L), l = (int)(i % L);
+  __shared__ int sns;
+  if (threadIdx.x == 0) {
+    const int p0 = (int)((int64_t)blockIdx.x * blockDim.x / L);
+    sns = p0 < nVoxPad ? m.slots(p0 / TM) : 0;
   }
-  x[g] = make_float2(xr * scale, xi * scale);
+  __syncthreads();
+  const int g = p < nVoxPad ? perm[p] : -1;
+  float xr = 0.f, xi = 0.f;
+  if (p < nVoxPad) {
+    const int ns = sns;
+    for (int c = l; c < nCha; c += L) {
+      float qr = 0.f, qi = 0.f;
+      for (int k = 0; k < ns; ++k) {
+        const float2 v = part[((int64_t)k * nVoxPad + p) * nChaPad + c];
+        qr += v.x;
+        qi += v.y;
+      }
+      const float2 w = csm[(int64_t)p * nChaPad + c];
+      xr += w.x * qr + w.y * qi;   // conj(w) * q
+      xi += w.x * qi - w.y * qr;
+    }
+  }
+  for (int o = L / 2; o > 0; o >>= 1) {
+    xr += __shfl_down_sync(0xffffffffu, xr, o, L);
+    xi += __shfl_down_sync(0xffffffffu, xi, o, L);
+  }
+  if (l == 0 && g >= 0) x[g] = make_float2(xr * scale, xi * scale);   // padding voxels (g < 0) are dropped
 }
 
 // Anchor tables of the anchor k-step: v = 2*pi*tab[i] (radians) split into
@@ -1011,7 +1093,7 @@ SlotMap slot_map(int64_t first, int C, int64_t W, int G) {
 cudaError_t bop_forward(const hoe_handle *h, const TcBuffers &b, const float2 *x, cudaStream_t st) {
   const auto &t = h->t;
   const int chunks = t.nVoxPad / TV;
-  int64_t n = (int64_t)chunks * b.N * TK;
+  const int64_t n = (int64_t)chunks * b.N * (TK / 8);   // 16-byte units
   k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, t.perm, t.csm, b.bopF, chunks, b.N, t.nChaPad);
   h->launches += 1;
   return cudaGetLastError();
@@ -1020,7 +1102,7 @@ cudaError_t bop_forward(const hoe_handle *h, const TcBuffers &b, const float2 *x
 cudaError_t bop_adjoint(const hoe_handle *h, const TcBuffers &b, const float2 *y, const float *D, cudaStream_t st) {
   const auto &t = h->t;
   const int chunks = t.nSamPad / TV;
-  int64_t n = (int64_t)chunks * b.N * TK;
+  const int64_t n = (int64_t)chunks * b.N * (TK / 8);   // 16-byte units
   k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, D, b.bopA, chunks, b.N, t.nSam, t.nCha);
   h->launches += 1;
   return cudaGetLastError();
@@ -1030,9 +1112,9 @@ cudaError_t bop_adjoint(const hoe_handle *h, const TcBuffers &b, const float2 *y
 cudaError_t reduce_forward(const hoe_handle *h, const TcBuffers &b, const SlotMap &m, float2 *y, const float *D,
                            bool toBop, cudaStream_t st) {
   const auto &t = h->t;
-  const int64_t n = (int64_t)t.nSamPad * b.nChaTC;
+  static_assert(TM % FR_S == 0 && TV % FR_S == 0, "reduction blocks within one row tile and one chunk");
   const float scale = (float)(1.0 / sqrt((double)t.nVox));
-  k_tc_fwd_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b.part, t.nSamPad, t.nChaPad, b.nChaTC, t.nSam,
+  k_tc_fwd_reduce<<<(unsigned)(t.nSamPad / FR_S), 256, 0, st>>>(b.part, t.nSamPad, t.nChaPad, b.nChaTC, t.nSam,
                                                                t.nCha, scale, m, y, D, toBop ? b.bopA : nullptr,
                                                                b.N);
   h->launches += 1;
@@ -1044,7 +1126,9 @@ cudaError_t reduce_adjoint(const hoe_handle *h, const TcBuffers &b, const SlotMa
   cudaError_t e = cudaMemsetAsync(x, 0, (size_t)t.nFull * sizeof(float2), st);
   if (e != cudaSuccess) return e;
   const float scale = (float)(1.0 / sqrt((double)t.nVox));
-  k_tc_adj_reduce<<<(t.nVoxPad + 255) / 256, 256, 0, st>>>(b.part, t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm,
+  const int lanes = t.nChaPad < 32 ? t.nChaPad : 32;   // per voxel; divides 32
+  const int64_t n = (int64_t)t.nVoxPad * lanes;
+  k_tc_adj_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b.part, t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm,
                                                            scale, m, x);
   h->launches += 1;
   return cudaGetLastError();
