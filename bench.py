@@ -214,8 +214,7 @@ def time_engine(op, x, y, steps, warmup, flush, stream):
     # the timed steps run without the operator's trace events
     op.set_timing(False)
     for _ in range(steps):
-        flush.zero_()
-        torch.cuda.synchronize()
+        flush.zero_()   # L2 flush, before ev0 in stream order; the step is queued behind it
         ev0.record(stream)
         op.prod_(yout, x)
         op.ctprod_(xout, y)
@@ -258,8 +257,7 @@ def time_recon(op, w, y, flush, stream, iterations, reps):
         l0 = op.timings()["launches"]
         ms = []
         for _ in range(reps):
-            flush.zero_()
-            torch.cuda.synchronize()
+            flush.zero_()   # L2 flush, before ev0 in stream order; the step is queued behind it
             ev0.record(stream)
             hrecon.solve(op, data, weight, iterations=iterations, rel_tol=0.0, lam=1e-9,
                          use_graph=use_graph, out=out, stats=False)
@@ -308,8 +306,7 @@ def run_batch(a):
         torch.cuda.synchronize()
         ms = []
         for _ in range(steps):
-            flush.zero_()
-            torch.cuda.synchronize()
+            flush.zero_()   # L2 flush, before ev0 in stream order; the step is queued behind it
             ev0.record(stream)
             fn()
             ev1.record(stream)
@@ -416,8 +413,7 @@ def time_backward(op, x, y, flush, stream, reps):
         torch.cuda.synchronize()
         ms = []
         for _ in range(n):
-            flush.zero_()
-            torch.cuda.synchronize()
+            flush.zero_()   # L2 flush, before ev0 in stream order; the step is queued behind it
             ev0.record(stream)
             op.backward(x, r, kspha=True, fieldmap=True, t0_b0=True)
             ev1.record(stream)
@@ -455,8 +451,7 @@ def time_normal(op, w, x, flush, stream, reps):
     torch.cuda.synchronize()
     ms = []
     for _ in range(reps):
-        flush.zero_()
-        torch.cuda.synchronize()
+        flush.zero_()   # L2 flush, before ev0 in stream order; the step is queued behind it
         ev0.record(stream)
         D.prod_(out, x)
         ev1.record(stream)
