@@ -305,6 +305,10 @@ __global__ void __launch_bounds__(Warps<N>::THREADS, 1) k_tc_contract(const __gr
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // the prologue above touches no global memory; the B operand, the slots
+  // and the tables may be written by the previous kernel in the stream
+  pdl_wait();
+  pdl_trigger();
 
   if (warp < PW) {
     // ---------------- phase generator: one row x 64 (N <= 32) or 32 columns
@@ -716,6 +720,8 @@ __device__ __forceinline__ void bop_adj_pair(float2 z, int q, float *v) {
 __global__ void k_tc_bop_forward(const float2 *__restrict__ x, const int *__restrict__ perm,
                                  const float2 *__restrict__ csm, uint16_t *__restrict__ Bop, int nChunks, int N,
                                  int nChaPad) {
+  pdl_wait();
+  pdl_trigger();
   const int units = N * (TK / 8);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)nChunks * units) return;
@@ -747,6 +753,8 @@ __global__ void k_tc_bop_forward(const float2 *__restrict__ x, const int *__rest
 // One thread per 16-byte unit (4 samples of one row n).
 __global__ void k_tc_bop_adjoint(const float2 *__restrict__ y, const float *__restrict__ D,
                                  uint16_t *__restrict__ Bop, int nChunks, int N, int nSam, int nCha) {
+  pdl_wait();
+  pdl_trigger();
   const int units = N * (TK / 8);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)nChunks * units) return;
@@ -791,6 +799,8 @@ __global__ void __launch_bounds__(256) k_tc_fwd_reduce(const float2 *__restrict_
                                                        int nChaTC, int nSam, int nCha, float scale, SlotMap m,
                                                        float2 *__restrict__ y, const float *__restrict__ D,
                                                        uint16_t *__restrict__ bopA, int N) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ float2 tile[64][FR_S + 1];
   const int s0 = blockIdx.x * FR_S;
   __shared__ int sns;
@@ -850,6 +860,8 @@ __global__ void __launch_bounds__(256) k_tc_adj_reduce(const float2 *__restrict_
                                                        int nCha, const float2 *__restrict__ csm,
                                                        const int *__restrict__ perm, float scale, SlotMap m,
                                                        float2 *__restrict__ x) {
+  pdl_wait();
+  pdl_trigger();
   const int L = nChaPad < 32 ? nChaPad : 32;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int p = (int)(i / L), l = (int)(i % L);
@@ -920,9 +932,9 @@ template <int N, int KP, int MS>
 cudaError_t launch_contract(const hoe_handle *h, const TcParams<MS> &p, int G, cudaStream_t st) {
   using K = Kern<N, KP>;
   auto kern = k_tc_contract<N, KP, K::NS, MS>;
-  kern<<<G, Warps<N>::THREADS, K::S::BYTES, st>>>(p);
+  const cudaError_t e = launch_pdl(kern, dim3(G), dim3(Warps<N>::THREADS), K::S::BYTES, st, p);
   h->launches += 1;
-  return cudaGetLastError();
+  return e;
 }
 
 // One-time per (process, instantiation): shared-memory limit; returns the
@@ -1094,18 +1106,20 @@ cudaError_t bop_forward(const hoe_handle *h, const TcBuffers &b, const float2 *x
   const auto &t = h->t;
   const int chunks = t.nVoxPad / TV;
   const int64_t n = (int64_t)chunks * b.N * (TK / 8);   // 16-byte units
-  k_tc_bop_forward<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, t.perm, t.csm, b.bopF, chunks, b.N, t.nChaPad);
+  const cudaError_t e = launch_pdl(k_tc_bop_forward, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, x,
+                                   t.perm, t.csm, b.bopF, chunks, b.N, t.nChaPad);
   h->launches += 1;
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t bop_adjoint(const hoe_handle *h, const TcBuffers &b, const float2 *y, const float *D, cudaStream_t st) {
   const auto &t = h->t;
   const int chunks = t.nSamPad / TV;
   const int64_t n = (int64_t)chunks * b.N * (TK / 8);   // 16-byte units
-  k_tc_bop_adjoint<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(y, D, b.bopA, chunks, b.N, t.nSam, t.nCha);
+  const cudaError_t e = launch_pdl(k_tc_bop_adjoint, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, y, D,
+                                   b.bopA, chunks, b.N, t.nSam, t.nCha);
   h->launches += 1;
-  return cudaGetLastError();
+  return e;
 }
 
 // y = E x (toBop false), or the adjoint B operand of D * E x (toBop true).
@@ -1114,11 +1128,11 @@ cudaError_t reduce_forward(const hoe_handle *h, const TcBuffers &b, const SlotMa
   const auto &t = h->t;
   static_assert(TM % FR_S == 0 && TV % FR_S == 0, "reduction blocks within one row tile and one chunk");
   const float scale = (float)(1.0 / sqrt((double)t.nVox));
-  k_tc_fwd_reduce<<<(unsigned)(t.nSamPad / FR_S), 256, 0, st>>>(b.part, t.nSamPad, t.nChaPad, b.nChaTC, t.nSam,
-                                                               t.nCha, scale, m, y, D, toBop ? b.bopA : nullptr,
-                                                               b.N);
+  const cudaError_t e = launch_pdl(k_tc_fwd_reduce, dim3((unsigned)(t.nSamPad / FR_S)), dim3(256), 0, st, b.part,
+                                   t.nSamPad, t.nChaPad, b.nChaTC, t.nSam, t.nCha, scale, m, y, D,
+                                   toBop ? b.bopA : nullptr, b.N);
   h->launches += 1;
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t reduce_adjoint(const hoe_handle *h, const TcBuffers &b, const SlotMap &m, float2 *x, cudaStream_t st) {
@@ -1128,10 +1142,10 @@ cudaError_t reduce_adjoint(const hoe_handle *h, const TcBuffers &b, const SlotMa
   const float scale = (float)(1.0 / sqrt((double)t.nVox));
   const int lanes = t.nChaPad < 32 ? t.nChaPad : 32;   // per voxel; divides 32
   const int64_t n = (int64_t)t.nVoxPad * lanes;
-  k_tc_adj_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b.part, t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm,
-                                                           scale, m, x);
+  const cudaError_t e2 = launch_pdl(k_tc_adj_reduce, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, b.part,
+                                    t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm, scale, m, x);
   h->launches += 1;
-  return cudaGetLastError();
+  return e2;
 }
 
 TcParams<1> single_params(const hoe_handle *h, const TcBuffers &b, const TcSlice &sl) {
