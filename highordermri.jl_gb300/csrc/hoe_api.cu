@@ -99,7 +99,7 @@ void release_device(hoe_handle *h) {
   auto &t = h->t;
   dfree(t.dbeta); dfree(t.kappa); dfree(t.Atab); dfree(t.Btab); dfree(t.csm);
   dfree(t.dbHi); dfree(t.dbLo); dfree(t.kpHi); dfree(t.kpLo);
-  dfree(t.perm);  dfree(t.bfraw); dfree(t.kdot); dfree(t.times);
+  dfree(t.perm);  dfree(t.unmasked);  dfree(t.bfraw); dfree(t.kdot); dfree(t.times);
   dfree(t.beta64); dfree(t.betabar); dfree(t.gambar); dfree(t.kap64); dfree(t.times64);
   dfree(t.bal); dfree(t.Vr);
   auto &s = h->s;
@@ -192,7 +192,7 @@ namespace {
 // hoe_create.  Built without touching the device (also used by hoe_plan).
 struct Plan {
   hoe::Tables t;                                   // sizes (device pointers unused)
-  std::vector<int> order, perm;
+  std::vector<int> order, perm, unmasked;
   std::vector<double> beta64, gam64, betabar, gambar, kap64, bal, Vr;
   std::vector<float> dbeta, kappa, bfraw, kdot, times_f;
   std::vector<float> dbHi, dbLo, kpHi, kpLo;   // TF32 hi/lo, UMMA K-major tiles
@@ -305,6 +305,15 @@ int make_plan(const hoe_desc *d, Plan &P) {
   beta64.assign((size_t)t.nVoxPad * R, 0.0);
   gam64.assign((size_t)t.nSamPad * R, 0.0);
   perm.assign(t.nVoxPad, -1);
+  {
+    // grid points outside the mask: the adjoint writes zeros there
+    std::vector<char> in(t.nFull, 0);
+    for (int m = 0; m < nVox; ++m) in[d->mask_idx[m]] = 1;
+    P.unmasked.clear();
+    for (int g = 0; g < t.nFull; ++g)
+      if (!in[g]) P.unmasked.push_back(g);
+    t.nUnmasked = (int)P.unmasked.size();
+  }
   for (int p = 0; p < nVox; ++p) {
     int m = order[p];
     perm[p] = d->mask_idx[m];
@@ -605,6 +614,7 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
   A(al.alloc(&t.Btab, (size_t)t.nSt * t.nVoxPad));
   A(al.alloc(&t.csm, csm.size()));
   A(al.alloc(&t.perm, perm.size()));
+  A(al.alloc(&t.unmasked, std::max<size_t>(P.unmasked.size(), 1)));
   A(al.alloc(&t.bfraw, bfraw.size()));
   A(al.alloc(&t.kdot, kdot.size()));
   A(al.alloc(&t.times, times_f.size()));
@@ -636,6 +646,7 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
     H2D(t.kpLo, P.kpLo.data(), P.kpLo.size() * sizeof(float));
     H2D(t.csm, csm.data(), csm.size() * sizeof(float2));
     H2D(t.perm, perm.data(), perm.size() * sizeof(int));
+    if (!P.unmasked.empty()) H2D(t.unmasked, P.unmasked.data(), P.unmasked.size() * sizeof(int));
     H2D(t.bfraw, bfraw.data(), bfraw.size() * sizeof(float));
     H2D(t.kdot, kdot.data(), kdot.size() * sizeof(float));
     H2D(t.times, times_f.data(), times_f.size() * sizeof(float));

@@ -63,6 +63,8 @@ struct Tables {
   float  *Btab  = nullptr;   // [nSt][nVoxPad] frac(beta . gammabar)
   float2 *csm   = nullptr;   // [nVoxPad][nChaPad]
   int    *perm  = nullptr;   // [nVoxPad] linear grid index, -1 for padding
+  int    *unmasked = nullptr;   // [nUnmasked] linear grid indices outside the mask, ascending
+  int    nUnmasked = 0;
   // TF32 hi/lo copies of the reduced residual vectors for the tensor-core
   // phase MMA, in UMMA K-major no-swizzle layout: 8-row groups of KP/4 core
   // matrices (8 rows x 4 TF32 each); width KP = rank rounded up to 8, 16 or 24

@@ -849,7 +849,8 @@ __global__ void __launch_bounds__(256) k_tc_fwd_reduce(const float2 *__restrict_
 }
 
 // Adjoint reduction over the written slots: conj(csm), sum over coils,
-// scale, scatter into the full grid (zeroed beforehand).  L = min(nChaPad,
+// scale, scatter into the full grid; the threads after the voxels' write
+// zeros to the grid points outside the mask.  L = min(nChaPad,
 // 32) consecutive lanes take one voxel, coils innermost, so that the slot
 // and csm loads are coalesced; the coil sum is a shuffle reduction over the
 // L lanes (every lane of the warp takes part).  A block of 256 threads
@@ -859,6 +860,7 @@ __global__ void __launch_bounds__(256) k_tc_fwd_reduce(const float2 *__restrict_
 __global__ void __launch_bounds__(256) k_tc_adj_reduce(const float2 *__restrict__ part, int nVoxPad, int nChaPad,
                                                        int nCha, const float2 *__restrict__ csm,
                                                        const int *__restrict__ perm, float scale, SlotMap m,
+                                                       const int *__restrict__ unmasked, int nUnmasked,
                                                        float2 *__restrict__ x) {
   pdl_wait();
   pdl_trigger();
@@ -892,6 +894,8 @@ __global__ void __launch_bounds__(256) k_tc_adj_reduce(const float2 *__restrict_
     xi += __shfl_down_sync(0xffffffffu, xi, o, L);
   }
   if (l == 0 && g >= 0) x[g] = make_float2(xr * scale, xi * scale);   // padding voxels (g < 0) are dropped
+  const int64_t z = i - (int64_t)nVoxPad * L;   // nVoxPad * L is a multiple of 32: whole warps
+  if (z >= 0 && z < nUnmasked) x[unmasked[z]] = make_float2(0.f, 0.f);
 }
 
 // Anchor tables of the anchor k-step: v = 2*pi*tab[i] (radians) split into
@@ -1137,13 +1141,12 @@ cudaError_t reduce_forward(const hoe_handle *h, const TcBuffers &b, const SlotMa
 
 cudaError_t reduce_adjoint(const hoe_handle *h, const TcBuffers &b, const SlotMap &m, float2 *x, cudaStream_t st) {
   const auto &t = h->t;
-  cudaError_t e = cudaMemsetAsync(x, 0, (size_t)t.nFull * sizeof(float2), st);
-  if (e != cudaSuccess) return e;
   const float scale = (float)(1.0 / sqrt((double)t.nVox));
   const int lanes = t.nChaPad < 32 ? t.nChaPad : 32;   // per voxel; divides 32
-  const int64_t n = (int64_t)t.nVoxPad * lanes;
+  const int64_t n = (int64_t)t.nVoxPad * lanes + t.nUnmasked;
   const cudaError_t e2 = launch_pdl(k_tc_adj_reduce, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, b.part,
-                                    t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm, scale, m, x);
+                                    t.nVoxPad, t.nChaPad, t.nCha, t.csm, t.perm, scale, m, t.unmasked,
+                                    t.nUnmasked, x);
   h->launches += 1;
   return e2;
 }

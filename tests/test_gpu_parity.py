@@ -369,6 +369,14 @@ def test_in_place_products_with_host_buffers(engine):
     torch.cuda.synchronize()
     assert dense.rel(host(yd), g["forward"]) < tol
     assert dense.rel(xh.numpy(), (op.H * dev(g["forward"])).cpu().numpy()) < tol
+    # the adjoint writes every grid point: zeros outside the mask, whatever
+    # the output buffer held
+    mask = g["mask"].astype(bool)
+    xf = torch.full((op.ncol,), 7 - 3j, dtype=torch.complex64, device="cuda")
+    op.ctprod_(xf, dev(g["probe"]))
+    xf = host(xf)
+    assert not mask.all() and np.all(xf[~mask] == 0)
+    assert dense.rel(xf, g["adjoint"]) < tol
     with pytest.raises(DimensionMismatch):
         op.prod_(torch.empty(op.nrow + 1, dtype=torch.complex64), x0)
     with pytest.raises(ArgumentError):
