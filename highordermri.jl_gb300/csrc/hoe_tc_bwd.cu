@@ -500,40 +500,71 @@ __device__ __forceinline__ void store_split(uint16_t *tile, int64_t per, uint32_
   tile[per + byteOff / 2] = *reinterpret_cast<uint16_t *>(&l);
 }
 
-// A of the W product: row s of sample tile st, k = 2c + j: (Re, Im) r[s, c]
-// (r samples fastest, then coils; zero beyond nSam and nCha).
+// 16-byte unit u of a [TM x KK] K-major tile (kmaj): row n, k = 8*kg ..
+// 8*kg+7; consecutive units are consecutive addresses.
+__device__ __forceinline__ void bw_unit(int u, int KK, int &n, int &kg) {
+  n = (u / (8 * (KK / 8))) * 8 + u % 8;
+  kg = (u / 8) % (KK / 8);
+}
+// Eight values split into BF16 hi + lo, stored as one unit of the hi tile and
+// one of the lo tile (per elements further on).
+__device__ __forceinline__ void store_split8(uint16_t *tile, int64_t per, int u, const float *v) {
+  uint32_t hw[4], lw[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) split_bf16x2(v[2 * j], v[2 * j + 1], hw[j], lw[j]);
+  reinterpret_cast<uint4 *>(tile)[u] = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+  reinterpret_cast<uint4 *>(tile + per)[u] = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+}
+
+// A of the W product: sample tile st, row s, k = 2c + m: (Re r, Im r)[c].
+// One thread per 16-byte unit (4 coils of one sample).
 __global__ void k_bw_ra(const float2 *__restrict__ r, int nSam, int nCha, int nSamPad, int KC,
                         uint16_t *__restrict__ ra) {
+  const int units = TM * (KC / 8);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)nSamPad * KC) return;
-  const int s = (int)(i / KC), k = (int)(i % KC), c = k / 2;
-  float v = 0.f;
-  if (s < nSam && c < nCha) {
-    const float2 z = r[(int64_t)c * nSam + s];
-    v = (k & 1) ? z.y : z.x;
+  if (i >= (int64_t)(nSamPad / TM) * units) return;
+  const int st = (int)(i / units), u = (int)(i % units);
+  int n, kg;
+  bw_unit(u, KC, n, kg);
+  const int s = st * TM + n;
+  float v[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = kg * 4 + j;
+    const float2 z = (s < nSam && c < nCha) ? r[(int64_t)c * nSam + s] : make_float2(0.f, 0.f);
+    v[2 * j] = z.x;
+    v[2 * j + 1] = z.y;
   }
   const int64_t per = (int64_t)TM * KC;
-  store_split(ra + (size_t)(s / TM) * 2 * per, per, kmaj(s % TM, k, KC), v);
+  store_split8(ra + (size_t)st * 2 * per, per, u, v);
 }
 
 // B of the W product: chunk ch, row n = 2v + j (voxel v of the chunk), k = 2c + m:
 //   j = 0 (Re W): (Re Z, Im Z);   j = 1 (Im W): (Im Z, -Re Z),  Z = x[perm[v]] csm[v, c]
+// One thread per 16-byte unit (4 coils of one row).
 __global__ void k_bw_zb(const float2 *__restrict__ x, const int *__restrict__ perm, const float2 *__restrict__ csm,
                         int nChunks, int nChaPad, int nCha, int KC, uint16_t *__restrict__ zb) {
+  const int units = TM * (KC / 8);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t per = (int64_t)TM * KC;
-  if (i >= (int64_t)nChunks * per) return;
-  const int ch = (int)(i / per), e = (int)(i % per);
-  const int n = e / KC, k = e % KC;
-  const int v = ch * TV + n / 2, j = n & 1, c = k / 2, m = k & 1;
-  float2 z = make_float2(0.f, 0.f);
-  const int g = perm[v];
-  if (c < nCha && g >= 0) {
-    const float2 xv = x[g], cv = csm[(int64_t)v * nChaPad + c];
-    z = make_float2(xv.x * cv.x - xv.y * cv.y, xv.x * cv.y + xv.y * cv.x);
+  if (i >= (int64_t)nChunks * units) return;
+  const int ch = (int)(i / units), u = (int)(i % units);
+  int n, kg;
+  bw_unit(u, KC, n, kg);
+  const int vx = ch * TV + n / 2, jj = n & 1;
+  const int g = perm[vx];
+  const float2 xv = g >= 0 ? x[g] : make_float2(0.f, 0.f);
+  float v[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = kg * 4 + j;
+    // csm rows exist for every tile-order voxel and padded coil (zeros)
+    const float2 cv = c < nCha ? csm[(int64_t)vx * nChaPad + c] : make_float2(0.f, 0.f);
+    const float2 z = make_float2(xv.x * cv.x - xv.y * cv.y, xv.x * cv.y + xv.y * cv.x);
+    v[2 * j] = jj == 0 ? z.x : z.y;
+    v[2 * j + 1] = jj == 0 ? z.y : -z.x;
   }
-  const float val = j == 0 ? (m == 0 ? z.x : z.y) : (m == 0 ? z.y : -z.x);
-  store_split(zb + (size_t)ch * 2 * per, per, kmaj(n, k, KC), val);
+  const int64_t per = (int64_t)TM * KC;
+  store_split8(zb + (size_t)ch * 2 * per, per, u, v);
 }
 
 // Basis tiles: chunk ch, row l (basis column, kRF used), k = voxel of the chunk.
@@ -640,7 +671,8 @@ cudaError_t tc_backward(hoe_handle *h, const float2 *x, const float2 *r, float *
   const TcBuffers &tb = *(const TcBuffers *)h->tc_host;
   const auto &t = h->t;
   const int nChunks = t.nVoxPad / TV;
-  const int64_t nR = (int64_t)t.nSamPad * b.KC, nZ = (int64_t)nChunks * TM * b.KC;
+  const int64_t nR = (int64_t)(t.nSamPad / TM) * TM * (b.KC / 8);   // 16-byte units
+  const int64_t nZ = (int64_t)nChunks * TM * (b.KC / 8);
   k_bw_ra<<<(unsigned)((nR + 255) / 256), 256, 0, st>>>(r, t.nSam, t.nCha, t.nSamPad, b.KC, b.ra);
   k_bw_zb<<<(unsigned)((nZ + 255) / 256), 256, 0, st>>>(x, t.perm, (const float2 *)t.csm, nChunks, t.nChaPad, t.nCha,
                                                          b.KC, b.zb);
