@@ -31,10 +31,12 @@ constexpr int TM = 128;             // rows per CTA (one sample tile / one voxel
 constexpr int TV = 64;              // complex columns per pipeline stage
 constexpr int TK = 2 * TV;          // real K per stage (128 BF16 = 8 UMMA k-steps)
 
-// Phase warps: two groups of 8 take alternate stages (group = warp >> 3), so
-// one group's barrier and tensor-memory latencies overlap the other's
+// Phase warps of the backward kernel and of the forward/adjoint kernel above
+// 16 coils: two groups of 8 take alternate stages (group = warp >> 3), so one
+// group's barrier and tensor-memory latencies overlap the other's
 // arithmetic; within a group a warp covers one TMEM lane quarter (warp & 3)
-// and half of the stage's columns ((warp >> 2) & 1).
+// and half of the stage's columns ((warp >> 2) & 1).  (Up to 16 coils the
+// forward/adjoint kernel uses three groups of 4: Warps<N> in hoe_tc.cu.)
 constexpr int PHASE_WARPS = 16;
 constexpr int GROUP_WARPS = PHASE_WARPS / 2;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s bound on any single wait
