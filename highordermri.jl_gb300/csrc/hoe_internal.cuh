@@ -140,6 +140,33 @@ struct CgState {
   CgGraph graph;
 };
 
+// Programmatic dependent launch.  The engine's kernels are launched with
+// programmatic stream serialisation (launch_pdl), so a kernel may become
+// resident while the previous kernel in the stream is still running.  Each
+// kernel calls pdl_wait() before its first global-memory access (it returns
+// once the previous grid has completed and its writes are visible) and
+// pdl_trigger() only after that, so that kernel k+1 cannot start before
+// kernel k-1 has finished.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Launch with programmatic stream serialisation (cudaLaunchKernelEx).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 }  // namespace hoe
 
 struct hoe_handle {

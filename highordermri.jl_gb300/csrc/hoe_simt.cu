@@ -369,6 +369,8 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
 
 __global__ void k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamPad, int R0,
                          int nSam, float *__restrict__ dk) {
+  pdl_wait();
+  pdl_trigger();
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)nSam * R0) return;
   int s = (int)(i / R0), l = (int)(i % R0);
@@ -381,11 +383,18 @@ __global__ void k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamP
 // Sums of the partial rows [nRows][nVoxPad] per voxel in kBwdVoxSplit row
 // ranges (grid.y): vpart[0][split][p] (sum_s G), vpart[1][split][p] (sum_s G t).
 // A range holds a few dozen rows, summed in FP32 (GB300's FP64 add rate would
-// bound this pass); the ranges are added in FP64 by k_bwd_vox.
+// bound this pass); the ranges are added in FP64 by k_bwd_vox.  With ddf
+// given, the first range's threads also write the zeros of dL/dfieldmap
+// outside the mask (k_bwd_vox writes the voxels).
 __global__ void k_bwd_rows(const float *__restrict__ g1part, const float *__restrict__ gtpart, int nRows,
-                           int nVoxPad, double *__restrict__ vpart) {
+                           int nVoxPad, double *__restrict__ vpart, float *__restrict__ ddf,
+                           const int *__restrict__ unmasked, int nUnmasked) {
+  pdl_wait();
+  pdl_trigger();
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nVoxPad) return;
+  if (ddf && blockIdx.y == 0)
+    for (int z = p; z < nUnmasked; z += nVoxPad) ddf[unmasked[z]] = 0.f;
   const int per = (nRows + kBwdVoxSplit - 1) / kBwdVoxSplit;
   const int k0 = blockIdx.y * per, k1 = min(nRows, k0 + per);
   float a1 = 0.f, at = 0.f;
@@ -400,6 +409,8 @@ __global__ void k_bwd_rows(const float *__restrict__ g1part, const float *__rest
 __global__ void k_bwd_vox(const double *__restrict__ vpart, int nVoxPad, const int *__restrict__ perm,
                           const float *__restrict__ bfraw, int R0, float *__restrict__ ddf,
                           double *__restrict__ blockAcc) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double red[256];
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   double contrib = 0.0;
@@ -425,6 +436,8 @@ __global__ void k_bwd_t0(const double *__restrict__ blockAcc, int nBlocks, int u
                          const float *__restrict__ dkpart, int nSplit, int nSamPad,
                          const float *__restrict__ kdot, int nSam, int nTerm, int useCoef,
                          double *__restrict__ dt0) {
+  pdl_wait();
+  pdl_trigger();
   __shared__ double red[256];
   double acc = 0.0;
   if (useB0)
@@ -624,22 +637,24 @@ cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const flo
   const int nVB = (t.nVoxPad + 255) / 256;
   cudaError_t e = cudaSuccess;
   h->launches += 2 + ((flags & HOE_GRAD_KSPHA) ? 1 : 0) + ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
+  // programmatic dependent launches: each kernel waits for its predecessor
+  // before its first global access (pdl_wait)
+  auto ok = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
   if (flags & HOE_GRAD_KSPHA) {
     int64_t n = (int64_t)t.nSam * t.R0;
-    k_bwd_dk<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dkpart, nSplit, t.nSamPad, t.R0, t.nSam, dk);
+    ok(launch_pdl(k_bwd_dk, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, dkpart, nSplit, t.nSamPad, t.R0,
+                  t.nSam, dk));
   }
-  if (flags & HOE_GRAD_FIELDMAP) {
-    e = cudaMemsetAsync(ddf, 0, (size_t)t.nFull * sizeof(float), st);
-    if (e != cudaSuccess) return e;
-  }
-  k_bwd_rows<<<dim3(nVB, kBwdVoxSplit), 256, 0, st>>>(g1, gt, nRows, t.nVoxPad, vpart);
-  k_bwd_vox<<<nVB, 256, 0, st>>>(vpart, t.nVoxPad, t.perm, t.bfraw, t.R0, (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr,
-                                 dred);
+  float *ddfOut = (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr;
+  ok(launch_pdl(k_bwd_rows, dim3(nVB, kBwdVoxSplit), dim3(256), 0, st, g1, gt, nRows, t.nVoxPad, vpart, ddfOut,
+                (const int *)t.unmasked, t.nUnmasked));
+  ok(launch_pdl(k_bwd_vox, dim3(nVB), dim3(256), 0, st, vpart, t.nVoxPad, (const int *)t.perm,
+                (const float *)t.bfraw, t.R0, ddfOut, dred));
   if (flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF))
-    k_bwd_t0<<<1, 256, 0, st>>>(dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0, dkpart, nSplit,
-                                t.nSamPad, t.kdot, t.nSam, t.nTerm,
-                                (flags & HOE_GRAD_T0_COEF) ? 1 : 0, dt0);
-  return cudaGetLastError();
+    ok(launch_pdl(k_bwd_t0, dim3(1), dim3(256), 0, st, (const double *)dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0,
+                  dkpart, nSplit, t.nSamPad, (const float *)t.kdot, t.nSam, t.nTerm,
+                  (flags & HOE_GRAD_T0_COEF) ? 1 : 0, dt0));
+  return e;
 }
 
 }  // namespace hoe

@@ -198,6 +198,10 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // the prologue above touches no global memory; the W operands and the dk
+  // slots are written by the kernels before this one in the stream
+  pdl_wait();
+  pdl_trigger();
 
   if (warp < PHASE_WARPS) {
     // ---------------- phase warps: rows (warp & 3)*32 + lane, stage columns
@@ -517,11 +521,16 @@ __device__ __forceinline__ void store_split8(uint16_t *tile, int64_t per, int u,
 }
 
 // A of the W product: sample tile st, row s, k = 2c + m: (Re r, Im r)[c].
-// One thread per 16-byte unit (4 coils of one sample).
+// One thread per 16-byte unit (4 coils of one sample).  The threads also
+// zero the dk partial slots (dkz, nz4 float4s) that the backward kernel
+// accumulates into.
 __global__ void k_bw_ra(const float2 *__restrict__ r, int nSam, int nCha, int nSamPad, int KC,
-                        uint16_t *__restrict__ ra) {
+                        uint16_t *__restrict__ ra, float4 *__restrict__ dkz, int64_t nz4) {
+  pdl_wait();
+  pdl_trigger();
   const int units = TM * (KC / 8);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int64_t z = i; z < nz4; z += (int64_t)gridDim.x * blockDim.x) dkz[z] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (i >= (int64_t)(nSamPad / TM) * units) return;
   const int st = (int)(i / units), u = (int)(i % units);
   int n, kg;
@@ -544,6 +553,8 @@ __global__ void k_bw_ra(const float2 *__restrict__ r, int nSam, int nCha, int nS
 // One thread per 16-byte unit (4 coils of one row).
 __global__ void k_bw_zb(const float2 *__restrict__ x, const int *__restrict__ perm, const float2 *__restrict__ csm,
                         int nChunks, int nChaPad, int nCha, int KC, uint16_t *__restrict__ zb) {
+  pdl_wait();
+  pdl_trigger();
   const int units = TM * (KC / 8);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (int64_t)nChunks * units) return;
@@ -606,8 +617,7 @@ cudaError_t bw_launch(const BwParams &p, int G, cudaStream_t st) {
   constexpr int NS = bw_stages<KC, KP>();
   static int nb = bw_configure<KC, KP>();
   if (nb < 1) return cudaErrorInvalidConfiguration;
-  k_tc_backward<KC, KP, NS><<<G, BW_THREADS, BwSmem<KC, KP, NS>::BYTES, st>>>(p);
-  return cudaGetLastError();
+  return launch_pdl(k_tc_backward<KC, KP, NS>, dim3(G), dim3(BW_THREADS), BwSmem<KC, KP, NS>::BYTES, st, p);
 }
 
 cudaError_t bw_dispatch(int KC, int KP, const BwParams &p, int G, cudaStream_t st) {
@@ -673,10 +683,14 @@ cudaError_t tc_backward(hoe_handle *h, const float2 *x, const float2 *r, float *
   const int nChunks = t.nVoxPad / TV;
   const int64_t nR = (int64_t)(t.nSamPad / TM) * TM * (b.KC / 8);   // 16-byte units
   const int64_t nZ = (int64_t)nChunks * TM * (b.KC / 8);
-  k_bw_ra<<<(unsigned)((nR + 255) / 256), 256, 0, st>>>(r, t.nSam, t.nCha, t.nSamPad, b.KC, b.ra);
-  k_bw_zb<<<(unsigned)((nZ + 255) / 256), 256, 0, st>>>(x, t.perm, (const float2 *)t.csm, nChunks, t.nChaPad, t.nCha,
-                                                         b.KC, b.zb);
-  e = cudaMemsetAsync(b.dkpart, 0, (size_t)b.slots * t.nSamPad * kRF * sizeof(float), st);
+  // programmatic dependent launches (pdl_wait before each kernel's first
+  // global access); k_bw_ra also zeroes the dk partial slots
+  const int64_t nz4 = (int64_t)b.slots * t.nSamPad * kRF / 4;
+  e = launch_pdl(k_bw_ra, dim3((unsigned)((nR + 255) / 256)), dim3(256), 0, st, r, t.nSam, t.nCha, t.nSamPad, b.KC,
+                 b.ra, (float4 *)b.dkpart, nz4);
+  if (e == cudaSuccess)
+    e = launch_pdl(k_bw_zb, dim3((unsigned)((nZ + 255) / 256)), dim3(256), 0, st, x, (const int *)t.perm,
+                   (const float2 *)t.csm, nChunks, t.nChaPad, t.nCha, b.KC, b.zb);
   if (e != cudaSuccess) return e;
   BwParams p{};
   p.kpHi = t.kpHi; p.kpLo = t.kpLo; p.dbHi = t.dbHi; p.dbLo = t.dbLo;
