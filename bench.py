@@ -188,6 +188,19 @@ def cpu_baseline(w, seconds: float, x_gpu=None, y_gpu=None, op=None):
     res = {"value": units / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
            "sample": f"E and E^H over {n_rows} of {nSam} samples x {len(idx)} voxels x {w.nCha} coils "
                      f"(FP64 C restatement of array_operator.jl:241-348, OpenMP), {dt:.1f} s"}
+    # the same restatement on one thread, on about 1 s of rows
+    n1 = int(min(nSam, max(4, 1.0 / max(per_row * nthreads, 1e-9))))
+    rows1 = np.sort(rng.choice(nSam, n1, replace=False))
+    m1 = model_rows(rows1)
+    oracle.set_threads(1)
+    try:
+        t0 = time.perf_counter()
+        oracle.adjoint(m1, oracle.forward(m1, xm))
+        dt1 = time.perf_counter() - t0
+    finally:
+        oracle.set_threads(nthreads)
+    res["single_thread"] = {"value": 2.0 * len(idx) * n1 / dt1, "unit": UNIT, "cores": 1,
+                            "sample": f"E and E^H over {n1} of {nSam} samples, {dt1:.1f} s"}
     if op is not None and x_gpu is not None:
         yg = (op * x_gpu).cpu().numpy().reshape(w.nCha, nSam)[:, rows].reshape(-1)
         res["gpu_forward_rel_err_vs_fp64"] = dense.rel(yg, yo)
