@@ -625,6 +625,8 @@ cudaError_t bw_dispatch(int KC, int KP, const BwParams &p, int G, cudaStream_t s
   if (KC == 16 && KP == 16) return bw_launch<16, 16>(p, G, st);
   if (KC == 32 && KP == 8) return bw_launch<32, 8>(p, G, st);
   if (KC == 32 && KP == 16) return bw_launch<32, 16>(p, G, st);
+  if (KC == 16 && KP == 24) return bw_launch<16, 24>(p, G, st);
+  if (KC == 32 && KP == 24) return bw_launch<32, 24>(p, G, st);
   return cudaErrorNotSupported;
 }
 
@@ -670,7 +672,7 @@ cudaError_t bw_prepare(hoe_handle *h) {
 }  // namespace
 
 bool tc_backward_supported(const hoe_handle *h) {
-  return h->tc.ready && h->t.nCha <= 16 && h->t.KP <= 16;
+  return h->tc.ready && h->t.nCha <= 16 && h->t.KP <= 24;
 }
 
 cudaError_t tc_backward(hoe_handle *h, const float2 *x, const float2 *r, float *dk, float *ddf, double *dt0,

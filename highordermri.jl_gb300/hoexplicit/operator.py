@@ -379,7 +379,7 @@ class ExplicitGB300Op:
         one element); unrequested outputs are None.  ``t0_coef`` needs
         ``kspha_dt`` or ``kdot`` at construction.  The tensor-core engine forms
         the gradient on the tensor cores for up to 16 coils and residual widths
-        up to 16 (``info()["residual_width"]``), otherwise the FP32 kernel does.
+        up to 24 (``info()["residual_width"]``), otherwise the FP32 kernel does.
         """
         torch = _torch()
         xv = _Vec(self, x, self.ncol, "x")

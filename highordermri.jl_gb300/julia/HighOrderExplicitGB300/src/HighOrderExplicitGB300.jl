@@ -234,7 +234,7 @@ mask), dt0::Float64)`.  The same call is the pullback of `x -> op*x` for the
 phase parameters when `r` is the output cotangent.  `t0_coef` needs
 `kspha_dt` at construction.  With `engine=:tc` (or `:auto` on a GB300) the
 gradient is formed on the tensor cores for up to 16 coils and residual widths
-up to 16, else on the FP32 kernel.
+up to 24, else on the FP32 kernel.
 """
 function explicit_backward(op::GB300ExplicitOp, x, r; kspha=true, fieldmap=true, t0_b0=true, t0_coef=false)
     h = activate(op)

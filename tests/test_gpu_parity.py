@@ -259,7 +259,7 @@ BWD_CASES = [
     dict(shape=(10, 9, 1), nSam=300, nCha=4, nTerm=16),            # residual width 16, 4 coils
     dict(shape=(11, 9, 1), nSam=300, nCha=8, nTerm=9),             # width 8, 8 coils
     dict(shape=(9, 8, 1), nSam=280, nCha=12, nTerm=9),             # width 8, 12 coils
-    dict(shape=(7, 6, 3), nSam=260, nCha=6, nTerm=16, conc=True),  # width 24: FP32 kernel under "tc"
+    dict(shape=(7, 6, 3), nSam=260, nCha=6, nTerm=16, conc=True),  # width 24
 ]
 
 
@@ -300,6 +300,29 @@ def test_tc_backward_long_pipeline_matches_fp32_engine():
     a = op.backward(x, r)
     op.set_engine("fp32")
     b = op.backward(x, r)
+    for u, v in zip(a, b):
+        u = u.cpu().numpy().astype(np.float64).ravel()
+        v = v.cpu().numpy().astype(np.float64).ravel()
+        assert np.all(np.isfinite(u))
+        assert dense.rel(u, v) < 2e-3
+    op.check()
+    op.close()
+
+
+@pytest.mark.parametrize("nCha", [8, 16])
+def test_tc_backward_width24_matches_fp32_engine(nCha):
+    # 3D grid with concomitant terms: residual rank 17-24, TF32 residual width
+    # 24 (the 16-coil instance runs a 2-stage ring); tens of stages per CTA
+    maybe_skip("tc")
+    w = workloads.small(seed=8, shape=(24, 24, 8), nSam=3000, nCha=nCha, nTerm=16, conc=True)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=w.kspha_dt, engine="tc", **w.op_kwargs())
+    assert op.info()["residual_width"] == 24
+    rng = np.random.default_rng(6)
+    x = dev(w.x)
+    r = op * x - dev(0.98 * (op * x).cpu().numpy() + 0.02 * (rng.standard_normal(op.nrow) + 1j * rng.standard_normal(op.nrow)))
+    a = op.backward(x, r, t0_coef=True)
+    op.set_engine("fp32")
+    b = op.backward(x, r, t0_coef=True)
     for u, v in zip(a, b):
         u = u.cpu().numpy().astype(np.float64).ravel()
         v = v.cpu().numpy().astype(np.float64).ravel()
