@@ -434,8 +434,10 @@ def time_backward(op, x, y, flush, stream, reps):
             ms.append(ev0.elapsed_time(ev1))
         return statistics.mean(ms)
 
-    # the tensor-core backward covers up to 16 coils and residual widths <= 24
-    tc = op.engine == "tc" and op.nCha <= 16 and op.info()["residual_width"] <= 24
+    # the tensor-core backward covers up to 16 coils with residual widths <= 24
+    # and up to 32 coils with widths <= 16
+    rw = op.info()["residual_width"]
+    tc = op.engine == "tc" and ((op.nCha <= 16 and rw <= 24) or (op.nCha <= 32 and rw <= 16))
     m = run(reps)
     pairs = float(op.nVox) * op.nSam
     out = {"ms_per_call": m, "value": pairs / (m / 1e3), "unit": UNIT,

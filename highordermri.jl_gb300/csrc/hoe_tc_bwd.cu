@@ -65,13 +65,13 @@ static_assert(BW_ACC_COL + 3 * BW_NF <= 512, "tensor memory plan");
 // the W product), KP = residual width:
 //   stage ring [NS]: ZB [hi|lo] 128 x KC, CV [hi|lo] 64 x KP (TF32),
 //                    XR [data|0] 128 x 4, XC [data|0] 64 x 4
-//   basis ring [NF]: FB [hi|lo] 32 x 64
+//   basis ring [NF]: FB [hi|lo] 32 x 64 (NF = 4; 2 at KC = 64, 32 coils)
 //   row-tile tables: RV [hi|lo] 128 x KP (TF32), RA [hi|lo] 128 x KC
 //   G tiles [2 parities]: [hi|lo] 128 x 64
 constexpr int BW_NFB = 4;
 template <int KC, int KP, int NS>
 struct BwSmem {
-  static constexpr int NF = BW_NFB;
+  static constexpr int NF = KC > 32 ? 2 : BW_NFB;
   static constexpr int ZB = 128 * KC * 2, FB = BW_NF * TV * 2, CV = TV * KP * 4;
   static constexpr int XR = TM * 4 * 4, XC = TV * 4 * 4;
   static constexpr int RV = TM * KP * 4, RA = TM * KC * 2, GT = TM * TV * 2;
@@ -617,6 +617,7 @@ cudaError_t bw_launch(const BwParams &p, int G, cudaStream_t st) {
   constexpr int NS = bw_stages<KC, KP>();
   static int nb = bw_configure<KC, KP>();
   if (nb < 1) return cudaErrorInvalidConfiguration;
+  static_assert(BwSmem<KC, KP, NS>::BYTES <= 227 * 1024, "shared-memory plan");
   return launch_pdl(k_tc_backward<KC, KP, NS>, dim3(G), dim3(BW_THREADS), BwSmem<KC, KP, NS>::BYTES, st, p);
 }
 
@@ -627,6 +628,8 @@ cudaError_t bw_dispatch(int KC, int KP, const BwParams &p, int G, cudaStream_t s
   if (KC == 32 && KP == 16) return bw_launch<32, 16>(p, G, st);
   if (KC == 16 && KP == 24) return bw_launch<16, 24>(p, G, st);
   if (KC == 32 && KP == 24) return bw_launch<32, 24>(p, G, st);
+  if (KC == 64 && KP == 8) return bw_launch<64, 8>(p, G, st);
+  if (KC == 64 && KP == 16) return bw_launch<64, 16>(p, G, st);
   return cudaErrorNotSupported;
 }
 
@@ -634,7 +637,7 @@ cudaError_t bw_prepare(hoe_handle *h) {
   if (h->tcb_host) return cudaSuccess;
   const auto &t = h->t;
   BwBuffers b;
-  b.KC = t.nCha <= 8 ? 16 : 32;
+  b.KC = t.nCha <= 8 ? 16 : (t.nCha <= 16 ? 32 : 64);
   const int nChunks = t.nVoxPad / TV;
   b.grid = std::min<int64_t>(h->numSMs, (int64_t)t.nSt * nChunks);
   b.slots = max_slots(t.nSt, nChunks, b.grid);
@@ -672,7 +675,9 @@ cudaError_t bw_prepare(hoe_handle *h) {
 }  // namespace
 
 bool tc_backward_supported(const hoe_handle *h) {
-  return h->tc.ready && h->t.nCha <= 16 && h->t.KP <= 24;
+  // shared memory: up to 16 coils with residual widths up to 24, or up to
+  // 32 coils with widths up to 16
+  return h->tc.ready && ((h->t.nCha <= 16 && h->t.KP <= 24) || (h->t.nCha <= 32 && h->t.KP <= 16));
 }
 
 cudaError_t tc_backward(hoe_handle *h, const float2 *x, const float2 *r, float *dk, float *ddf, double *dt0,

@@ -378,8 +378,9 @@ class ExplicitGB300Op:
         (nFull,) float32 tensor zero outside the mask, dL/dt0 float64 tensor of
         one element); unrequested outputs are None.  ``t0_coef`` needs
         ``kspha_dt`` or ``kdot`` at construction.  The tensor-core engine forms
-        the gradient on the tensor cores for up to 16 coils and residual widths
-        up to 24 (``info()["residual_width"]``), otherwise the FP32 kernel does.
+        the gradient on the tensor cores for up to 16 coils with residual widths
+        up to 24 (``info()["residual_width"]``) and up to 32 coils with widths up
+        to 16; otherwise the FP32 kernel does (up to 16 coils).
         """
         torch = _torch()
         xv = _Vec(self, x, self.ncol, "x")

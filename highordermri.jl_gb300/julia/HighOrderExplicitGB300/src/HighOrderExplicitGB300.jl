@@ -233,8 +233,9 @@ Gradient of `0.5*norm(op*x - y)^2` given the residual `r = op*x - y`
 mask), dt0::Float64)`.  The same call is the pullback of `x -> op*x` for the
 phase parameters when `r` is the output cotangent.  `t0_coef` needs
 `kspha_dt` at construction.  With `engine=:tc` (or `:auto` on a GB300) the
-gradient is formed on the tensor cores for up to 16 coils and residual widths
-up to 24, else on the FP32 kernel.
+gradient is formed on the tensor cores for up to 16 coils with residual widths
+up to 24 and up to 32 coils with widths up to 16, else on the FP32 kernel (up to
+16 coils).
 """
 function explicit_backward(op::GB300ExplicitOp, x, r; kspha=true, fieldmap=true, t0_b0=true, t0_coef=false)
     h = activate(op)

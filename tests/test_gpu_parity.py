@@ -267,7 +267,22 @@ BWD_CASES = [
 @pytest.mark.parametrize("case", range(len(BWD_CASES)))
 def test_backward_vs_oracle_and_fd(engine, case):
     maybe_skip(engine)
-    w = workloads.small(seed=4, **BWD_CASES[case])
+    check_backward_vs_oracle(engine, BWD_CASES[case])
+
+
+# 17-32 coils: the tensor-core backward only (KC = 64, 2-stage ring, 2-tile
+# basis ring); the FP32 backward kernel stops at 16 coils
+@pytest.mark.parametrize("params", [dict(shape=(10, 9, 1), nSam=300, nCha=24, nTerm=16),
+                                    dict(shape=(9, 8, 1), nSam=280, nCha=32, nTerm=9),
+                                    dict(shape=(64, 64, 1), nSam=6000, nCha=20, nTerm=16)],
+                         ids=["24c", "32c", "20c-long"])
+def test_tc_backward_many_coils_vs_oracle(params):
+    maybe_skip("tc")
+    check_backward_vs_oracle("tc", params)
+
+
+def check_backward_vs_oracle(engine, params):
+    w = workloads.small(seed=4, **params)
     op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=w.kspha_dt, engine=engine, **w.op_kwargs())
     bf, k, t, f, c, idx = workloads.prepared_model(w)
     # kspha_dt has the nTerm rows of kspha (no concomitant rows)
