@@ -1115,6 +1115,10 @@ int hoe_backward(hoe_handle *h, const void *x, const void *r, float *dk, float *
   cudaError_t e = cudaSuccess;
   if (h->engine == HOE_ENGINE_TC_BF16X3 && hoe::tc_backward_supported(h)) {
     e = hoe::tc_backward(h, (const float2 *)x, (const float2 *)r, dk, ddf, dt0, flags, st);
+  } else if (h->t.nChaPad > 16) {
+    return fail(h, HOE_ERR_UNSUPPORTED,
+                "hoe_backward: the tensor-core backward covers up to 32 coils (residual width <= 16 above 16 "
+                "coils), the FP32 backward up to 16 coils");
   } else {
     e = hoe::prep_Z(h, (const float2 *)x, st);
     if (e == cudaSuccess)

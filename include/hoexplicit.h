@@ -255,7 +255,9 @@ HOE_API int  hoe_derivative(hoe_handle *h, const void *x_dev, void *y_dev, void 
  *   dk_dev   float [nTermEff x nSam] (same layout as kspha) or NULL
  *   ddf_dev  float [prod(matrixSize)], zero outside the mask, or NULL
  *   dt0_dev  double [1] or NULL
- * flags: HOE_GRAD_* bits. */
+ * flags: HOE_GRAD_* bits.  Coverage: the tensor-core engine up to 32 coils
+ * (residual width <= 16 above 16 coils), the FP32 engine up to 16 coils;
+ * beyond that HOE_ERR_UNSUPPORTED. */
 HOE_API int  hoe_backward(hoe_handle *h, const void *x_dev, const void *r_dev,
                   float *dk_dev, float *ddf_dev, double *dt0_dev,
                   int32_t flags, void *stream);

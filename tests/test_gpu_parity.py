@@ -281,6 +281,20 @@ def test_tc_backward_many_coils_vs_oracle(params):
     check_backward_vs_oracle("tc", params)
 
 
+def test_backward_coil_limits_raise():
+    # beyond the kernels' coil counts the call fails cleanly (ArgumentError)
+    maybe_skip("tc")
+    for engine, nCha in (("fp32", 20), ("tc", 40)):
+        w = workloads.small(seed=4, shape=(8, 8, 1), nSam=200, nCha=nCha, nTerm=9)
+        op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine=engine, **w.op_kwargs())
+        x = dev(w.x)
+        with pytest.raises(ArgumentError):
+            op.backward(x, op * x)
+        op * x   # the operator stays usable
+        op.check()
+        op.close()
+
+
 def check_backward_vs_oracle(engine, params):
     w = workloads.small(seed=4, **params)
     op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=w.kspha_dt, engine=engine, **w.op_kwargs())
