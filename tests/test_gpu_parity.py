@@ -240,6 +240,51 @@ def test_config1_full_size_vs_oracle(engine):
     assert info["residual_rank"] <= 10 and info["residual_width"] == 12
 
 
+def test_config2_full_size_properties():
+    # the 200x200 / 12,000-sample / 16-coil workload at full size on the
+    # tensor-core engine: FP64 spot check on sampled rows, agreement with the
+    # FP32 engine, adjoint identity, linearity, bitwise repeatability, and the
+    # fused normal against E^H (D * E x)
+    maybe_skip("tc")
+    w = workloads.config2()
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    rng = np.random.default_rng(12)
+    x = dev(w.x)
+    y0 = op * x
+    ynp = host(y0)
+    # FP64 oracle on 48 sampled rows (all coils)
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    rows = np.sort(rng.choice(w.nSam, 48, replace=False))
+    m = oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=w.kspha.shape[0])
+    yo = oracle.forward(m, w.x[idx])
+    assert dense.rel(ynp.reshape(w.nCha, w.nSam)[:, rows].reshape(-1), yo) < 1e-4
+    # FP32 engine at full size
+    op32 = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    y = dev(ynp + 0.05 * np.linalg.norm(ynp) / np.sqrt(ynp.size) * (rng.standard_normal(ynp.size) + 1j * rng.standard_normal(ynp.size)))
+    assert dense.rel(ynp, host(op32 * x)) < 1e-4
+    xa = op.H * y
+    assert dense.rel(host(xa), host(op32.H * y)) < 1e-4
+    # adjoint identity <y, E x> = <E^H y, x>
+    lhs = np.vdot(host(y), ynp)
+    rhs = np.vdot(host(xa), host(x))
+    assert abs(lhs - rhs) / (np.linalg.norm(ynp) * np.linalg.norm(host(y))) < 1e-5
+    # linearity
+    x2 = dev(rng.standard_normal(op.ncol) + 1j * rng.standard_normal(op.ncol))
+    a, b = 0.7 - 0.2j, -1.3 + 0.4j
+    lin = host(op * (a * x + b * x2))
+    assert dense.rel(lin, a * ynp + b * host(op * x2)) < 1e-5
+    # repeatability (fixed reduction order)
+    assert np.array_equal(host(op * x), ynp)
+    # fused normal vs E^H (D * E x)
+    D = np.tile(0.05 + rng.random(w.nSam), w.nCha)
+    nrm = host(normalOperator(op, D) * x)
+    ref = host(op.H * dev(D * ynp))
+    assert dense.rel(nrm, ref) < 1e-4
+    op.check()
+    op32.close()
+    op.close()
+
+
 def test_derivative_mode_vs_oracle():
     # array_operator.jl:153-166 / 187-235: kspha_dt switches prod to B x
     w = workloads.small(seed=3, shape=(11, 10, 1), nSam=260, nCha=4, nTerm=16, conc=True)
