@@ -147,3 +147,33 @@ def test_batch_errors():
     with pytest.raises(ArgumentError):
         B.forward([dev(w.x) for w in ws])
     ops[0].close()
+
+
+def test_config5_full_size_batch():
+    # the 24-slice workload (160^2-224^2 voxels, 8,000-20,000 samples, 16
+    # coils) in one persistent launch per direction: each member's product
+    # as applied alone, and an FP64 spot check on sampled rows of two slices
+    maybe_skip("tc")
+    ws = workloads.config5()
+    ops = [HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs()) for w in ws]
+    B = OperatorBatch(ops)
+    assert B.info()["n"] == len(ws) == 24
+    rng = np.random.default_rng(55)
+    xs = [dev(w.x) for w in ws]
+    ys = [dev(rng.standard_normal(op.nrow) + 1j * rng.standard_normal(op.nrow)) for op in ops]
+    yb = B.forward(xs)
+    xb = B.adjoint(ys)
+    for op, x, y, a, b in zip(ops, xs, ys, yb, xb):
+        assert rel(host(a), host(op * x)) < 2e-6
+        assert rel(host(b), host(op.H * y)) < 2e-6
+    for i in (0, len(ws) - 1):
+        w = ws[i]
+        bf, k, t, f, cs, idx = workloads.prepared_model(w)
+        rows = np.sort(rng.choice(w.nSam, 32, replace=False))
+        m = oracle.Model(bf, k[:, rows], t[rows], f, cs, nTerm=w.kspha.shape[0])
+        ya = host(yb[i]).reshape(w.nCha, w.nSam)[:, rows].reshape(-1)
+        assert rel(ya, oracle.forward(m, w.x[idx])) < 1e-4
+    B.check()
+    B.close()
+    for op in ops:
+        op.close()
