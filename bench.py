@@ -452,6 +452,52 @@ def time_backward(op, x, y, flush, stream, reps):
     return out
 
 
+def time_extras(w, x, reps=10):
+    """The functions around the operator at the workload's shapes, each timed
+    as the mean of `reps` synchronised calls after two warm calls: the
+    derivative product B x (kspha_dt mode, FindDelay.jl:199-200), the k-dot
+    stencil (FindDelay.jl:179-180), InterpTrajTime (InterpTraj.jl:18-40) on a
+    (nSam, nTerm) series, and the SVD coil compression fit and apply
+    (CoilCompression.jl:239-301) from 2 x nCha to nCha virtual coils."""
+    import torch
+    from hoexplicit import (HighOrderExplicitOp, InterpTrajTime, apply_coil_compression,
+                            fit_coil_compression, kspha_dt)
+
+    def timed_ms(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps * 1e3
+
+    out = {}
+    if w.kspha_dt is not None:
+        opd = HighOrderExplicitOp(w.grid, w.kspha, w.times, kspha_dt=w.kspha_dt, **w.op_kwargs())
+        yd = torch.empty(opd.nrow, dtype=torch.complex64, device=x.device)
+        ms = timed_ms(lambda: opd.prod_(yd, x))
+        out["derivative"] = {"ms_per_call": ms, "value": w.nVox * w.nSam / (ms / 1e3), "unit": UNIT,
+                             "engine": "tc (virtual-coil passes)" if opd.engine == "tc" else "fp32 (CUDA cores)"}
+        opd.close()
+    dt = float(w.times[1] - w.times[0])
+    traj = torch.from_numpy(np.ascontiguousarray(w.kspha.T)).cuda()          # (nSam, nTerm) float64
+    tq = torch.from_numpy(np.asarray(w.times, dtype=np.float64) + 0.37 * dt).cuda()
+    out["kdot_stencil_ms"] = timed_ms(lambda: kspha_dt(traj, dt))
+    out["interp_traj_time_ms"] = timed_ms(lambda: InterpTrajTime(traj, dt, 0.0, tq))
+    rng = np.random.default_rng(7)
+    nc = 2 * w.nCha
+    cal = torch.from_numpy((rng.standard_normal((w.nSam, nc)) + 1j * rng.standard_normal((w.nSam, nc)))
+                           .astype(np.complex64)).cuda()
+    tr = fit_coil_compression(cal, n_virtual_coils=w.nCha)
+    out["coil_fit_ms"] = timed_ms(lambda: fit_coil_compression(cal, n_virtual_coils=w.nCha))
+    out["coil_apply_ms"] = timed_ms(lambda: apply_coil_compression(cal, tr))
+    out["shapes"] = (f"derivative {w.nVox} voxels x {w.nSam} samples x {w.nCha} coils; series {w.nSam} x "
+                     f"{w.kspha.shape[0]}; coils {w.nSam} x {nc} -> {w.nCha}")
+    return out
+
+
 def time_normal(op, w, x, flush, stream, reps):
     """E^H D E (hoe_normal) with square-root-density-like weights squared:
     2*nVox*nSam voxel.samples per application."""
@@ -632,6 +678,11 @@ def run_gb300(a):
         out["normal"] = time_normal(op, w, x, flush, stream, max(3, a.steps // 2))
     except Exception as exc:  # report, do not substitute
         out["normal"] = {"error": str(exc)}
+    if not a.no_recon:
+        try:
+            out["extras"] = time_extras(w, x)
+        except Exception as exc:  # report, do not substitute
+            out["extras"] = {"error": str(exc)}
     if tuned is not None:
         out["autotune"] = tuned
 

@@ -1068,6 +1068,13 @@ cudaError_t apply_forward(hoe_handle *h, const float2 *x, float2 *y, cudaStream_
   return e;
 }
 
+cudaError_t apply_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st) {
+  if (h->engine == HOE_ENGINE_TC_BF16X3 && tc_derivative_supported(h)) return tc_derivative(h, x, y, st);
+  cudaError_t e = prep_Z(h, x, st);
+  if (e == cudaSuccess) e = simt_forward(h, nullptr, y, nullptr, FWD_DERIV_TO_Y, st);
+  return e;
+}
+
 cudaError_t apply_normal(hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st) {
   if (h->engine == HOE_ENGINE_TC_BF16X3) return tc_normal(h, D, x, out, st);
   cudaError_t e = prep_Z(h, x, st);
@@ -1095,8 +1102,7 @@ int hoe_derivative(hoe_handle *h, const void *x, void *y, void *stream) {
   if (!x || !y) return fail(h, HOE_ERR_ARG, "x and y must be device pointers");
   DeviceGuard guard(h->device);
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = hoe::prep_Z(h, (const float2 *)x, st);
-  if (e == cudaSuccess) e = hoe::simt_forward(h, nullptr, (float2 *)y, nullptr, hoe::FWD_DERIV_TO_Y, st);
+  const cudaError_t e = hoe::apply_derivative(h, (const float2 *)x, (float2 *)y, st);
   return finish(h, e, "hoe_derivative");
 }
 

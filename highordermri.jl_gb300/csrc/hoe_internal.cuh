@@ -305,6 +305,13 @@ constexpr int kBwdVoxSplit = 16;   // row ranges of the first voxel reduction pa
 cudaError_t tc_forward(const hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st);
 cudaError_t tc_adjoint(const hoe_handle *h, const float2 *y, const float *D, float2 *x, cudaStream_t st);
 cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st);
+// B x (kspha_dt mode) on the tensor cores, as forward passes over virtual
+// coils (term x coil); buffers on first use.
+bool tc_derivative_supported(const hoe_handle *h);
+cudaError_t tc_derivative_prepare(hoe_handle *h);
+cudaError_t tc_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st);
+// B x on the operator's engine (the tensor-core passes where supported)
+cudaError_t apply_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st);
 bool tc_supported(const hoe_handle *h, std::string *why);
 int *tc_error_word(const hoe_handle *h);   // device word set by a timed-out wait
 // Rebuilds the tensor-core anchor tables from Atab/Btab (no-op before tc_prepare).

@@ -324,6 +324,9 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
   if (e == cudaSuccess) e = cudaMemcpyAsync(mask, hm.data(), kRmax * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = kdot_stencil(traj, nField, nTerm, q.dt, kd, st);
   if (e == cudaSuccess) e = cg_prepare(h);
+  // the replan below supplies kspha_dt, so the tensor-core derivative runs
+  // in the captured iteration: its buffers are allocated before the capture
+  if (e == cudaSuccess && h->engine == HOE_ENGINE_TC_BF16X3 && h->tc.ready) e = tc_derivative_prepare(h);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host staging above must be consumed
   if (e != cudaSuccess) { cleanup(); return e; }
 
@@ -337,8 +340,7 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
     if (err == cudaSuccess) err = replan_samples(h, ks, nTerm, kdt, nTerm, mask, s);
     if (err == cudaSuccess) err = cg_enqueue(h, data, weights, x, r, s);
     if (err == cudaSuccess) err = apply_forward(h, x, yf, s);
-    if (err == cudaSuccess) err = prep_Z(h, x, s);  // the derivative runs on the FP32 engine
-    if (err == cudaSuccess) err = simt_forward(h, nullptr, yd, nullptr, FWD_DERIV_TO_Y, s);
+    if (err == cudaSuccess) err = apply_derivative(h, x, yd, s);
     if (err == cudaSuccess) {
       k_delay_dots<<<G, kThreads, 0, s>>>(data, yf, yd, nD, S, part);
       k_delay_update<<<1, kThreads, 0, s>>>(part, G, S, q.start_time, q.dtau_min);

@@ -848,6 +848,80 @@ __global__ void __launch_bounds__(256) k_tc_fwd_reduce(const float2 *__restrict_
   }
 }
 
+// Derivative mode (kspha_dt), array_operator.jl:187-235:
+//   (B x)[s,c] = scale sum_v e^{i phi} 2 pi i (sum_l bf[v,l] kdot[l,s]) Z[v,c]
+//              = 2 pi i sum_l kdot[l,s] (E (bf_l . x))[s,c]
+// so B x is formed from forward products of the 128-wide instance, each
+// carrying 64 virtual coils cv = lt*CP + c: TP = 64/CP terms (l = l0 + lt)
+// times the CP real coils.  One pass's B operand: Z[v, cv] = bf[v, l] x[perm[v]]
+// csm[v][c] (zero for l >= nTerm or c >= nCha).  One thread per 16-byte unit.
+__global__ void k_tc_bop_deriv(const float2 *__restrict__ x, const int *__restrict__ perm,
+                               const float2 *__restrict__ csm, const float *__restrict__ bfraw,
+                               uint16_t *__restrict__ Bop, int nChunks, int nChaPad, int nCha, int CP, int l0,
+                               int nTerm) {
+  pdl_wait();
+  pdl_trigger();
+  constexpr int ND = 128;
+  const int units = ND * (TK / 8);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nChunks * units) return;
+  const int ch = (int)(i / units), u = (int)(i % units);
+  int n, kg;
+  bop_unit(u, n, kg);
+  const int cv = n / 2, q = n & 1, c = cv % CP, l = l0 + cv / CP;
+  const bool on = l < nTerm && c < nCha;
+  float v[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int vx = ch * TV + kg * 4 + j;
+    float2 z = make_float2(0.f, 0.f);
+    const int g = perm[vx];
+    if (on && g >= 0) {
+      const float2 xv = x[g], cw = csm[(int64_t)vx * nChaPad + c];
+      const float b = bfraw[(int64_t)vx * kRF + l];
+      z = make_float2(b * (xv.x * cw.x - xv.y * cw.y), b * (xv.x * cw.y + xv.y * cw.x));
+    }
+    bop_fwd_pair(z, q, v + 2 * j);
+  }
+  const int64_t per = (int64_t)ND * TK;
+  store_bop8(Bop + (size_t)ch * 2 * per, per, u, v);
+}
+
+// One derivative pass: y[c*nSam + s] (+)= scale2pi * i * sum_{lt < TP}
+// kdot[s][l0 + lt] * (sum over the written slots of part[.][s][lt*CP + c]).
+// The first pass writes y, later passes add to it (fixed order).
+__global__ void k_tc_deriv_reduce(const float2 *__restrict__ part, int nSamPad, int nSam, int nCha, int CP, int l0,
+                                  int TP, int nTerm, const float *__restrict__ kdot, float scale2pi, SlotMap m,
+                                  float2 *__restrict__ y, int accumulate) {
+  pdl_wait();
+  pdl_trigger();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nSamPad * CP) return;
+  const int s = (int)(i / CP), c = (int)(i % CP);
+  if (s >= nSam || c >= nCha) return;
+  const int ns = m.slots(s / TM);
+  float rr = 0.f, ri = 0.f;
+  for (int lt = 0; lt < TP && l0 + lt < nTerm; ++lt) {
+    float ar = 0.f, ai = 0.f;
+    for (int k = 0; k < ns; ++k) {
+      const float2 v = part[((int64_t)k * nSamPad + s) * 64 + lt * CP + c];
+      ar += v.x;
+      ai += v.y;
+    }
+    const float kd = kdot[(int64_t)s * kRF + l0 + lt];
+    rr = fmaf(kd, ar, rr);
+    ri = fmaf(kd, ai, ri);
+  }
+  const int64_t o = (int64_t)c * nSam + s;
+  float2 out = make_float2(-scale2pi * ri, scale2pi * rr);   // i * (rr + i ri)
+  if (accumulate) {
+    const float2 old = y[o];
+    out.x += old.x;
+    out.y += old.y;
+  }
+  y[o] = out;
+}
+
 // Adjoint reduction over the written slots: conj(csm), sum over coils,
 // scale, scatter into the full grid; the threads after the voxels' write
 // zeros to the grid points outside the mask.  L = min(nChaPad,
@@ -1055,6 +1129,7 @@ cudaError_t tc_prepare(hoe_handle *h) {
 
 void tc_release(hoe_handle *h) {
   if (h->tc.buf) cudaFree(h->tc.buf);
+  if (h->tc_host && ((TcBuffers *)h->tc_host)->memD) cudaFree(((TcBuffers *)h->tc_host)->memD);
   delete (TcBuffers *)h->tc_host;
   h->tc_host = nullptr;
   h->tc = TcState();
@@ -1243,6 +1318,65 @@ cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, floa
   if (e == cudaSuccess) e = reduce_forward(h, b, single_map_forward(h, b), nullptr, D, true, st);
   if (e == cudaSuccess) e = contract_adjoint(h, b, st);
   if (e == cudaSuccess) e = reduce_adjoint(h, b, single_map_adjoint(h, b), out, st);
+  return e;
+}
+
+bool tc_derivative_supported(const hoe_handle *h) { return h->tc.ready && h->t.hasKdot; }
+
+// B x in derivative mode: ceil(nTerm / TP) passes of the 128-wide instance,
+// TP = 64 / CP terms of CP = nChaTC coils each (k_tc_bop_deriv,
+// k_tc_deriv_reduce).  tc_derivative_prepare allocates the pass buffers
+// once; the delay search calls it before its graph capture.
+cudaError_t tc_derivative_prepare(hoe_handle *h) {
+  TcBuffers &b = *(TcBuffers *)h->tc_host;
+  const auto &t = h->t;
+  const int chunks = t.nVoxPad / TV;
+  constexpr int ND = 128;
+  if (!b.memD) {
+    const int bps = configure_kernel<1>(t.KP, ND);
+    if (bps < 1) return cudaErrorInvalidConfiguration;
+    b.gridD = (int)std::min<int64_t>((int64_t)h->numSMs * bps, (int64_t)t.nSt * chunks);
+    b.slotsD = max_slots(t.nSt, chunks, b.gridD);
+    const size_t bopB = (size_t)chunks * 2 * ND * TK * 2, partB = (size_t)b.slotsD * t.nSamPad * 64 * sizeof(float2);
+    b.bytesD = (bopB + 255) / 256 * 256 + partB;
+    cudaError_t e = cudaMalloc(&b.memD, b.bytesD);
+    if (e != cudaSuccess) { b.memD = nullptr; return e; }
+    b.bopD = (uint16_t *)b.memD;
+    b.partD = (float2 *)((unsigned char *)b.memD + (bopB + 255) / 256 * 256);
+    h->bytes += (int64_t)b.bytesD;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t tc_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st) {
+  cudaError_t e = tc_derivative_prepare(h);
+  if (e != cudaSuccess) return e;
+  const TcBuffers &b = *(const TcBuffers *)h->tc_host;
+  const auto &t = h->t;
+  const int chunks = t.nVoxPad / TV;
+  constexpr int ND = 128;
+  const int CP = b.nChaTC, TP = 64 / CP, passes = (t.nTerm + TP - 1) / TP;
+  TcSlice sl = slice_forward(h, b);
+  sl.Bop = b.bopD;
+  sl.part = b.partD;
+  TcParams<1> p = single_params(h, b, sl);
+  p.nChaPad = 64;   // the slots' row stride: 64 virtual coils
+  p.nChaTC = 64;
+  const SlotMap m = slot_map(0, chunks, (int64_t)t.nSt * chunks, b.gridD);
+  const float scale2pi = (float)(2.0 * 3.14159265358979323846 / sqrt((double)t.nVox));
+  const int64_t nU = (int64_t)chunks * ND * (TK / 8), nR = (int64_t)t.nSamPad * CP;
+  for (int q = 0; q < passes && e == cudaSuccess; ++q) {
+    const int l0 = q * TP;
+    e = launch_pdl(k_tc_bop_deriv, dim3((unsigned)((nU + 255) / 256)), dim3(256), 0, st, x, (const int *)t.perm,
+                   (const float2 *)t.csm, (const float *)t.bfraw, b.bopD, chunks, t.nChaPad, t.nCha, CP, l0,
+                   t.nTerm);
+    if (e == cudaSuccess) e = launch(h, p, t.KP, ND, b.gridD, st);
+    if (e == cudaSuccess)
+      e = launch_pdl(k_tc_deriv_reduce, dim3((unsigned)((nR + 255) / 256)), dim3(256), 0, st,
+                     (const float2 *)b.partD, t.nSamPad, t.nSam, t.nCha, CP, l0, TP, t.nTerm,
+                     (const float *)t.kdot, scale2pi, m, y, q > 0 ? 1 : 0);
+    h->launches += 2;
+  }
   return e;
 }
 

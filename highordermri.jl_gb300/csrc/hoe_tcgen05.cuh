@@ -23,6 +23,13 @@ struct TcBuffers {
   int N = 0, nChaTC = 0;
   int gridF = 1, gridA = 1, slotsF = 1, slotsA = 1;
   size_t bopFElems = 0, bopAElems = 0, partElems = 0;
+  // derivative passes (kspha_dt mode), allocated on first use: the 128-wide
+  // B operand of 64 virtual coils and its partial slots
+  uint16_t *bopD = nullptr;
+  float2 *partD = nullptr;
+  void *memD = nullptr;
+  size_t bytesD = 0;
+  int gridD = 1, slotsD = 1;
 };
 
 namespace {

@@ -296,6 +296,34 @@ def test_derivative_mode_vs_oracle():
     assert dense.rel(bg, bo) < 1e-5
 
 
+DERIV_CASES = [
+    dict(shape=(11, 10, 1), nSam=260, nCha=4, nTerm=16, conc=True),   # one pass of 16 terms
+    dict(shape=(12, 11, 1), nSam=300, nCha=8, nTerm=9),               # 8 terms, then 1
+    dict(shape=(10, 12, 1), nSam=700, nCha=16, nTerm=16),             # four passes of 4 terms
+    dict(shape=(9, 13, 1), nSam=333, nCha=20, nTerm=9),               # 32-coil padding, 5 passes
+]
+
+
+@pytest.mark.parametrize("case", DERIV_CASES, ids=lambda c: f"{c['nCha']}c-{c['nTerm']}t")
+def test_tc_derivative_vs_oracle(case):
+    # the tensor-core derivative: B x = 2 pi i sum_l kdot[l,s] E(bf_l . x)
+    # (array_operator.jl:187-235) from virtual-coil forward passes
+    if not have_tc():
+        pytest.skip("tensor-core engine unavailable")
+    w = workloads.small(seed=11, **case)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kspha_dt=w.kspha_dt, engine="tc", **w.op_kwargs())
+    op32 = HighOrderExplicitOp(w.grid, w.kspha, w.times, kspha_dt=w.kspha_dt, engine="fp32", **w.op_kwargs())
+    bf, k, t, f, c, idx = workloads.prepared_model(w, derivative=True)
+    bo = oracle.derivative(oracle.Model(bf, k, t, f, c), w.kspha_dt, w.x[idx])
+    bg = host(op * dev(w.x))
+    assert dense.rel(bg, bo) < 1e-4, dense.rel(bg, bo)
+    assert dense.rel(bg, host(op32 * dev(w.x))) < 1e-4
+    assert np.array_equal(host(op * dev(w.x)), bg)   # fixed reduction order
+    op.check()
+    op32.close()
+    op.close()
+
+
 # relative L2 tolerances of the backward vs the FP64 oracle's analytic gradient
 BWD_TOL = {"fp32": 1e-4, "tc": 1e-3}
 

@@ -119,7 +119,7 @@ def test_set_kspha_matches_a_new_operator(engine):
     from hoexplicit import _lib
     yd = torch.empty(op.nrow, dtype=torch.complex64, device="cuda")
     _lib.check(_lib.load().hoe_derivative(op._handle(), x.data_ptr(), yd.data_ptr(), op._stream()), op._h)
-    assert rel(yd.cpu().numpy(), oracle.derivative(m2, w2.kspha_dt, w.x[idx])) < 1e-5
+    assert rel(yd.cpu().numpy(), oracle.derivative(m2, w2.kspha_dt, w.x[idx])) < tol
     op.check()
     op.close()
     ref.close()
