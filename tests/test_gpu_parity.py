@@ -324,6 +324,33 @@ def test_tc_derivative_vs_oracle(case):
     op.close()
 
 
+def test_tc_derivative_config2_full_size():
+    # B x at 200x200 / 12,000 samples / 16 coils / 16 terms (4 passes): FP64
+    # spot check on sampled rows, agreement with the FP32 engine, linearity,
+    # bitwise repeatability
+    maybe_skip("tc")
+    w = workloads.config2()
+    kw = dict(kspha_dt=w.kspha_dt, **w.op_kwargs())
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **kw)
+    rng = np.random.default_rng(13)
+    x = dev(w.x)
+    bnp = host(op * x)
+    bf, k, t, f, c, idx = workloads.prepared_model(w, derivative=True)
+    rows = np.sort(rng.choice(w.nSam, 48, replace=False))
+    m = oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=w.kspha.shape[0])
+    bo = oracle.derivative(m, np.asarray(w.kspha_dt)[:, rows], w.x[idx])
+    assert dense.rel(bnp.reshape(w.nCha, w.nSam)[:, rows].reshape(-1), bo) < 1e-4
+    op32 = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **kw)
+    assert dense.rel(bnp, host(op32 * x)) < 1e-4
+    x2 = dev(rng.standard_normal(op.ncol) + 1j * rng.standard_normal(op.ncol))
+    a, b = 0.6 + 0.3j, -1.1 + 0.2j
+    assert dense.rel(host(op * (a * x + b * x2)), a * bnp + b * host(op * x2)) < 1e-4
+    assert np.array_equal(host(op * x), bnp)
+    op.check()
+    op32.close()
+    op.close()
+
+
 # relative L2 tolerances of the backward vs the FP64 oracle's analytic gradient
 BWD_TOL = {"fp32": 1e-4, "tc": 1e-3}
 
