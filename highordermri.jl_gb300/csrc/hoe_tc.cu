@@ -855,12 +855,13 @@ __global__ void __launch_bounds__(256) k_tc_fwd_reduce(const float2 *__restrict_
 //              = 2 pi i sum_l kdot[l,s] (E (bf_l . x))[s,c]
 // so B x is formed from forward products of the 128-wide instance, each
 // carrying 64 virtual coils cv = lt*CP + c: TP = 64/CP terms (l = l0 + lt)
-// times the CP real coils.  One pass's B operand: Z[v, cv] = bf[v, l] x[perm[v]]
-// csm[v][c] (zero for l >= nTerm or c >= nCha).  One thread per 16-byte unit.
+// times the CP = nCha real coils (columns cv >= TP*CP stay zero).  One pass's
+// B operand: Z[v, cv] = bf[v, l] x[perm[v]] csm[v][c] (zero for lt >= TP,
+// l >= nTerm or c >= nCha).  One thread per 16-byte unit.
 __global__ void k_tc_bop_deriv(const float2 *__restrict__ x, const int *__restrict__ perm,
                                const float2 *__restrict__ csm, const float *__restrict__ bfraw,
-                               uint16_t *__restrict__ Bop, int nChunks, int nChaPad, int nCha, int CP, int l0,
-                               int nTerm) {
+                               uint16_t *__restrict__ Bop, int nChunks, int nChaPad, int nCha, int CP, int TP,
+                               int l0, int nTerm) {
   pdl_wait();
   pdl_trigger();
   constexpr int ND = 128;
@@ -870,8 +871,8 @@ __global__ void k_tc_bop_deriv(const float2 *__restrict__ x, const int *__restri
   const int ch = (int)(i / units), u = (int)(i % units);
   int n, kg;
   bop_unit(u, n, kg);
-  const int cv = n / 2, q = n & 1, c = cv % CP, l = l0 + cv / CP;
-  const bool on = l < nTerm && c < nCha;
+  const int cv = n / 2, q = n & 1, c = cv % CP, lt = cv / CP, l = l0 + lt;
+  const bool on = lt < TP && l < nTerm && c < nCha;
   float v[8];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -1326,7 +1327,7 @@ cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, floa
 bool tc_derivative_supported(const hoe_handle *h) { return h->tc.ready && h->t.hasKdot; }
 
 // B x in derivative mode: ceil(nTerm / TP) passes of the 128-wide instance,
-// TP = 64 / CP terms of CP = nChaTC coils each (k_tc_bop_deriv,
+// TP = 64 / CP terms of CP = nCha coils each (k_tc_bop_deriv,
 // k_tc_deriv_reduce).  tc_derivative_prepare allocates the pass buffers
 // once; the delay search calls it before its graph capture.
 cudaError_t tc_derivative_prepare(hoe_handle *h) {
@@ -1357,7 +1358,7 @@ cudaError_t tc_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_
   const auto &t = h->t;
   const int chunks = t.nVoxPad / TV;
   constexpr int ND = 128;
-  const int CP = b.nChaTC, TP = 64 / CP, passes = (t.nTerm + TP - 1) / TP;
+  const int CP = t.nCha, TP = 64 / CP, passes = (t.nTerm + TP - 1) / TP;
   TcSlice sl = slice_forward(h, b);
   sl.Bop = b.bopD;
   sl.part = b.partD;
@@ -1370,8 +1371,8 @@ cudaError_t tc_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_
   for (int q = 0; q < passes && e == cudaSuccess; ++q) {
     const int l0 = q * TP;
     e = launch_pdl(k_tc_bop_deriv, dim3((unsigned)((nU + 255) / 256)), dim3(256), 0, st, x, (const int *)t.perm,
-                   (const float2 *)t.csm, (const float *)t.bfraw, b.bopD, chunks, t.nChaPad, t.nCha, CP, l0,
-                   t.nTerm);
+                   (const float2 *)t.csm, (const float *)t.bfraw, b.bopD, chunks, t.nChaPad, t.nCha, CP, TP,
+                   l0, t.nTerm);
     if (e == cudaSuccess) e = launch(h, p, t.KP, ND, b.gridD, st);
     if (e == cudaSuccess)
       e = launch_pdl(k_tc_deriv_reduce, dim3((unsigned)((nR + 255) / 256)), dim3(256), 0, st,

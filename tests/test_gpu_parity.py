@@ -300,7 +300,8 @@ DERIV_CASES = [
     dict(shape=(11, 10, 1), nSam=260, nCha=4, nTerm=16, conc=True),   # one pass of 16 terms
     dict(shape=(12, 11, 1), nSam=300, nCha=8, nTerm=9),               # 8 terms, then 1
     dict(shape=(10, 12, 1), nSam=700, nCha=16, nTerm=16),             # four passes of 4 terms
-    dict(shape=(9, 13, 1), nSam=333, nCha=20, nTerm=9),               # 32-coil padding, 5 passes
+    dict(shape=(9, 13, 1), nSam=333, nCha=20, nTerm=9),               # 3 terms of 20 coils per pass
+    dict(shape=(10, 10, 1), nSam=280, nCha=10, nTerm=16),             # 6, 6, then 4 terms of 10 coils
 ]
 
 
