@@ -46,6 +46,14 @@ namespace hoe {
 constexpr int kTileS = 128;   // samples per sample tile (phase anchors, SIMT CTA rows)
 constexpr int kTileV = 128;   // voxels per voxel tile
 constexpr int kRF = 24;       // stored width of the raw basis / kspha_dt rows
+// Largest residual phase bound (cycles) the tensor-core engine accepts.  Its
+// phase is formed on the tensor cores (TF32 split products, FP32
+// accumulation) and goes to the FP32 sincos without a further reduction, so
+// its error grows with the magnitude of the residual: measured on GB300 at
+// 5.6e-6 (relative L2 vs FP64) up to 79 cycles and 1.3e-5 at 308 cycles.
+// Above this bound the engine refuses the plan and AUTO takes the FP32
+// engine, whose phase is range-reduced before every sincos.
+constexpr double kTcMaxPhaseBound = 1024.0;
 
 struct Tables {
   // sizes

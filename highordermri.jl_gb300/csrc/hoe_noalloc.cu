@@ -206,13 +206,25 @@ int hoe_forward_noalloc(const hoe_raw_model *m, const void *x_dev, void *y_dev, 
                         "ceil(nSam/128)*128 * nChaPad exceeds the static scratch of 2^21 "
                         "complex partial sums (for example nSam*nCha <= 2,097,152 with nCha a "
                         "multiple of 16)");
+  // an error left by earlier work on this thread is reported as such, not as
+  // a failure of this call's launches
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) {
+    char buf[200];
+    snprintf(buf, sizeof(buf), "an earlier CUDA error is pending on this thread (%s)", cudaGetErrorString(e));
+    return noalloc_fail(HOE_ERR_CUDA, buf);
+  }
   int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 64) return noalloc_fail(HOE_ERR_CUDA, "no current device");
   void *scratch = nullptr;
   {
     // one-time set-up per device, on the first call with that device current:
-    // the device address of the static scratch and the kernels' shared-memory limit
+    // the device address of the static scratch and the kernels' shared-memory
+    // limit.  With lazy module loading (the CUDA default) this first call is
+    // also what loads the module, and with it the static scratch, onto the
+    // device.  The cached address is not refreshed: after cudaDeviceReset
+    // this entry point must not be used again in the process.
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_scratch_ptr[dev]) {
       void *ptr = nullptr;
@@ -232,7 +244,8 @@ int hoe_forward_noalloc(const hoe_raw_model *m, const void *x_dev, void *y_dev, 
     scratch = g_scratch_ptr[dev];
   }
   int numSMs = 0;
-  cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return noalloc_fail(HOE_ERR_CUDA, cudaGetErrorString(e));
   const int nChunks = (m->nVox + kT - 1) / kT;
   const int nCC = nChaPad <= 8 ? 1 : nChaPad / 16;
   int maxSplit = (int)(kScratchElems / perSplit);
@@ -255,6 +268,8 @@ int hoe_forward_noalloc(const hoe_raw_model *m, const void *x_dev, void *y_dev, 
   else if (nChaPad == 8) HOE_NOALLOC(8);
   else HOE_NOALLOC(16);
 #undef HOE_NOALLOC
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return noalloc_fail(HOE_ERR_CUDA, cudaGetErrorString(e));
   int64_t n = (int64_t)m->nSam * m->nCha;
   k_reduce_noalloc<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(
       part, nSplit, nSamPad, nChaPad, m->nSam, m->nCha, (float)(1.0 / sqrt((double)m->nVox)),

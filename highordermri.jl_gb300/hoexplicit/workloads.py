@@ -272,6 +272,53 @@ def spiral_slice(seed, n: int, nSam: int, nCha: int = 16, d: float = 1e-3, dwell
                     kspha_dt=np.gradient(kspha, dwell, axis=1))
 
 
+def volume3d(seed: int = 1006, shape=(64, 64, 32), d: float = 3.125e-3, parts: int = 8,
+             per: int = 1024, nCha: int = 8, frac: float = 0.5, df_peak: float = 300.0,
+             dwell: float = 2e-6) -> Workload:
+    """3-D volume (default 64x64x32 at 3.125 mm) read by a stack of spirals:
+    ``parts`` kz partitions (R = nZ/parts along z) of ``per`` samples each.
+    Zeroth/second/third-order coefficients are smooth polynomials scaled to
+    ``frac`` x the peak linear phase (as in the 64x64 spiral workload, whose
+    factor is 0.5); the fieldmap is a sum of 3-D Gaussians scaled to
+    +-``df_peak`` Hz; ring coils.  A large volume with strong higher orders
+    is the shape with the largest phase per (sample, voxel) pair."""
+    rng = np.random.default_rng(seed)
+    nX, nY, nZ = shape
+    grid = Grid(nX, nY, nZ, d, d, d)
+    fovx, fovz = nX * d, nZ * d
+    kmax = 1.0 / (2 * d)
+    u = np.arange(per) / (per - 1)
+    turns = fovx * kmax / 2
+    kxy, kz, t = [], [], []
+    for pz in range(parts):
+        kxy.append(kmax * u * np.exp(1j * (2 * np.pi * turns * u + 2 * np.pi * pz / parts)))
+        kz.append(np.full(per, (pz - parts / 2 + 0.5) * 2 * kmax / parts))
+        t.append(np.arange(per) * dwell)
+    kxy = np.concatenate(kxy)
+    kspha = np.zeros((16, kxy.size))
+    kspha[1], kspha[2], kspha[3] = kxy.real, kxy.imag, np.concatenate(kz)
+    t = np.concatenate(t)
+    mask = np.ones(nX * nY * nZ, dtype=bool)
+    lin_peak = kmax * np.max(np.sqrt(grid.x ** 2 + grid.y ** 2 + grid.z ** 2))
+    _higher_orders(rng, grid, mask, kspha, t, lin_peak, frac=frac)
+    xs = grid.x / max(np.max(np.abs(grid.x)), 1e-30)
+    ys = grid.y / max(np.max(np.abs(grid.y)), 1e-30)
+    zs = grid.z / max(np.max(np.abs(grid.z)), 1e-30)
+    fm = np.zeros(xs.size)
+    for _ in range(4):
+        cx, cy, cz = rng.uniform(-0.6, 0.6, 3)
+        wd = rng.uniform(0.2, 0.5)
+        fm += rng.uniform(-1, 1) * np.exp(-((xs - cx) ** 2 + (ys - cy) ** 2 + (zs - cz) ** 2) / (2 * wd * wd))
+    fm *= df_peak / max(np.max(np.abs(fm)), 1e-30)
+    csm = _ring_coils(rng, grid, nCha, fovx)
+    x = _ellipse_phantom(rng, grid) * (np.abs(zs) <= 0.9)
+    sh = (nX, nY, nZ)
+    return Workload(f"vol3d-{nX}x{nY}x{nZ}-{kxy.size}s-{nCha}c-16t-f{frac:g}", grid, kspha, t,
+                    fm.reshape(sh, order="F"), csm.reshape(sh + (nCha,), order="F"),
+                    mask.reshape(sh, order="F"), x, dwell=dwell,
+                    kspha_dt=np.gradient(kspha, dwell, axis=1))
+
+
 def config5(seed: int = 1005, slices: int = 24, nCha: int = 16):
     """24 slices of 160^2-224^2 voxels (steps of 8) with 8,000-20,000 samples
     each (uneven), 16 coils: a list of Workloads."""

@@ -100,7 +100,9 @@ extern "C" {
 #define HOE_ENGINE_FP32_SIMT  0  /* plain FP32 CUDA-core direct kernel              */
 #define HOE_ENGINE_TC_BF16X3  1  /* tcgen05 tensor cores, split-BF16 3-product, FP32 accumulate */
 #define HOE_ENGINE_AUTO       2  /* hoe_create / hoe_set_engine: the tensor-core engine where the device
-                                    and coil count allow it, else FP32; hoe_get_info reports the choice */
+                                    (sm_103), the coil count (<= 64) and the plan's residual phase bound
+                                    (<= 1024 cycles, hoe_info.residual_phase_bound) allow it, else FP32;
+                                    hoe_get_info reports the choice */
 
 /* hoe_backward flags */
 #define HOE_GRAD_KSPHA     1     /* write dL/dkspha                                   */
@@ -380,7 +382,13 @@ HOE_API int  hoe_batch_check(hoe_batch *b, void *stream);
  *
  * The first call on a device, with that device current, looks up the
  * scratch's device address (cudaGetSymbolAddress) and sets the kernels'
- * shared-memory limit.  Make that first call before any stream capture.
+ * shared-memory limit.  Under lazy module loading (the CUDA default) that
+ * first call is also when the CUDA runtime loads this library's device
+ * code onto the device and allocates the 16 MiB static array, so a caller
+ * that must not allocate later should make the first call during its own
+ * set-up, and before any stream capture.  The address is looked up once per
+ * device and not refreshed: do not call this entry point again after
+ * cudaDeviceReset in the same process.
  * All calls share the one scratch array, and each call overwrites every
  * slot it reads, so nothing has to be cleared between calls.  Calls whose
  * work overlaps on the GPU (other streams, other threads) race on the

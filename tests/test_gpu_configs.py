@@ -1,0 +1,271 @@
+"""Full-size parity of the benchmark workloads that the per-kernel tests do not
+reach: the 200x200 EPI with eddy-current terms, the gradient problem on the
+64x64 spiral operator, and the FP64 check of the tensor-core backward at
+200x200 / 12,000 samples / 16 coils.
+
+The 200x200 products are checked whole against the FP64 oracle (about 2 s
+per product on 16 host cores).  Beside that each test uses properties that do
+not depend on size (adjoint identity, linearity, bitwise repeatability,
+agreement between engines) and FP64 oracle checks on sampled rows, sampled
+voxels or sampled gradient entries where a whole FP64 product would be slow.
+
+Tolerances (relative L2 vs FP64): 1e-5 for the plain FP32 engine and 1e-4 for
+the tensor-core engine on products; 1e-4 (FP32 engine) and 1e-3 (tensor-core
+engine) for gradients against the oracle's analytic FP64 gradient; 1e-3 for
+every gradient against central FP64 finite differences at a step of 1e-3
+relative.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from hoexplicit import HighOrderExplicitOp, normalOperator, workloads  # noqa: E402
+from oracle import dense, oracle  # noqa: E402
+from tests.test_gpu_parity import ENGINE_PARAMS, TOL, dev, have_tc, host, maybe_skip  # noqa: E402
+
+BWD_TOL = {"fp32": 1e-4, "tc": 1e-3}
+FD_TOL = 1e-3
+
+
+def _noise(rng, n, scale):
+    return scale * (rng.standard_normal(n) + 1j * rng.standard_normal(n))
+
+
+def _voxel_adjoint_fp64(bf, k, t, f, c, y, vox, nVox):
+    """E^H y in FP64 on a subset of the masked voxels.  The oracle normalises
+    by the square root of its own voxel count, so the subset result is
+    rescaled to the full operator's 1/sqrt(nVox)."""
+    m = oracle.Model(bf[vox], k, t, f[vox], c[vox], nTerm=16)
+    return oracle.adjoint(m, y) * np.sqrt(len(vox) / nVox)
+
+
+@pytest.fixture(scope="module")
+def cfg3():
+    """The EPI workload with its whole FP64 forward and adjoint (about 2 s
+    each with the oracle on 16 cores)."""
+    w = workloads.config3()
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=16)
+    y64 = oracle.forward(m, w.x[idx])
+    rng = np.random.default_rng(31)
+    y = y64 + _noise(rng, y64.size, 0.05 * np.linalg.norm(y64) / np.sqrt(y64.size))
+    x64 = oracle.scatter(oracle.adjoint(m, y), np.asarray(w.mask).reshape(-1, order="F"))
+    return w, y64, y, x64
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_config3_full_size_properties(engine, cfg3):
+    # 200x200 blipped EPI, 50 lines x (200 + ramps) = 12,000 samples, 2.5 us
+    # dwell, 16 coils, eddy-current exponentials on all 16 coefficients:
+    # whole products against FP64, agreement between engines, adjoint
+    # identity, linearity, bitwise repeatability, normal operator
+    maybe_skip(engine)
+    w, y64, y, x64 = cfg3
+    assert w.nSam == 12000 and w.nCha == 16 and w.nVox == 40000
+    tol = TOL[engine]
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine=engine, **w.op_kwargs())
+    rng = np.random.default_rng(32)
+    x = dev(w.x)
+    ynp = host(op * x)
+    assert dense.rel(ynp, y64) < tol, dense.rel(ynp, y64)
+    xa = host(op.H * dev(y))
+    assert dense.rel(xa, x64) < tol, dense.rel(xa, x64)
+    assert np.all(xa[~np.asarray(w.mask).reshape(-1, order="F")] == 0)
+    # the two engines agree on every element
+    if engine == "tc" or have_tc():
+        other = HighOrderExplicitOp(w.grid, w.kspha, w.times,
+                                    engine="fp32" if engine == "tc" else "tc", **w.op_kwargs())
+        assert dense.rel(ynp, host(other * x)) < 1e-4
+        assert dense.rel(xa, host(other.H * dev(y))) < 1e-4
+        other.close()
+    # adjoint identity <y, E x> = <E^H y, x>
+    lhs, rhs = np.vdot(y, ynp), np.vdot(xa, w.x)
+    assert abs(lhs - rhs) / (np.linalg.norm(ynp) * np.linalg.norm(y)) < 1e-5
+    # linearity
+    x2 = rng.standard_normal(op.ncol) + 1j * rng.standard_normal(op.ncol)
+    a, b = 0.8 + 0.1j, -0.9 + 0.5j
+    assert dense.rel(host(op * dev(a * w.x + b * x2)), a * ynp + b * host(op * dev(x2))) < 1e-5
+    # bitwise repeatability (fixed reduction order)
+    assert np.array_equal(host(op * x), ynp)
+    assert np.array_equal(host(op.H * dev(y)), xa)
+    # normal operator E^H D E against E^H (D * E x)
+    D = np.tile(0.05 + rng.random(w.nSam), w.nCha)
+    assert dense.rel(host(normalOperator(op, D) * x), host(op.H * dev(D * ynp))) < 1e-4
+    op.check()
+    op.close()
+
+
+def test_tc_large_residual_phase_bound():
+    # a 64x64x32 volume (stack of spirals, 8,192 samples, 8 coils) whose
+    # second/third-order coefficients reach 32x the peak linear phase and a
+    # +-300 Hz fieldmap: the residual phase bound is ~300 cycles (~1,900 rad),
+    # ten times the 200x200 spiral's, and the tensor-core phase still meets
+    # 1e-4 against FP64 on sampled rows and voxels
+    maybe_skip("tc")
+    w = workloads.volume3d(frac=32.0)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    assert 250 < op.info()["residual_phase_bound"] < 1024
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    rng = np.random.default_rng(3)
+    ynp = host(op * dev(w.x))
+    rows = np.sort(rng.choice(w.nSam, 32, replace=False))
+    yo = oracle.forward(oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=16), w.x[idx])
+    assert dense.rel(ynp.reshape(w.nCha, w.nSam)[:, rows].reshape(-1), yo) < TOL["tc"]
+    vox = np.sort(rng.choice(w.nVox, 128, replace=False))
+    xo = _voxel_adjoint_fp64(bf, k, t, f, c, ynp, vox, w.nVox)
+    assert dense.rel(host(op.H * dev(ynp))[idx[vox]], xo) < TOL["tc"]
+    op.check()
+    op.close()
+
+
+def test_plans_above_the_tensor_core_phase_bound_use_fp32():
+    # a residual phase bound just above 1,024 cycles (a 32x32x16 volume whose
+    # higher orders reach 80x the peak linear phase): the tensor-core engine
+    # refuses the plan and the default engine choice takes the FP32 engine.
+    # The FP32 engine forms its residual phase in FP32 too, so its own error
+    # grows with the bound (measured 7.5e-6 at 934 cycles, 6.7e-5 at 5,549):
+    # just above the guard it is held to 2e-5
+    from hoexplicit import ArgumentError
+    from hoexplicit.operator import plan
+    w = workloads.volume3d(frac=80.0, shape=(32, 32, 16), parts=4, per=512)
+    assert 1024 < plan(w.grid, w.kspha, w.times, **w.op_kwargs())["residual_phase_bound"] < 1200
+    with pytest.raises(ArgumentError):
+        HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, **w.op_kwargs())
+    assert op.engine == "fp32"
+    with pytest.raises(ArgumentError):
+        op.set_engine("tc")
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    y64 = oracle.forward(oracle.Model(bf, k, t, f, c, nTerm=16), w.x[idx])
+    assert dense.rel(host(op * dev(w.x)), y64) < 2e-5
+    op.close()
+
+
+def _config4_problem():
+    """The 64x64 / 4,096-sample / 8-coil spiral operator with data made from
+    perturbed coefficients: kspha + 2% seeded smooth noise per row, and the
+    whole coefficient and B0 time base delayed by t0 = 3.7 us."""
+    w = workloads.config1()
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    rng = np.random.default_rng(1004)
+    nT, nS = k.shape
+    u = np.arange(nS) / (nS - 1)
+    noise = np.zeros_like(k)
+    for l in range(nT):
+        p = np.polynomial.polynomial.polyval(u, rng.standard_normal(6))
+        noise[l] = 0.02 * p / np.max(np.abs(p)) * np.max(np.abs(k[l]))
+    t0 = 3.7e-6
+    kp = np.stack([np.interp(t - t0, t, k[l] + noise[l]) for l in range(nT)])
+    y = oracle.forward(oracle.Model(bf, kp, t - t0, f, c), w.x[idx])
+    return w, (bf, k, t, f, c, idx), y, rng, t0
+
+
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_config4_gradients(engine):
+    # loss = 1/2 ||E(kspha, fieldmap, t0) x - y||^2 at the nominal model, with
+    # y from perturbed coefficients and a 3.7 us delay; dL/dt0 covers both
+    # parts: -fieldmap (B0 term) and -sum_l bf_l kdot_l (coefficient time base)
+    maybe_skip(engine)
+    w, (bf, k, t, f, c, idx), y, rng, t0 = _config4_problem()
+    kd = np.asarray(w.kspha_dt)
+    m = oracle.Model(bf, k, t, f, c)
+    xm = w.x[idx]
+    r = oracle.forward(m, xm) - y
+    dk_o, ddf_o, t0b, t0c = oracle.backward(m, xm, r, kd)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=kd, engine=engine, **w.op_kwargs())
+    # the GPU gradient from the GPU residual, and from the FP64 residual
+    rg = op * dev(w.x) - dev(y)
+    assert dense.rel(host(rg), r) < TOL[engine]
+    dk, ddf, dt0 = op.backward(dev(w.x), dev(r), t0_coef=True)
+    dk = dk.cpu().numpy().astype(np.float64)
+    ddf = ddf.cpu().numpy().astype(np.float64)
+    dt0 = dt0.item()
+    tol = BWD_TOL[engine]
+    assert dense.rel(dk, dk_o) < tol
+    assert dense.rel(ddf[idx], ddf_o) < tol
+    assert abs(dt0 - (t0b + t0c)) <= tol * abs(t0b + t0c)
+    # shapes quoted for the gradient: 16 x nSam coefficients, the image grid
+    assert dk.shape == (16, w.nSam) and ddf.shape == (w.x.size,)
+
+    # central FP64 finite differences, step 1e-3 relative, on a seeded subset
+    def loss(kk, ff, tz):
+        mm = oracle.Model(bf, kk - tz * kd, t - tz, ff, c)
+        rr = oracle.forward(mm, xm) - y
+        return 0.5 * np.vdot(rr, rr).real
+
+    checked = 0
+    for l in range(16):
+        # one sample per coefficient row, among the row's larger gradients
+        top = np.argsort(np.abs(dk_o[l]))[-200:]
+        s = int(rng.choice(top))
+        if k[l, s] == 0:
+            continue
+        h = 1e-3 * abs(k[l, s])
+        a, b = k.copy(), k.copy()
+        a[l, s] += h
+        b[l, s] -= h
+        fd = (loss(a, f, 0.0) - loss(b, f, 0.0)) / (2 * h)
+        assert abs(dk[l, s] - fd) <= FD_TOL * abs(fd), (l, s, dk[l, s], fd)
+        checked += 1
+    # a 2-D slice: the basis functions with a z factor vanish, their
+    # coefficient rows are zero and so are their gradients
+    assert checked == 10
+    zero = np.flatnonzero(np.all(bf[:, :16] == 0, axis=0))
+    assert len(zero) == 6 and np.all(np.abs(dk[zero]) <= 1e-6 * np.max(np.abs(dk)))
+    live = np.flatnonzero((np.abs(xm) > 0) & (np.abs(f) > 1.0))
+    for v in rng.choice(live, 6, replace=False):
+        h = 1e-3 * abs(f[v])
+        a, b = f.copy(), f.copy()
+        a[v] += h
+        b[v] -= h
+        fd = (loss(k, a, 0.0) - loss(k, b, 0.0)) / (2 * h)
+        assert abs(ddf[idx[v]] - fd) <= FD_TOL * abs(fd), (v, ddf[idx[v]], fd)
+    h = 1e-3 * t0
+    fd = (loss(k, f, h) - loss(k, f, -h)) / (2 * h)
+    assert abs(dt0 - fd) <= FD_TOL * abs(fd), (dt0, fd)
+    # directional derivative along a smooth seeded direction of all coefficients
+    d = np.zeros_like(k)
+    u = np.arange(w.nSam) / (w.nSam - 1)
+    for l in range(16):
+        p = np.polynomial.polynomial.polyval(u, rng.standard_normal(6))
+        d[l] = p / np.max(np.abs(p)) * np.max(np.abs(k[l]))
+    eps = 1e-3
+    fd = (loss(k + eps * d, f, 0.0) - loss(k - eps * d, f, 0.0)) / (2 * eps)
+    assert abs(np.sum(dk * d) - fd) <= FD_TOL * abs(fd)
+    op.check()
+    op.close()
+
+
+def test_config2_tc_backward_vs_fp64():
+    # tensor-core backward at 200x200 / 12,000 samples / 16 coils / 20 terms:
+    # dL/dkspha on 48 sampled sample columns (each a sum over all 40,000
+    # voxels) and dL/dfieldmap on 256 sampled voxels (each a sum over all
+    # samples) against the FP64 oracle given the same residual
+    maybe_skip("tc")
+    w = workloads.config2()
+    kd = np.asarray(w.kspha_dt)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, kdot=kd, engine="tc", **w.op_kwargs())
+    rng = np.random.default_rng(22)
+    x = dev(w.x)
+    y0 = host(op * x)
+    r = 0.03 * y0 + _noise(rng, y0.size, 0.01 * np.linalg.norm(y0) / np.sqrt(y0.size))
+    dk, ddf, dt0 = op.backward(x, dev(r), t0_coef=True)
+    dk = dk.cpu().numpy().astype(np.float64)
+    ddf = ddf.cpu().numpy().astype(np.float64)
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    xm = w.x[idx]
+    cols = np.sort(rng.choice(w.nSam, 48, replace=False))
+    rcols = r.reshape(w.nCha, w.nSam)[:, cols].reshape(-1)
+    m = oracle.Model(bf, k[:, cols], t[cols], f, c, nTerm=16)
+    dk_o, _, _, _ = oracle.backward(m, xm, rcols)
+    assert dense.rel(dk[:, cols], dk_o) < BWD_TOL["tc"], dense.rel(dk[:, cols], dk_o)
+    vox = np.sort(rng.choice(w.nVox, 256, replace=False))
+    mv = oracle.Model(bf[vox], k, t, f[vox], c[vox], nTerm=16)
+    _, ddf_o, _, _ = oracle.backward(mv, xm[vox], r)
+    ddf_o *= np.sqrt(len(vox) / w.nVox)   # the oracle normalises by its own voxel count
+    assert dense.rel(ddf[idx[vox]], ddf_o) < BWD_TOL["tc"], dense.rel(ddf[idx[vox]], ddf_o)
+    assert np.isfinite(dt0.item())
+    op.check()
+    op.close()
