@@ -41,19 +41,50 @@ METRIC = "E+E^H voxel·samples/s, TC vs plain FP32 on GB300 at <=1e-4 rel err vs
 UNIT = "voxel·samples/s"
 L2_FLUSH_BYTES = 256 << 20
 
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
-# the dominant kernels, from one `ncu --set full` capture of this command on
-# the 200x200 / 12,000-sample / 16-coil workload (profiles/tc_engine_cfg2.md,
-# profiles/simt_engine_cfg2.md).  Other workloads report None.
-NCU_TRAFFIC_BYTES = {
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "forward"): 138_284_032 + 4_328_448,
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "tc", "adjoint"): 138_284_032 + 4_328_448,
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "forward"): 40_267_776 + 25_856,
-    ("cfg2-vdspiral-200x200-12000s-16c-16t+conc", "fp32", "adjoint"): 36_679_424 + 11_776,
+# Per-launch ncu figures of the dominant kernels (DRAM bytes read + written,
+# warp instructions issued) come from a committed capture summary,
+# profiles/ncu_figures.txt, which records a hash of the kernel sources it was
+# taken on.  A figure is used only when that hash equals the hash of the
+# sources in this tree; otherwise the bench reports null and says why.
+KERNEL_SOURCES = {
+    "tc": ("hoe_tc.cu", "hoe_tcgen05.cuh", "hoe_internal.cuh", "hoe_api.cu"),
+    "fp32": ("hoe_simt.cu", "hoe_internal.cuh", "hoe_api.cu"),
 }
-# Warp instructions issued by one tensor-core contraction launch at the
-# 200x200 spiral workload (ncu smsp__inst_executed.sum, same capture).
-NCU_TC_WARP_INST = {"cfg2-vdspiral-200x200-12000s-16c-16t+conc": 201_034_673}
+NCU_FIGURES = ROOT / "profiles" / "ncu_figures.txt"
+
+
+def kernel_source_hash(engine: str) -> str:
+    """sha256 (first 16 hex digits) of the sources the engine's contraction
+    kernel and its tables are built from."""
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES[engine]:
+        h.update(name.encode())
+        h.update((PKG / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def ncu_figure(kind: str, workload_name: str, engine: str, direction: str):
+    """(value, provenance) of one committed ncu figure: kind 'traffic' (DRAM
+    bytes per launch) or 'inst' (warp instructions per launch).  value is
+    None when no capture of these sources exists."""
+    want = kernel_source_hash(engine)
+    seen = None
+    try:
+        lines = NCU_FIGURES.read_text().splitlines()
+    except OSError:
+        return None, "no committed ncu capture"
+    for ln in lines:
+        f = ln.split()
+        if len(f) == 6 and f[0] == kind and f[1] == workload_name and f[2] == engine and f[3] == direction:
+            if f[5] == want:
+                return int(f[4]), f"ncu capture of kernel sources {want}"
+            seen = f[5]
+    if seen:
+        return None, f"stale: the committed capture is of kernel sources {seen}, this tree is {want}"
+    return None, "no committed ncu capture for this workload"
+
+
 # Cycles a converged warp's elected lane waits per tcgen05.mma issued back to
 # back (kind::f16, M = 128, N = 64, A from TMEM), measured in isolation on
 # this GPU (N = 32: 32 cycles).
@@ -89,6 +120,12 @@ def workload(cfg: str):
     from hoexplicit import workloads
     return {"1": workloads.config1, "2": workloads.config2, "3": workloads.config3,
             "5": lambda: workloads.config5()[0]}[cfg]()
+
+
+def workload_config(w, nTermEff: int) -> dict:
+    """The config dict of the JSON line, the same in both arms."""
+    return {"workload": w.name, "nVox": w.nVox, "nSam": w.nSam, "nCha": w.nCha, "nTermEff": int(nTermEff),
+            "l2": "GPU arm: L2 flushed between timed steps (256 MiB write)"}
 
 
 def dist_env():
@@ -585,8 +622,9 @@ def run_gb300(a):
     flops_per_launch = 8.0 * w.nCha * w.nVox * w.nSam
     achieved = flops_per_launch / (dom_ms / 1e3) / 1e12
     bf16_peak, hbm_peak, peak_src = measured_peaks()
+    traffic, traffic_src = ncu_figure("traffic", w.name, engine, dom)
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved / bf16_peak, "traffic": NCU_TRAFFIC_BYTES.get((w.name, engine, dom)),
+                "frac": achieved / bf16_peak, "traffic": traffic, "traffic_source": traffic_src,
                 "kernel": f"{engine} {dom} contraction", "peak_source": f"bf16_tflops ({peak_src}, burst)",
                 "kernel_ms": dom_ms, "flops_per_launch": flops_per_launch,
                 "frac_of_split_peak": achieved / (bf16_peak / 3.0) if engine == "tc" else None,
@@ -610,7 +648,7 @@ def run_gb300(a):
         t_mma = stages * mma_busiest * MMA_ISSUE_CYCLES / hz
         t_pipe = stages * pipe_cycles / hz
         t_sfu = 2.0 * w.nVox * w.nSam / (16.0 * nsm * hz)
-        inst = NCU_TC_WARP_INST.get(w.name)
+        inst, inst_src = ncu_figure("inst", w.name, engine, dom)
         t_issue = inst / (4.0 * nsm * hz) if inst else None
         dom_s = dom_ms / 1e3
         roofline["ceilings"] = [
@@ -618,7 +656,7 @@ def run_gb300(a):
              "note": "2 MUFU ops per (voxel, sample), 16 per clock per SM"},
             {"pipe": "warp instruction issue", "ms": t_issue * 1e3 if t_issue else None,
              "frac": t_issue / dom_s if t_issue else None,
-             "note": "ncu warp instructions of one launch / (4 per clock per SM)"},
+             "note": f"ncu warp instructions of one launch / (4 per clock per SM); {inst_src}"},
             {"pipe": "tensor pipe (all MMAs)", "ms": t_pipe * 1e3, "frac": t_pipe / dom_s,
              "note": f"{pipe_cycles} cycles per 64-column stage: contraction (3 BF16 products, "
                      f"{mma_contract} MMAs) + {mma_resid} TF32 residual-phase MMAs, {stages} stages per SM"},
@@ -642,11 +680,10 @@ def run_gb300(a):
            "scaling": "weak", "vs_baseline": None,
            "dtype": "bf16x3/f32-acc" if engine == "tc" else "f32",
            "data": "synthetic (seeded, shapes/distributions of the named configuration)",
-           "config": {"workload": w.name, "nVox": w.nVox, "nSam": w.nSam, "nCha": w.nCha,
-                      "nTermEff": info["nTermEff"], "engine": engine, "parallelism": f"replicas x{ws}",
-                      "l2": "flushed between timed steps (256 MiB write)",
-                      "residual_phase_bound_cycles": info["residual_phase_bound"],
-                      "residual_rank": info["residual_rank"]},
+           "config": workload_config(w, info["nTermEff"]),
+           "parallelism": f"replicas x{ws}",
+           "plan": {"engine": engine, "residual_phase_bound_cycles": info["residual_phase_bound"],
+                    "residual_rank": info["residual_rank"], "residual_width": info["residual_width"]},
            "roofline": roofline, "clocks": clk.summary(),
            "gpu_launches": int(r["launches"]),
            "kernel_ms": {"forward": fk, "adjoint": ak}}
@@ -785,7 +822,7 @@ def run_reference(a):
            "steps": a.steps, "warmup": a.warmup, "ms_per_step": s * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic (seeded, shapes/distributions of the named configuration)",
-           "config": {"workload": w.name, "nVox": w.nVox, "nSam": w.nSam, "nCha": w.nCha},
+           "config": workload_config(w, k.shape[0]),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
                             "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
