@@ -17,10 +17,14 @@ from ._lib import ArgumentError, DimensionMismatch
 
 @dataclass
 class Grid:
-    """Centred Cartesian grid (src/Grid/Grid.jl:116-128, constructor :163-194).
+    """Centred Cartesian grid (src/Grid/Grid.jl:18-30, constructor :65-96).
 
     ``r[j] = (j - (N+1)/2) * delta`` for 1-based j, x index fastest in the
-    flattened coordinate vectors, metres.
+    flattened coordinate vectors, metres.  As in the reference constructor,
+    ``exchange_xy`` swaps the x and y coordinate vectors and each
+    ``reverse_*`` reverses one flattened coordinate vector (Grid.jl:83-94);
+    neither permutes image, mask, field-map or coil arrays.  They apply only
+    when the coordinates are generated, not to explicit ``x``/``y``/``z``.
     """
 
     nX: int
@@ -32,6 +36,10 @@ class Grid:
     x: np.ndarray = field(default=None, repr=False)
     y: np.ndarray = field(default=None, repr=False)
     z: np.ndarray = field(default=None, repr=False)
+    exchange_xy: bool = field(default=False, repr=False)
+    reverse_x: bool = field(default=False, repr=False)
+    reverse_y: bool = field(default=False, repr=False)
+    reverse_z: bool = field(default=False, repr=False)
 
     def __post_init__(self):
         if self.x is None:
@@ -41,9 +49,14 @@ class Grid:
             ii = np.tile(i, self.nY * self.nZ)
             jj = np.tile(np.repeat(j, self.nX), self.nZ)
             kk = np.repeat(k, self.nX * self.nY)
-            self.x = (ii - (self.nX + 1) / 2.0) * self.dx
-            self.y = (jj - (self.nY + 1) / 2.0) * self.dy
-            self.z = (kk - (self.nZ + 1) / 2.0) * self.dz
+            x = (ii - (self.nX + 1) / 2.0) * self.dx
+            y = (jj - (self.nY + 1) / 2.0) * self.dy
+            z = (kk - (self.nZ + 1) / 2.0) * self.dz
+            if self.exchange_xy:
+                x, y = y, x
+            self.x = x[::-1].copy() if self.reverse_x else x
+            self.y = y[::-1].copy() if self.reverse_y else y
+            self.z = z[::-1].copy() if self.reverse_z else z
 
     @property
     def matrixSize(self):
@@ -54,7 +67,7 @@ class Grid:
         return (self.dx, self.dy, self.dz)
 
     def struct_to_dict(self):
-        """Dictionary round trip of Grid.jl:196-209."""
+        """Dictionary form of Grid.jl:98-111."""
         return {"schema_version": 1, "nX": self.nX, "nY": self.nY, "nZ": self.nZ,
                 "delta_x": self.dx, "delta_y": self.dy, "delta_z": self.dz,
                 "x": np.asarray(self.x), "y": np.asarray(self.y), "z": np.asarray(self.z),
@@ -63,7 +76,7 @@ class Grid:
 
     @classmethod
     def from_dict(cls, d):
-        """Restore from ``struct_to_dict`` output (Grid.jl:224-250)."""
+        """Restore from ``struct_to_dict`` output (Grid.jl:126-152)."""
         s = lambda v: np.asarray(v).reshape(-1)[0].item() if np.ndim(v) else v
         return cls(int(s(d["nX"])), int(s(d["nY"])), int(s(d["nZ"])), float(s(d["delta_x"])),
                    float(s(d["delta_y"])), float(s(d["delta_z"])),
@@ -129,8 +142,20 @@ def prep_kspha(kspha, k_nominal, nTerm: int, recon_terms=None):
     """Order selection of prep_kspha.jl:1-56; returns a modified copy.
 
     A '0' digit zeroes its order, except first order, whose rows 2:4 are
-    replaced by ``k_nominal``.
+    replaced by ``k_nominal``.  Three-dimensional coefficients
+    ``(nTerm, nSam, nDyn)`` with ``k_nominal`` ``(3, nSam, nDyn)`` are
+    prepared as one ``(nTerm, nSam*nDyn)`` matrix in column-major order and
+    reshaped back (prep_kspha.jl:59-73).
     """
+    kspha = np.asarray(kspha)
+    if kspha.ndim == 3:
+        nT, nSam, nDyn = kspha.shape
+        kn = np.asarray(k_nominal, dtype=np.float64)
+        if kn.size != 3 * nSam * nDyn:
+            raise DimensionMismatch(f"k_nominal must have size (3, {nSam}, {nDyn}), got {kn.shape}")
+        flat = prep_kspha(kspha.reshape(nT, nSam * nDyn, order="F"),
+                          kn.reshape(3, nSam * nDyn, order="F"), nTerm, recon_terms)
+        return flat.reshape(nT, nSam, nDyn, order="F")
     if recon_terms is None:
         recon_terms = "111" if nTerm == 9 else "1111"
     expected = 3 if nTerm == 9 else (4 if nTerm == 16 else 0)
@@ -161,8 +186,12 @@ def prep_concomitant(bf, kspha, x, y, z, concomitant=None):
     c = np.asarray(concomitant)
     if np.iscomplexobj(c) or not np.issubdtype(c.dtype, np.number):
         raise ArgumentError("concomitant must be a real array or nothing")
-    if c.shape != (4, kspha.shape[1]):
-        raise DimensionMismatch(f"concomitant must have size {(4, kspha.shape[1])}, got {c.shape}")
+    kspha = np.asarray(kspha)
+    dims = (4,) + kspha.shape[1:]
+    # a (4, nSam) matrix also serves coefficients (nTerm, nSam, 1) (prep_kspha.jl:89-92)
+    single = kspha.ndim == 3 and kspha.shape[2] == 1 and c.shape == dims[:2]
+    if c.shape != dims and not single:
+        raise DimensionMismatch(f"concomitant must have size {dims}, got {c.shape}")
     bf_c = np.stack([z ** 2, x ** 2 + y ** 2, x * z, y * z], axis=1)
     return (np.asfortranarray(np.hstack([bf, bf_c])),
-            np.vstack([kspha, c.astype(np.float64)]))
+            np.concatenate([kspha, c.astype(np.float64).reshape(dims, order="F")], axis=0))

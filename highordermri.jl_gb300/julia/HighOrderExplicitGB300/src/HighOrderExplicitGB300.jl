@@ -82,6 +82,7 @@ mutable struct GB300ExplicitOp{T,F,G} <: HighOrderExplicitOp{Complex{T}}
     nCha::Int
     nTermEff::Int
     derivative::Bool
+    has_kdot::Bool
 end
 
 LinearOperators.storage_type(op::GB300ExplicitOp) = typeof(op.Mv)
@@ -115,8 +116,8 @@ end
 
 """
     GB300ExplicitOp(grid, kspha, times; fieldmap, csm, mask, concomitant=nothing,
-        recon_terms=nothing, k_nominal=kspha[2:4,:], kspha_dt=nothing, gpus=nothing,
-        engine=:auto)
+        recon_terms=nothing, k_nominal=kspha[2:4,:], kspha_dt=nothing, kdot=nothing,
+        gpus=nothing, engine=:auto)
 
 The `:gb300` implementation of `HighOrderExplicitOp` (see
 HighOrderExplicitOp.jl:44-51).  `engine=:tc` uses the tcgen05 tensor-core
@@ -124,12 +125,16 @@ contraction (split-BF16, FP32 accumulation), `engine=:fp32` the plain FP32
 CUDA-core kernel, `engine=:auto` the tensor cores where the device and the
 coil count (at most 64) allow them, else the FP32 kernel.  With `kspha_dt` the forward product evaluates the
 derivative `B x` of the reference's kspha_dt mode and concomitant terms are
-ignored (array_operator.jl:139, 159-166).
+ignored (array_operator.jl:139, 159-166).  `kdot` (the same shape as `kspha`)
+supplies dkspha/dt for the coefficient part of the t0 gradient without
+switching the product to the derivative.  A plan whose residual phase bound
+exceeds 1024 cycles runs on the FP32 kernel (`engine=:auto`) or is refused
+(`engine=:tc`).
 """
 function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::AbstractVector{T};
     fieldmap=zeros(T, grid.matrixSize...), csm=ones(Complex{T}, grid.matrixSize..., 1),
     mask=trues(grid.matrixSize...), concomitant=nothing, recon_terms=nothing,
-    k_nominal=kspha[2:4, :], kspha_dt=nothing, gpus=nothing, engine::Symbol=:auto,
+    k_nominal=kspha[2:4, :], kspha_dt=nothing, kdot=nothing, gpus=nothing, engine::Symbol=:auto,
 ) where {T<:AbstractFloat}
     if gpus !== nothing
         ids = Int.(collect(gpus))
@@ -150,6 +155,8 @@ function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::Abstrac
     nVox > 0 || throw(ArgumentError("mask must contain voxels"))
     derivative = kspha_dt !== nothing
     derivative && size(kspha_dt) != size(kspha) && throw(ArgumentError("kspha_dt must have same size as kspha"))
+    kd = derivative ? kspha_dt : kdot
+    kd !== nothing && size(kd) != size(kspha) && throw(ArgumentError("kspha_dt must have same size as kspha"))
 
     prepared = prep_kspha(kspha, k_nominal, nTerm; recon_terms)
     bf = basisfunc_spha(grid.x[indices], grid.y[indices], grid.z[indices], collect(1:nTerm))
@@ -161,7 +168,7 @@ function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::Abstrac
     f64 = Vector{Float64}(vec(fieldmap)[indices])
     c128 = Matrix{ComplexF64}(reshape(csm, :, nCha)[indices, :])
     idx32 = Int32.(indices .- 1)
-    kd64 = derivative ? Matrix{Float64}(kspha_dt) : nothing
+    kd64 = kd === nothing ? nothing : Matrix{Float64}(kd)
     dev = CUDA.device()
     handle = Ref{Ptr{Cvoid}}(C_NULL)
     GC.@preserve bf64 k64 t64 f64 c128 idx32 kd64 begin
@@ -179,7 +186,7 @@ function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::Abstrac
     op = GB300ExplicitOp{Float32,typeof(prodf),typeof(ctprodf)}(
         nSam * nCha, prod(grid.matrixSize), false, false, prodf, nothing, ctprodf, 0, 0, 0,
         CUDA.zeros(ComplexF32, 0), CUDA.zeros(ComplexF32, 0), handle[], dev, nSam, nCha,
-        size(k64, 1), derivative)
+        size(k64, 1), derivative, kd !== nothing)
     finalizer(o -> ccall((:hoe_free, libhoe), Cvoid, (Ptr{Cvoid},), o.handle), op)
     return op
 end
@@ -232,7 +239,7 @@ Gradient of `0.5*norm(op*x - y)^2` given the residual `r = op*x - y`
 (nTermEff, nSam), dfieldmap::CuVector{Float32} (full grid, zero outside the
 mask), dt0::Float64)`.  The same call is the pullback of `x -> op*x` for the
 phase parameters when `r` is the output cotangent.  `t0_coef` needs
-`kspha_dt` at construction.  With `engine=:tc` (or `:auto` on a GB300) the
+`kspha_dt` or `kdot` at construction.  With `engine=:tc` (or `:auto` on a GB300) the
 gradient is formed on the tensor cores for up to 16 coils with residual widths
 up to 24 and up to 32 coils with widths up to 16, else on the FP32 kernel (up to
 16 coils).
@@ -252,20 +259,35 @@ function explicit_backward(op::GB300ExplicitOp, x, r; kspha=true, fieldmap=true,
 end
 
 """
-    encode(op, x) = op * x
+    encode(op, kspha, fieldmap, t0, x) = op * x
 
-Differentiable application: the `rrule` returns the cotangents of the phase
-model (kspha, fieldmap, t0) computed by the backward kernel, and `op' * ȳ`
-for `x`.
+Differentiable application for phase-model refinement (coefficient and
+field-map synchronisation).  `kspha` (nTermEff x nSam: the coefficients the
+operator applies, after order selection, with the concomitant rows appended),
+`fieldmap` (Hz, the grid's shape) and `t0` (s; 0 for the operator as built)
+name the model that `op` was built with.  They are not read again: the
+operator holds its own copy, and a changed model needs a new operator or
+`hoe_set_kspha`.  They are arguments so that the pullback can return their
+cotangents beside the one of `x`.
+
+For a real loss L of `y = op * x`, ChainRulesCore's cotangent of a complex
+output is ȳ = ∂L/∂Re(y) + i ∂L/∂Im(y) (for L = ½‖y - d‖² it is y - d).  The
+pullback returns, for `op` nothing (`NoTangent`), then
+- kspha:    Re Σ conj(ȳ) ∂y/∂kspha   (nTermEff x nSam, Float32)
+- fieldmap: Re Σ conj(ȳ) ∂y/∂fieldmap (reshaped to `size(fieldmap)`, zero outside the mask)
+- t0:       Re Σ conj(ȳ) ∂y/∂t0 with ∂φ/∂t0 = -fieldmap - Σ_l bf_l kdot_l, the
+            coefficient part only when the operator was built with `kdot`
+- x:        op' * ȳ
+These are the gradients of hoe_backward with ȳ in the place of the residual.
 """
-encode(op::GB300ExplicitOp, x) = op * x
+encode(op::GB300ExplicitOp, kspha, fieldmap, t0, x) = op * x
 
-function ChainRulesCore.rrule(::typeof(encode), op::GB300ExplicitOp, x)
+function ChainRulesCore.rrule(::typeof(encode), op::GB300ExplicitOp, kspha, fieldmap, t0, x)
     y = op * x
     function encode_pullback(ȳ)
         ybar = CuArray{ComplexF32}(unthunk(ȳ))
-        dk, ddf, dt0 = explicit_backward(op, x, ybar)
-        return NoTangent(), Tangent{typeof(op)}(; kspha=dk, fieldmap=ddf, t0=dt0), op' * ybar
+        dk, ddf, dt0 = explicit_backward(op, x, ybar; t0_coef=op.has_kdot)
+        return NoTangent(), NoTangent(), dk, reshape(ddf, size(fieldmap)), dt0, op' * ybar
     end
     return y, encode_pullback
 end

@@ -23,7 +23,7 @@ def reference_basis(x: float, y: float, z: float):
 
 
 def grid_coordinates(nX, nY, nZ, dx, dy, dz):
-    """Centred coordinates, x index fastest (Grid.jl:176-180), as flat vectors."""
+    """Centred coordinates, x index fastest (Grid.jl:78-82), as flat vectors."""
     i = np.arange(1, nX + 1)
     j = np.arange(1, nY + 1)
     k = np.arange(1, nZ + 1)

@@ -7,7 +7,7 @@
  * and bench.py (cpu_baseline / --impl reference) may load it.
  *
  * Followed reference code (paths inside HighOrderMRI.jl):
- *   oracle_grid          src/Grid/Grid.jl:163-194 (r_j = (j-(N+1)/2)*delta, x fastest)
+ *   oracle_grid          src/Grid/Grid.jl:65-96 (r_j = (j-(N+1)/2)*delta, x fastest)
  *   oracle_basis         src/SphericalHarmonics/basisfunction.jl:27-126 (terms 1-17)
  *   oracle_forward       src/EncodingOperator/Explicit/array_operator.jl:241-288
  *                        (sample blocks of nSam/nBlock plus a remainder block,
@@ -52,7 +52,7 @@ void oracle_set_threads(int n) {
 #endif
 }
 
-/* Grid.jl:176-180: centred coordinates, x index fastest. */
+/* Grid.jl:78-82: centred coordinates, x index fastest. */
 void oracle_grid(int64_t nX, int64_t nY, int64_t nZ, double dx, double dy, double dz,
                  double *x, double *y, double *z) {
   for (int64_t k = 0; k < nZ; ++k)

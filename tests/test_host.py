@@ -17,6 +17,44 @@ def test_grid_matches_oracle_and_roundtrips():
     assert g2.matrixSize == g.matrixSize and np.array_equal(g2.x, g.x)
 
 
+def test_grid_orientation_keywords():
+    # Grid.jl:83-94: exchange_xy swaps the coordinate vectors, reverse_*
+    # reverses one flattened vector; sizes and spacings are unchanged
+    g = Grid(5, 4, 3, 0.7, 0.9, 1.2)
+    e = Grid(5, 4, 3, 0.7, 0.9, 1.2, exchange_xy=True)
+    assert np.array_equal(e.x, g.y) and np.array_equal(e.y, g.x) and np.array_equal(e.z, g.z)
+    r = Grid(5, 4, 3, 0.7, 0.9, 1.2, reverse_x=True, reverse_z=True)
+    assert np.array_equal(r.x, g.x[::-1]) and np.array_equal(r.y, g.y) and np.array_equal(r.z, g.z[::-1])
+    b = Grid(5, 4, 3, 0.7, 0.9, 1.2, exchange_xy=True, reverse_y=True)
+    assert np.array_equal(b.y, g.x[::-1]) and np.array_equal(b.x, g.y)
+    assert b.matrixSize == (5, 4, 3) and b.resolution == (0.7, 0.9, 1.2)
+
+
+def test_prep_kspha_three_dimensional():
+    # prep_kspha.jl:59-73: (nTerm, nSam, nDyn) coefficients are prepared as
+    # one column-major (nTerm, nSam*nDyn) matrix; each dynamic equals the
+    # two-dimensional preparation of its own slab
+    rng = np.random.default_rng(8)
+    k = rng.standard_normal((16, 11, 3))
+    kn = rng.standard_normal((3, 11, 3))
+    out = prep_kspha(k, kn, 16, "0101")
+    assert out.shape == k.shape
+    for d in range(3):
+        assert np.array_equal(out[:, :, d], prep_kspha(k[:, :, d], kn[:, :, d], 16, "0101"))
+    with pytest.raises(DimensionMismatch):
+        prep_kspha(k, kn[:, :, :2], 16, None)
+    # concomitant rows for 3-D coefficients: (4, nSam, nDyn), or (4, nSam) for one dynamic
+    x, y, z = rng.standard_normal((3, 6))
+    bf = rng.standard_normal((6, 16))
+    c = rng.standard_normal((4, 11, 3))
+    b2, k2 = prep_concomitant(bf, out, x, y, z, c)
+    assert b2.shape == (6, 20) and k2.shape == (20, 11, 3) and np.array_equal(k2[16:], c)
+    b1, k1 = prep_concomitant(bf, out[:, :, :1], x, y, z, c[:, :, 0])
+    assert k1.shape == (20, 11, 1) and np.array_equal(k1[16:, :, 0], c[:, :, 0])
+    with pytest.raises(DimensionMismatch):
+        prep_concomitant(bf, out, x, y, z, c[:, :, 0])
+
+
 def test_basis_matches_oracle():
     rng = np.random.default_rng(1)
     x, y, z = rng.standard_normal((3, 40))

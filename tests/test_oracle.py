@@ -28,7 +28,7 @@ def test_basis_terms_match_dense_restatement():
 
 
 def test_grid_coordinates():
-    # Grid.jl:176-180: (j - (N+1)/2) * delta, x fastest
+    # Grid.jl:78-82: (j - (N+1)/2) * delta, x fastest
     x, y, z = oracle.grid(4, 3, 2, 0.7, 0.9, 1.2)
     xd, yd, zd = dense.grid_coordinates(4, 3, 2, 0.7, 0.9, 1.2)
     assert np.array_equal(x, xd) and np.array_equal(y, yd) and np.array_equal(z, zd)
