@@ -516,7 +516,8 @@ def time_extras(w, x, reps=10):
         yd = torch.empty(opd.nrow, dtype=torch.complex64, device=x.device)
         ms = timed_ms(lambda: opd.prod_(yd, x))
         out["derivative"] = {"ms_per_call": ms, "value": w.nVox * w.nSam / (ms / 1e3), "unit": UNIT,
-                             "engine": "tc (virtual-coil passes)" if opd.engine == "tc" else "fp32 (CUDA cores)"}
+                             "engine": ("tc (one pass: phase tile scaled by 2 pi i F, F on the CUDA cores)" if opd.nCha <= 16
+                                        else "tc (virtual-coil passes)") if opd.engine == "tc" else "fp32 (CUDA cores)"}
         opd.close()
     dt = float(w.times[1] - w.times[0])
     traj = torch.from_numpy(np.ascontiguousarray(w.kspha.T)).cuda()          # (nSam, nTerm) float64

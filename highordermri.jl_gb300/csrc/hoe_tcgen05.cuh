@@ -23,10 +23,14 @@ struct TcBuffers {
   int N = 0, nChaTC = 0;
   int gridF = 1, gridA = 1, slotsF = 1, slotsA = 1;
   size_t bopFElems = 0, bopAElems = 0, partElems = 0;
-  // derivative passes (kspha_dt mode), allocated on first use: the 128-wide
-  // B operand of 64 virtual coils and its partial slots
+  // derivative product (kspha_dt mode), allocated on first use.  Up to 16
+  // coils one pass (fusedD): basis tiles bfT and 2 pi kdot per sample kd1; above, the
+  // 128-wide B operand of 64 virtual coils and its partial slots per pass
   uint16_t *bopD = nullptr;
   float2 *partD = nullptr;
+  float *bfT = nullptr;
+  float *kd1 = nullptr;
+  bool fusedD = false;
   void *memD = nullptr;
   size_t bytesD = 0;
   int gridD = 1, slotsD = 1;
@@ -232,6 +236,12 @@ __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *r) {
       : "r"(taddr));
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// 8 columns into registers without waiting: call tmem_wait_ld() before use.
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t *r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
 
 __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v) {
   uint32_t r[4];
@@ -274,6 +284,21 @@ __device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t &hi, uin
   asm("mov.b64 {%0, %1}, %2;" : "=f"(ra), "=f"(rb) : "l"(d));
   hi = hb;
   lo = pack_bf16(ra, rb);
+}
+
+// Packed FP32x2 arithmetic (two lanes of one 64-bit register pair).
+__device__ __forceinline__ uint64_t pack_f32x2(float a, float b) {
+  uint64_t v;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(a), "f"(b));
+  return v;
+}
+__device__ __forceinline__ void unpack_f32x2(uint64_t v, float &a, float &b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ uint64_t fma_f32x2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
 }
 
 // CTA that owns work item w when W items are split into G contiguous ranges

@@ -252,8 +252,11 @@ HOE_API int  hoe_adjoint(hoe_handle *h, const void *y_dev, void *x_dev, void *st
  * as in normalOperator; the device diagonal is used as given. */
 HOE_API int  hoe_normal(hoe_handle *h, const float *D_dev, const void *x_dev, void *out_dev, void *stream);
 /* B x of the kspha_dt mode: requires desc.kspha_dt (or hoe_set_kspha with
- * kspha_dt).  The tensor-core engine forms it from ceil(nTerm / (64 / padded
- * coils)) forward passes; the FP32 engine from one fused kernel. */
+ * kspha_dt).  The tensor-core engine forms it, up to 16 coils, in one pass of
+ * the forward contraction whose phase tile is scaled by 2 pi i F with
+ * F = sum_l kdot_l bf_l; above 16 coils from ceil(nTerm / (64 / padded
+ * coils)) forward passes of virtual coils.  The FP32 engine uses one fused
+ * kernel.  The first call allocates the engine's derivative buffers. */
 HOE_API int  hoe_derivative(hoe_handle *h, const void *x_dev, void *y_dev, void *stream);
 /* Gradient of L = 0.5*||E x - y||^2 given the residual r = E x - y.
  *   dk_dev   float [nTermEff x nSam] (same layout as kspha) or NULL
