@@ -263,10 +263,11 @@ int make_plan(const hoe_desc *d, Plan &P) {
     if (m > 0 && d->mask_idx[m] <= d->mask_idx[m - 1])
       return fail(nullptr, HOE_ERR_ARG, "mask indices must be strictly ascending");
   }
-  if (d->tile_samples != 0 && d->tile_samples != hoe::kTileS)
-    return fail(nullptr, HOE_ERR_ARG, "tile_samples must be 0 or %d", hoe::kTileS);
-  if (d->tile_voxels != 0 && d->tile_voxels != hoe::kTileV)
-    return fail(nullptr, HOE_ERR_ARG, "tile_voxels must be 0 or %d", hoe::kTileV);
+  if (d->tc_plan < 0 || d->tc_plan >= 5)
+    return fail(nullptr, HOE_ERR_ARG, "tc_plan must be in 0..4");
+  if (d->tc_plan > 0 && d->nCha > 16)
+    return fail(nullptr, HOE_ERR_ARG, "tensor-core plans 1-4 serve up to 16 coils");
+  if (d->reserved != 0) return fail(nullptr, HOE_ERR_ARG, "reserved must be 0");
 
   auto &t = P.t;
   t.nX = d->nX; t.nY = d->nY; t.nZ = d->nZ; t.nFull = (int)nFull;
@@ -594,6 +595,7 @@ int hoe_create(hoe_handle **out, const hoe_desc *d) {
     int sa = std::max(1, std::min(t.nSt, (target + t.nVt * nCC - 1) / (t.nVt * nCC)));
     tps = (t.nSt + sa - 1) / sa;
     h->splitA = (t.nSt + tps - 1) / tps;
+    h->tcPlan = d->tc_plan;
     if (d->split_hint > 0) {
       h->splitF = std::min(d->split_hint, t.nVt);
       h->splitA = std::min(d->split_hint, t.nSt);
@@ -701,6 +703,8 @@ int hoe_plan(const hoe_desc *d, hoe_info *o) {
   o->n_sample_tiles = t.nSt; o->n_voxel_tiles = t.nVt;
   o->residual_rank = t.rank; o->residual_width = t.Rp;
   o->residual_phase_bound = t.residBound;
+  o->tc_plan = d->tc_plan;
+  o->tc_plans = d->nCha <= 16 ? 5 : 1;
   return HOE_OK;
 }
 
@@ -732,6 +736,8 @@ int hoe_get_info(const hoe_handle *h, hoe_info *o) {
   o->residual_rank = t.rank; o->residual_width = t.Rp;
   o->residual_phase_bound = t.residBound;
   o->device_bytes = h->bytes + (int64_t)h->tc.bytes;
+  o->tc_plan = h->tc.ready ? hoe::tc_get_plan(h) : h->tcPlan;
+  o->tc_plans = t.nCha <= 16 ? 5 : 1;
   return HOE_OK;
 }
 
@@ -869,29 +875,41 @@ int hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *o, void *stream) 
   const int savedTiming = h->timing;
   h->timing = 0;
   const int defF = h->splitF, defA = h->splitA, defEngine = h->engine;
-  struct Cand { int engine, sf, sa; };
+  struct Cand { int engine, sf, sa, plan; };
   std::vector<Cand> cands;
   for (int div : {4, 2, 1}) {
-    Cand c{HOE_ENGINE_FP32_SIMT, std::max(1, defF / div), std::max(1, defA / div)};
+    Cand c{HOE_ENGINE_FP32_SIMT, std::max(1, defF / div), std::max(1, defA / div), -1};
     bool dup = false;
     for (auto &k : cands) dup = dup || (k.sf == c.sf && k.sa == c.sa);
     if (!dup) cands.push_back(c);
   }
   std::string why;
+  int defPlan = 0;
   if (hoe::tc_supported(h, &why)) {
     if (!h->tc.ready && e == cudaSuccess) {
       cudaError_t te = hoe::tc_prepare(h);
       if (te != cudaSuccess) cudaGetLastError();
     }
-    if (h->tc.ready) cands.push_back({HOE_ENGINE_TC_BF16X3, 0, 0});
+    if (h->tc.ready) {
+      defPlan = hoe::tc_get_plan(h);
+      for (int pl = 0; pl < hoe::tc_plan_count(h); ++pl) cands.push_back({HOE_ENGINE_TC_BF16X3, 0, 0, pl});
+    }
   }
   float best = INFINITY;
-  Cand bestC{defEngine, defF, defA};
+  Cand bestC{defEngine, defF, defA, defPlan};
+  float bestTc = INFINITY;
+  int bestPlan = defPlan;
   for (size_t i = 0; i < cands.size() && e == cudaSuccess && i < 8; ++i) {
     const Cand &c = cands[i];
     h->engine = c.engine;
     if (c.engine == HOE_ENGINE_FP32_SIMT) { h->splitF = c.sf; h->splitA = c.sa; }
-    else { h->splitF = defF; h->splitA = defA; }
+    else {
+      h->splitF = defF; h->splitA = defA;
+      if (hoe::tc_set_plan(h, c.plan) != cudaSuccess) {   // plan unavailable on this device
+        cudaGetLastError();
+        continue;
+      }
+    }
     auto run = [&]() {
       cudaError_t r = hoe::apply_forward(h, x, yo, st);
       if (r == cudaSuccess) r = hoe::apply_adjoint_weighted(h, y, nullptr, xo, st);
@@ -905,19 +923,30 @@ int hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *o, void *stream) 
     float ms = 0.f;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
     ms /= (float)reps;
-    o->cand_engine[i] = c.engine;
-    o->cand_split[i] = c.engine == HOE_ENGINE_FP32_SIMT ? c.sf : 0;
-    o->cand_ms[i] = ms;
-    o->candidates = (int)i + 1;
-    if (e == cudaSuccess && ms < best) { best = ms; bestC = {c.engine, h->splitF, h->splitA}; }
+    const int k = o->candidates;
+    o->cand_engine[k] = c.engine;
+    o->cand_split[k] = c.engine == HOE_ENGINE_FP32_SIMT ? c.sf : 0;
+    o->cand_plan[k] = c.plan;
+    o->cand_ms[k] = ms;
+    o->candidates = k + 1;
+    if (e == cudaSuccess && ms < best) { best = ms; bestC = {c.engine, h->splitF, h->splitA, c.plan}; }
+    if (e == cudaSuccess && c.engine == HOE_ENGINE_TC_BF16X3 && ms < bestTc) { bestTc = ms; bestPlan = c.plan; }
   }
+  for (int k = o->candidates; k < 8; ++k) o->cand_plan[k] = -1;
   h->engine = bestC.engine;
   h->splitF = bestC.sf;
   h->splitA = bestC.sa;
+  if (h->tc.ready) {
+    // the fastest tensor-core plan stays selected, also when the FP32 engine won
+    cudaError_t pe = hoe::tc_set_plan(h, bestPlan);
+    if (pe != cudaSuccess && e == cudaSuccess) e = pe;
+    h->tcPlan = bestPlan;
+  }
   h->timing = savedTiming;
   o->engine = h->engine;
   o->split_forward = h->splitF;
   o->split_adjoint = h->splitA;
+  o->tc_plan = h->tc.ready ? hoe::tc_get_plan(h) : h->tcPlan;
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaFree(x); cudaFree(xo); cudaFree(y); cudaFree(yo);

@@ -188,6 +188,7 @@ struct hoe_handle {
   int engine = HOE_ENGINE_FP32_SIMT;
   int numSMs = 0;
   int splitF = 1, splitA = 1;
+  int tcPlan = 0;                 // tensor-core execution plan requested at create (hoe_desc.tc_plan)
   int64_t bytes = 0;
   std::string err;
   hoe::Tables t;
@@ -315,6 +316,12 @@ cudaError_t tc_adjoint(const hoe_handle *h, const float2 *y, const float *D, flo
 cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, float2 *out, cudaStream_t st);
 // B x (kspha_dt mode) on the tensor cores, as forward passes over virtual
 // coils (term x coil); buffers on first use.
+// Execution plans of the contraction (hoe_autotune): count (5 up to 16
+// coils, else 1), current plan, selection (cudaErrorInvalidValue when out of
+// range).
+int tc_plan_count(const hoe_handle *h);
+int tc_get_plan(const hoe_handle *h);
+cudaError_t tc_set_plan(hoe_handle *h, int plan);
 bool tc_derivative_supported(const hoe_handle *h);
 cudaError_t tc_derivative_prepare(hoe_handle *h);
 cudaError_t tc_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_t st);

@@ -393,6 +393,7 @@ cudaError_t tc_prepare(hoe_handle *h) {
   h->tc_host = new TcBuffers(b);
   e = tc_anchor_tables(h, 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (e == cudaSuccess && h->tcPlan > 0) e = tc_set_plan(h, h->tcPlan);
   return e;
 }
 
@@ -536,10 +537,18 @@ int slots_needed(int64_t first, int rowTiles, int C, int64_t W, int G) {
 
 namespace {
 
+// A single operator's contraction with its execution plan (TcPlan; plans
+// above 0 exist for up to 16 coils, N <= 32).
+cudaError_t launch_planned(const hoe_handle *h, const TcBuffers &b, const TcParams<1> &p, int G, cudaStream_t st) {
+  if (b.plan == 0) return launch(h, p, h->t.KP, b.N, G, st);
+  return b.N == 16 ? tc_launch_plan16(h, p, h->t.KP, b.plan, G, st)
+                   : tc_launch_plan32(h, p, h->t.KP, b.plan, G, st);
+}
+
 cudaError_t contract_forward(const hoe_handle *h, const TcBuffers &b, cudaStream_t st) {
   const TcParams<1> p = single_params(h, b, slice_forward(h, b));
   trace(h, EV_FK0, st);
-  cudaError_t e = launch(h, p, h->t.KP, b.N, b.gridF, st);
+  cudaError_t e = launch_planned(h, b, p, b.gridF, st);
   trace(h, EV_FK1, st);
   return e;
 }
@@ -547,7 +556,7 @@ cudaError_t contract_forward(const hoe_handle *h, const TcBuffers &b, cudaStream
 cudaError_t contract_adjoint(const hoe_handle *h, const TcBuffers &b, cudaStream_t st) {
   const TcParams<1> p = single_params(h, b, slice_adjoint(h, b));
   trace(h, EV_AK0, st);
-  cudaError_t e = launch(h, p, h->t.KP, b.N, b.gridA, st);
+  cudaError_t e = launch_planned(h, b, p, b.gridA, st);
   trace(h, EV_AK1, st);
   return e;
 }
@@ -588,6 +597,26 @@ cudaError_t tc_normal(const hoe_handle *h, const float *D, const float2 *x, floa
   if (e == cudaSuccess) e = contract_adjoint(h, b, st);
   if (e == cudaSuccess) e = reduce_adjoint(h, b, single_map_adjoint(h, b), out, st);
   return e;
+}
+
+int tc_plan_count(const hoe_handle *h) {
+  return h->tc_host && ((const TcBuffers *)h->tc_host)->N <= 32 ? kTcPlans : 1;
+}
+
+int tc_get_plan(const hoe_handle *h) { return h->tc_host ? ((const TcBuffers *)h->tc_host)->plan : 0; }
+
+// Selects the contraction's execution plan for this operator's forward and
+// adjoint products (batches and the derivative product use plan 0); sets the
+// kernel's shared-memory limit on first use.
+cudaError_t tc_set_plan(hoe_handle *h, int plan) {
+  if (!h->tc_host || plan < 0 || plan >= tc_plan_count(h)) return cudaErrorInvalidValue;
+  TcBuffers &b = *(TcBuffers *)h->tc_host;
+  if (plan > 0) {
+    const int nb = b.N == 16 ? tc_configure_plan16(h->t.KP, plan) : tc_configure_plan32(h->t.KP, plan);
+    if (nb < 1) return cudaErrorInvalidConfiguration;
+  }
+  b.plan = plan;
+  return cudaSuccess;
 }
 
 bool tc_derivative_supported(const hoe_handle *h) { return h->tc.ready && h->t.hasKdot; }

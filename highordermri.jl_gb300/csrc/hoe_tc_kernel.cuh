@@ -60,9 +60,21 @@ namespace {
 //     residual-phase issuer's loop, the chain that sets the stage time.
 //   N >= 64: 2 groups of 8 (16 warps, 20 in all, 96 registers, which the
 //     wider accumulators need); a warp covers half of the columns.
-template <int N>
+// Execution plans of the contraction that hoe_autotune times on an operator,
+// for up to 16 coils (N <= 32); plan 0 is the default:
+//   1: two phase-warp groups (8 phase warps, 12 warps: more registers a thread)
+//   2: four phase-warp groups (16 phase warps, 20 warps, 96 registers)
+//   3: a stage ring of 4 (phase tiles in flight) instead of the deepest that fits
+//   4: accumulators flushed every 16 stages instead of 32
+template <int V> struct TcPlan { static constexpr int NG = 0, NS = 0, GROUP = 0; };
+template <> struct TcPlan<1> { static constexpr int NG = 2, NS = 0, GROUP = 0; };
+template <> struct TcPlan<2> { static constexpr int NG = 4, NS = 0, GROUP = 0; };
+template <> struct TcPlan<3> { static constexpr int NG = 0, NS = 4, GROUP = 0; };
+template <> struct TcPlan<4> { static constexpr int NG = 0, NS = 0, GROUP = 16; };
+
+template <int N, int V = 0>
 struct Warps {
-  static constexpr int NG = N <= 32 ? 3 : 2;
+  static constexpr int NG = TcPlan<V>::NG ? TcPlan<V>::NG : (N <= 32 ? 3 : 2);
   static constexpr int GW = N <= 32 ? 4 : 8;
   static constexpr int PW = NG * GW;
   static constexpr bool WIDE = GW == 4;
@@ -118,6 +130,13 @@ struct TcParams {
 constexpr int kBatchSlices = 32;
 static_assert(sizeof(TcParams<kBatchSlices>) <= 4096, "kernel parameter space");
 
+// Execution plans 1-4 for the autotuner (hoe_tc_plan16.cu, hoe_tc_plan32.cu).
+constexpr int kTcPlans = 5;
+cudaError_t tc_launch_plan16(const hoe_handle *h, const TcParams<1> &p, int KP, int plan, int G, cudaStream_t st);
+cudaError_t tc_launch_plan32(const hoe_handle *h, const TcParams<1> &p, int KP, int plan, int G, cudaStream_t st);
+int tc_configure_plan16(int KP, int plan);
+int tc_configure_plan32(int KP, int plan);
+
 // The derivative product's instances and tables (hoe_tc_deriv.cu).
 cudaError_t tc_launch_deriv(const hoe_handle *h, const TcParams<1> &p, int KP, int N, int G, cudaStream_t st);
 int tc_configure_deriv(int KP, int N);
@@ -167,7 +186,7 @@ struct Cursor {
 //     one set, flushed every 8 stages, and two phase tiles, so the phase
 //     warps write stage s+1 while stage s is multiplied (measured 1.3%
 //     faster than two sets with one phase tile; both leave the same PD).
-template <int N>
+template <int N, int V = 0>
 struct Tmem {
   static constexpr bool PSPLIT = N <= 64;
   static constexpr int NISS = PSPLIT ? 2 : 1;
@@ -176,7 +195,7 @@ struct Tmem {
   static constexpr int NPART = PSPLIT ? 3 : 1;   // N-wide parts of one set
   static constexpr int ACCW = NPART * N;
   static constexpr int QOFF = 2 * N;             // issuer 1's part of a set (PSPLIT)
-  static constexpr int GROUP = PSPLIT ? 32 : 8;
+  static constexpr int GROUP = TcPlan<V>::GROUP ? TcPlan<V>::GROUP : (PSPLIT ? 32 : 8);
   static constexpr int ACC = ACCBUF * ACCW;
   static constexpr int PD_MAX = (512 - ACC - ABUF * 2 * TV) / TV;
   static constexpr uint32_t A_COL = 0;
@@ -196,16 +215,16 @@ struct Tmem {
 // (nTerm <= 16, zero padded).
 constexpr int KF = 16;
 
-template <int N, int KP, int NS, bool DERIV = false>
+template <int N, int KP, int NS, bool DERIV = false, int V = 0>
 struct Smem {
-  static constexpr int ABUF = Tmem<N>::ABUF;
+  static constexpr int ABUF = Tmem<N, V>::ABUF;
   // Residual widths up to 16: the row tile's TF32 residual vectors (hi, lo)
   // also sit in tensor memory, 2*KP columns after the accumulators, as the A
   // operand of the residual MMAs (written by phase warps 0-3 once per row
   // tile), so that those MMAs read only the column tile from shared memory.
   static constexpr bool RT = KP <= 16;
   static constexpr int R_COLS = RT ? 2 * KP : 0;
-  static constexpr int PD_CAP = (512 - Tmem<N>::ACC - ABUF * 2 * TV - R_COLS) / TV;
+  static constexpr int PD_CAP = (512 - Tmem<N, V>::ACC - ABUF * 2 * TV - R_COLS) / TV;
   static constexpr int PD = (NS - 1) < PD_CAP ? (NS - 1) : (PD_CAP < 3 ? PD_CAP : 3);
   static constexpr int B_TILE = N * TK * 2;
   static constexpr int CV_TILE = TV * KP * 4;
@@ -229,7 +248,7 @@ struct Smem {
   // residual issuer has seen all arrivals for stage s before it writes stage
   // s + PD, so the arrivals for s and s + PB never mix.  Three groups get
   // two barriers each (6; measured 0.7% faster than 3 at 16 coils).
-  static constexpr int NG = Warps<N>::NG;
+  static constexpr int NG = Warps<N, V>::NG;
   static constexpr int PB = NG == 3 ? 6 : (PD > NG ? PD : NG);
   static_assert(PB >= NG && PB >= PD, "residual-tile barriers");
   static constexpr int NBAR = 2 * NS + ABUF + 10 + 2 * PB;
@@ -237,26 +256,28 @@ struct Smem {
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
 
-template <int N, int KP, bool DERIV = false>
+template <int N, int KP, bool DERIV = false, int V = 0>
 constexpr int pick_stages() {
-  return Smem<N, KP, 6, DERIV>::BYTES <= 227 * 1024 ? 6
-       : Smem<N, KP, 5, DERIV>::BYTES <= 227 * 1024 ? 5
-       : Smem<N, KP, 4, DERIV>::BYTES <= 227 * 1024 ? 4
-       : Smem<N, KP, 3, DERIV>::BYTES <= 227 * 1024 ? 3 : 2;
+  return TcPlan<V>::NS ? TcPlan<V>::NS
+       : Smem<N, KP, 6, DERIV, V>::BYTES <= 227 * 1024 ? 6
+       : Smem<N, KP, 5, DERIV, V>::BYTES <= 227 * 1024 ? 5
+       : Smem<N, KP, 4, DERIV, V>::BYTES <= 227 * 1024 ? 4
+       : Smem<N, KP, 3, DERIV, V>::BYTES <= 227 * 1024 ? 3 : 2;
 }
 
 // DERIV: the derivative product (array_operator.jl:216-218) in one pass of
 // the forward: the phase warps scale e^{i phi} by 2 pi i F[s,v] before the
 // BF16 split, F formed from the stage's basis tile and the row's kdot.
-template <int N, int KP, int NS, int MS, bool DERIV = false>
-__global__ void __launch_bounds__(Warps<N>::THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
+template <int N, int KP, int NS, int MS, bool DERIV = false, int V = 0>
+__global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
   static_assert(!DERIV || MS == 1, "the derivative product serves one operator per launch");
-  using S = Smem<N, KP, NS, DERIV>;
-  constexpr int ABUF = S::ABUF, PD = S::PD, PB = S::PB, NISS = Tmem<N>::NISS;
-  constexpr int ACCBUF = Tmem<N>::ACCBUF, NPART = Tmem<N>::NPART, ACCW = Tmem<N>::ACCW;
-  constexpr int QOFF = Tmem<N>::QOFF, GROUP = Tmem<N>::GROUP;
-  constexpr bool PSPLIT = Tmem<N>::PSPLIT;
-  using W = Warps<N>;
+  using S = Smem<N, KP, NS, DERIV, V>;
+  using TM_ = Tmem<N, V>;
+  constexpr int ABUF = S::ABUF, PD = S::PD, PB = S::PB, NISS = TM_::NISS;
+  constexpr int ACCBUF = TM_::ACCBUF, NPART = TM_::NPART, ACCW = TM_::ACCW;
+  constexpr int QOFF = TM_::QOFF, GROUP = TM_::GROUP;
+  constexpr bool PSPLIT = TM_::PSPLIT;
+  using W = Warps<N, V>;
   constexpr int NG = W::NG, GW = W::GW, PW = W::PW, FLW = W::FLW;
   constexpr int CISS_WARP = W::CISS, PISS_WARP = W::PISS, LOAD_WARP = W::LOAD;
   static_assert(PD >= 1, "residual-phase look-ahead");
@@ -282,7 +303,7 @@ __global__ void __launch_bounds__(Warps<N>::THREADS, 1) k_tc_contract(const __gr
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + S::MISC_OFF);
   volatile int *abort = reinterpret_cast<volatile int *>(smem + S::MISC_OFF + 8);
   constexpr uint32_t TMEM_COLS = 512;
-  constexpr uint32_t A_COL = Tmem<N>::A_COL, P_COL = Tmem<N>::P_COL;
+  constexpr uint32_t A_COL = TM_::A_COL, P_COL = TM_::P_COL;
   constexpr uint32_t ACC_COL = P_COL + PD * TV;   // group g, issuer q: ACC_COL + (g%ACCBUF)*ACCW + q*QOFF
   constexpr bool RT = S::RT;
   constexpr uint32_t R_COL = ACC_COL + ACCBUF * ACCW;   // [hi KP | lo KP] when RT
@@ -791,33 +812,39 @@ __global__ void __launch_bounds__(Warps<N>::THREADS, 1) k_tc_contract(const __gr
   }
 }
 
-template <int N, int KP, bool DERIV = false>
+// Every launch asks for at least 116 KB of shared memory, more than half of
+// an SM's, so that at most one CTA is resident per SM: each CTA allocates all
+// 512 tensor-memory columns.
+template <int N, int KP, bool DERIV = false, int V = 0>
 struct Kern {
-  static constexpr int NS = pick_stages<N, KP, DERIV>();
-  static_assert(Smem<N, KP, NS, DERIV>::PD >= 1, "residual-phase look-ahead");
-  using S = Smem<N, KP, NS, DERIV>;
+  static constexpr int NS = pick_stages<N, KP, DERIV, V>();
+  static_assert(Smem<N, KP, NS, DERIV, V>::PD >= 1, "residual-phase look-ahead");
+  using S = Smem<N, KP, NS, DERIV, V>;
   static_assert(S::BYTES <= 227 * 1024, "shared memory plan exceeds 227 KB");
+  static constexpr size_t LAUNCH_BYTES = S::BYTES < 116 * 1024 ? 116 * 1024 : S::BYTES;
 };
 
-template <int N, int KP, int MS, bool DERIV = false>
+template <int N, int KP, int MS, bool DERIV = false, int V = 0>
 cudaError_t launch_contract(const hoe_handle *h, const TcParams<MS> &p, int G, cudaStream_t st) {
-  using K = Kern<N, KP, DERIV>;
-  auto kern = k_tc_contract<N, KP, K::NS, MS, DERIV>;
-  const cudaError_t e = launch_pdl(kern, dim3(G), dim3(Warps<N>::THREADS), K::S::BYTES, st, p);
+  using K = Kern<N, KP, DERIV, V>;
+  auto kern = k_tc_contract<N, KP, K::NS, MS, DERIV, V>;
+  const cudaError_t e = launch_pdl(kern, dim3(G), dim3(Warps<N, V>::THREADS), K::LAUNCH_BYTES, st, p);
   h->launches += 1;
   return e;
 }
 
 // One-time per (process, instantiation): shared-memory limit; returns the
 // resident CTAs per SM.
-template <int N, int KP, int MS, bool DERIV = false>
+template <int N, int KP, int MS, bool DERIV = false, int V = 0>
 int configure() {
-  using K = Kern<N, KP, DERIV>;
-  auto kern = k_tc_contract<N, KP, K::NS, MS, DERIV>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::S::BYTES) != cudaSuccess)
+  using K = Kern<N, KP, DERIV, V>;
+  auto kern = k_tc_contract<N, KP, K::NS, MS, DERIV, V>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::LAUNCH_BYTES) != cudaSuccess)
     return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, Warps<N>::THREADS, K::S::BYTES) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, Warps<N, V>::THREADS, K::LAUNCH_BYTES) !=
+      cudaSuccess)
+    return 0;
   return nb;
 }
 
@@ -860,6 +887,26 @@ int configure_kernel(int KP, int N) {
 }
 
 
+
+// Plans 1..kTcPlans-1 of one coil width N (16 or 32) and residual width KP.
+template <int N, int KP>
+cudaError_t launch_plan_nk(const hoe_handle *h, const TcParams<1> &p, int plan, int G, cudaStream_t st) {
+  switch (plan) {
+    case 1: return launch_contract<N, KP, 1, false, 1>(h, p, G, st);
+    case 2: return launch_contract<N, KP, 1, false, 2>(h, p, G, st);
+    case 3: return launch_contract<N, KP, 1, false, 3>(h, p, G, st);
+    default: return launch_contract<N, KP, 1, false, 4>(h, p, G, st);
+  }
+}
+template <int N, int KP>
+int configure_plan_nk(int plan) {
+  switch (plan) {
+    case 1: return configure<N, KP, 1, false, 1>();
+    case 2: return configure<N, KP, 1, false, 2>();
+    case 3: return configure<N, KP, 1, false, 3>();
+    default: return configure<N, KP, 1, false, 4>();
+  }
+}
 
 // The derivative product for up to 16 coils (N = 16 or 32).
 template <int KP>

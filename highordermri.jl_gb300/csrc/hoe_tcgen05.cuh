@@ -21,6 +21,7 @@ struct TcBuffers {
   float2 *part = nullptr;
   int *err = nullptr;
   int N = 0, nChaTC = 0;
+  int plan = 0;                               // execution plan of the contraction (TcPlan)
   int gridF = 1, gridA = 1, slotsF = 1, slotsA = 1;
   size_t bopFElems = 0, bopAElems = 0, partElems = 0;
   // derivative product (kspha_dt mode), allocated on first use.  Up to 16

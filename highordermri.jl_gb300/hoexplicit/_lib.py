@@ -12,7 +12,7 @@ from pathlib import Path
 PKG_DIR = Path(__file__).resolve().parent.parent
 LIB_PATH = Path(os.environ.get("HOE_LIBRARY", PKG_DIR / "libhoexplicit.so"))
 
-HOE_ABI_VERSION = 1
+HOE_ABI_VERSION = 2
 HOE_OK = 0
 HOE_ERR_ARG = -1
 HOE_ERR_DIM = -2
@@ -70,7 +70,7 @@ class HoeDesc(ctypes.Structure):
         ("nSam", ctypes.c_int32), ("nCha", ctypes.c_int32), ("nTerm", ctypes.c_int32),
         ("has_concomitant", ctypes.c_int32), ("nVox", ctypes.c_int32),
         ("engine", ctypes.c_int32), ("device", ctypes.c_int32),
-        ("tile_samples", ctypes.c_int32), ("tile_voxels", ctypes.c_int32),
+        ("tc_plan", ctypes.c_int32), ("reserved", ctypes.c_int32),
         ("split_hint", ctypes.c_int32),
         ("mask_idx", ctypes.POINTER(ctypes.c_int32)),
         ("bf", ctypes.POINTER(ctypes.c_double)),
@@ -133,7 +133,7 @@ class HoeTuneResult(ctypes.Structure):
     _fields_ = [
         ("engine", ctypes.c_int32), ("split_forward", ctypes.c_int32), ("split_adjoint", ctypes.c_int32),
         ("candidates", ctypes.c_int32), ("cand_engine", ctypes.c_int32 * 8), ("cand_split", ctypes.c_int32 * 8),
-        ("cand_ms", ctypes.c_float * 8),
+        ("cand_ms", ctypes.c_float * 8), ("tc_plan", ctypes.c_int32), ("cand_plan", ctypes.c_int32 * 8),
     ]
 
 
@@ -152,6 +152,7 @@ class HoeInfo(ctypes.Structure):
         ("split_forward", ctypes.c_int32), ("split_adjoint", ctypes.c_int32),
         ("residual_rank", ctypes.c_int32), ("residual_width", ctypes.c_int32),
         ("residual_phase_bound", ctypes.c_double), ("device_bytes", ctypes.c_int64),
+        ("tc_plan", ctypes.c_int32), ("tc_plans", ctypes.c_int32),
     ]
 
 

@@ -91,9 +91,20 @@ class _Vec:
         return result
 
 
+# The tensor-core engine's execution plans (hoe_desc.tc_plan, hoe_autotune);
+# plans 1-4 exist up to 16 coils.
+TC_PLANS = {
+    0: "default: 3 groups of 4 phase warps, deepest stage ring, flush every 32 stages",
+    1: "2 groups of 4 phase warps",
+    2: "4 groups of 4 phase warps",
+    3: "stage ring of 4",
+    4: "accumulator flush every 16 stages",
+}
+
+
 def build_desc(grid: Grid, kspha, times, *, fieldmap=None, csm=None, mask=None, concomitant=None,
                recon_terms=None, k_nominal=None, kspha_dt=None, kdot=None, engine=DEFAULT_ENGINE,
-               device=0, split_hint=0):
+               device=0, split_hint=0, tc_plan=0):
     """Validate the constructor inputs (reference rules) and build the C
     descriptor.  Returns (desc, keep, meta); ``keep`` holds the host arrays the
     descriptor points to and must outlive every use of ``desc``."""
@@ -169,6 +180,7 @@ def build_desc(grid: Grid, kspha, times, *, fieldmap=None, csm=None, mask=None, 
     desc.engine = ENGINES[engine]
     desc.device = device
     desc.split_hint = int(split_hint)
+    desc.tc_plan = int(tc_plan)
     desc.mask_idx = k["mask_idx"].ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
     desc.bf = _dptr(k["bf"])
     desc.kspha = _dptr(k["kspha"])
@@ -202,7 +214,7 @@ class ExplicitGB300Op:
 
     def __init__(self, grid: Grid, kspha, times, *, fieldmap=None, csm=None, mask=None,
                  concomitant=None, recon_terms=None, k_nominal=None, kspha_dt=None, kdot=None,
-                 engine: str = DEFAULT_ENGINE, gpus=None, split_hint: int = 0):
+                 engine: str = DEFAULT_ENGINE, gpus=None, split_hint: int = 0, tc_plan: int = 0):
         lib = _lib.load()
         torch = _torch()
         if not torch.cuda.is_available():
@@ -220,7 +232,7 @@ class ExplicitGB300Op:
         desc, self._keep, meta = build_desc(
             grid, kspha, times, fieldmap=fieldmap, csm=csm, mask=mask, concomitant=concomitant,
             recon_terms=recon_terms, k_nominal=k_nominal, kspha_dt=kspha_dt, kdot=kdot,
-            engine=engine, device=device, split_hint=split_hint)
+            engine=engine, device=device, split_hint=split_hint, tc_plan=tc_plan)
         self.derivative_mode = meta["derivative_mode"]
         nSam, nCha, nVox, nTerm = meta["nSam"], meta["nCha"], meta["nVox"], meta["nTerm"]
         nFull, mask = meta["nFull"], meta["mask"]
@@ -274,14 +286,18 @@ class ExplicitGB300Op:
         _lib.check(_lib.load().hoe_check(self._handle(), self._stream()), self._h)
 
     def autotune(self, reps: int = 5) -> dict:
-        """Time forward+adjoint for each execution plan (FP32 engine at three
-        split-K factors, tensor-core engine) and keep the fastest (hoe_autotune)."""
+        """Time forward+adjoint for each execution plan and keep the fastest
+        (hoe_autotune): the FP32 engine at three split-K factors and the
+        tensor-core engine's plans (five up to 16 coils: phase-warp groups,
+        stage-ring depth, accumulator flush interval; TC_PLANS)."""
         r = _lib.HoeTuneResult()
         _lib.check(_lib.load().hoe_autotune(self._handle(), int(reps), ctypes.byref(r), self._stream()), self._h)
         names = _ENGINE_NAMES
         self.engine = names[r.engine]
         return {"engine": self.engine, "split_forward": r.split_forward, "split_adjoint": r.split_adjoint,
-                "candidates": [{"engine": names[r.cand_engine[i]], "split": r.cand_split[i], "ms": r.cand_ms[i]}
+                "tc_plan": r.tc_plan,
+                "candidates": [{"engine": names[r.cand_engine[i]], "split": r.cand_split[i],
+                                "plan": r.cand_plan[i], "ms": r.cand_ms[i]}
                                for i in range(r.candidates)]}
 
     def set_engine(self, engine: str) -> None:

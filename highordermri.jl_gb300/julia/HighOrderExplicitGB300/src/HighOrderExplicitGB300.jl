@@ -27,7 +27,7 @@ export GB300ExplicitOp, explicit_backward, encode, GB300Batch, set_kspha!
 const libhoe = get(ENV, "HOE_LIBRARY",
     normpath(joinpath(@__DIR__, "..", "..", "..", "libhoexplicit.so")))
 
-const HOE_ABI_VERSION = Int32(1)
+const HOE_ABI_VERSION = Int32(2)
 const HOE_ENGINE_FP32_SIMT = Int32(0)
 const HOE_ENGINE_TC_BF16X3 = Int32(1)
 const HOE_ENGINE_AUTO = Int32(2)
@@ -41,7 +41,7 @@ struct HoeDesc
     abi_version::Int32
     nX::Int32; nY::Int32; nZ::Int32
     nSam::Int32; nCha::Int32; nTerm::Int32; has_concomitant::Int32; nVox::Int32
-    engine::Int32; device::Int32; tile_samples::Int32; tile_voxels::Int32; split_hint::Int32
+    engine::Int32; device::Int32; tc_plan::Int32; reserved::Int32; split_hint::Int32
     mask_idx::Ptr{Int32}
     bf::Ptr{Float64}
     kspha::Ptr{Float64}

@@ -84,7 +84,7 @@
 extern "C" {
 #endif
 
-#define HOE_ABI_VERSION 1
+#define HOE_ABI_VERSION 2
 
 /* status codes */
 #define HOE_OK               0
@@ -123,8 +123,9 @@ typedef struct hoe_desc {
     int32_t nVox;             /* masked voxels (count(mask)) > 0                        */
     int32_t engine;           /* HOE_ENGINE_*                                          */
     int32_t device;           /* CUDA device ordinal; -1 = current device              */
-    int32_t tile_samples;     /* 0 = default (128); autotuner override                 */
-    int32_t tile_voxels;      /* 0 = default (128); autotuner override                 */
+    int32_t tc_plan;          /* tensor-core execution plan: 0 = default; 1-4 (up to 16
+                                 coils): the variants hoe_autotune times (hoe_tune_result) */
+    int32_t reserved;         /* must be 0                                             */
     int32_t split_hint;       /* 0 = automatic split-K                                 */
     const int32_t *mask_idx;  /* host [nVox], 0-based linear grid indices, ascending   */
     const double  *bf;        /* host [nVox x nTermEff], nTermEff = nTerm + 4*has_conc */
@@ -192,6 +193,8 @@ typedef struct hoe_tune_result {
     int32_t cand_engine[8];
     int32_t cand_split[8];         /* forward split-K factor (FP32 engine), 0 otherwise   */
     float   cand_ms[8];            /* mean forward+adjoint time of each candidate (ms)    */
+    int32_t tc_plan;               /* chosen tensor-core plan (kept if the FP32 engine wins) */
+    int32_t cand_plan[8];          /* tensor-core plan of each candidate, -1 for FP32     */
 } hoe_tune_result;
 
 typedef struct hoe_batch_info {
@@ -210,6 +213,8 @@ typedef struct hoe_info {
     int32_t residual_width;        /* stored width (r rounded up to 8, 12, 16 or 24)  */
     double  residual_phase_bound;  /* max |sum_l dbeta*kappa| in cycles over all tiles */
     int64_t device_bytes;          /* device memory owned by the handle */
+    int32_t tc_plan;               /* execution plan of the tensor-core contraction    */
+    int32_t tc_plans;              /* plans available: 5 up to 16 coils, else 1        */
 } hoe_info;
 
 /* Library */
@@ -238,10 +243,16 @@ HOE_API int  hoe_get_timings(hoe_handle *h, hoe_timings *out);
 HOE_API int  hoe_check(hoe_handle *h, void *stream);
 
 /* Times forward+adjoint of this operator for each available execution plan
- * (the FP32 engine at split-K factors 1/4, 1/2 and 1 of its default, and the
- * tensor-core engine) with CUDA events on `stream`, `reps` repetitions each,
- * and keeps the fastest.  Waits for the stream.  Counterpart of choosing
- * :array / :kernel / nBlock in the reference by hand. */
+ * with CUDA events on `stream`, `reps` repetitions each, and keeps the
+ * fastest: the FP32 engine at split-K factors 1/4, 1/2 and 1 of its default,
+ * and the tensor-core engine's plans.  Up to 16 coils there are five: the
+ * default (3 groups of 4 phase warps, the deepest stage ring that fits,
+ * accumulators flushed every 32 stages), 2 or 4 phase-warp groups, a stage
+ * ring of 4, and a flush every 16 stages; above 16 coils the default only.
+ * The chosen tensor-core plan serves the operator's forward, adjoint and
+ * normal products (batches and the derivative product use plan 0).  Waits
+ * for the stream.  Counterpart of choosing :array / :kernel / nBlock
+ * (explicit_gpu_operator.jl:333, array_operator.jl:129-135) by hand. */
 HOE_API int  hoe_autotune(hoe_handle *h, int32_t reps, hoe_tune_result *out, void *stream);
 
 /* Operator applications (complex64 device vectors) */

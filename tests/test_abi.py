@@ -36,9 +36,47 @@ def test_version_and_abi():
 def test_struct_layouts_match_header():
     # two int32 blocks followed by pointers / doubles, natural alignment
     assert ctypes.sizeof(_lib.HoeDesc) == 14 * 4 + 7 * 8
-    assert ctypes.sizeof(_lib.HoeInfo) == 14 * 4 + 8 + 8
+    assert ctypes.sizeof(_lib.HoeInfo) == 14 * 4 + 8 + 8 + 2 * 4
     assert ctypes.sizeof(_lib.HoeCgParams) == 2 * 4 + 2 * 8
     assert ctypes.sizeof(_lib.HoeCgStats) == 2 * 4 + 2 * 8
+
+
+STRUCTS = {
+    "hoe_desc": "HoeDesc", "hoe_info": "HoeInfo", "hoe_timings": "HoeTimings",
+    "hoe_cg_params": "HoeCgParams", "hoe_cg_stats": "HoeCgStats", "hoe_delay_params": "HoeDelayParams",
+    "hoe_delay_result": "HoeDelayResult", "hoe_tune_result": "HoeTuneResult",
+    "hoe_batch_info": "HoeBatchInfo", "hoe_raw_model": "HoeRawModel",
+}
+
+
+def test_struct_offsets_match_the_c_header(tmp_path):
+    # every ctypes field at the offset and every struct at the size that a C
+    # compiler gives the declarations in include/hoexplicit.h
+    import shutil
+    import subprocess
+    from pathlib import Path
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = Path(__file__).resolve().parent.parent / "include"
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "hoexplicit.h"', "int main(void) {"]
+    expect = {}
+    for cname, pyname in STRUCTS.items():
+        st = getattr(_lib, pyname)
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        expect[cname] = ctypes.sizeof(st)
+        for f in st._fields_:
+            cfield = f[0].rstrip("_")   # ctypes spells the C field `lambda` as `lambda_`
+            lines.append(f'  printf("{cname}.{f[0]} %zu\\n", offsetof({cname}, {cfield}));')
+            expect[f"{cname}.{f[0]}"] = getattr(st, f[0]).offset
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", str(inc), str(src), "-o", str(exe)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                    text=True).stdout.splitlines())
+    assert {k: int(v) for k, v in got.items()} == expect
 
 
 def _desc(**over):

@@ -626,3 +626,88 @@ def test_tc_long_pipelines_match_fp32_engine(n, nSam, nCha):
     a.check()
     a.close()
     b.close()
+
+
+# Execution plans of the tensor-core contraction (hoe_desc.tc_plan, chosen by
+# hoe_autotune): each plan is its own kernel instance, so each is held to the
+# same tolerance against the FP64 oracle, at both coil widths (up to 8 and
+# 9-16 coils) and the residual widths 8, 16 and 24
+PLAN_CASES = [
+    dict(shape=(13, 11, 1), nSam=257, nCha=6, nTerm=9),               # 8-coil tiles, width 8
+    dict(shape=(9, 7, 1), nSam=300, nCha=3, nTerm=16),                # 8-coil tiles, width 16
+    dict(shape=(14, 13, 1), nSam=333, nCha=12, nTerm=16, conc=True),  # 16-coil tiles, width 16
+    dict(shape=(6, 5, 4), nSam=300, nCha=16, nTerm=16, conc=True),    # 16-coil tiles, width 24
+]
+
+
+@pytest.mark.parametrize("plan", range(5))
+def test_tc_plans_vs_oracle(plan):
+    maybe_skip("tc")
+    for params in PLAN_CASES:
+        w = workloads.small(seed=19, **params)
+        op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", tc_plan=plan, **w.op_kwargs())
+        assert op.info()["tc_plan"] == plan
+        bf, k, t, f, c, idx = workloads.prepared_model(w)
+        m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+        mask = np.zeros(w.x.size, dtype=bool)
+        mask[idx] = True
+        yo = oracle.forward(m, w.x[idx])
+        rng = np.random.default_rng(plan)
+        y0 = rng.standard_normal(op.nrow) + 1j * rng.standard_normal(op.nrow)
+        xo = oracle.scatter(oracle.adjoint(m, y0), mask)
+        yg = host(op * dev(w.x))
+        assert dense.rel(yg, yo) < TOL["tc"], (plan, params, dense.rel(yg, yo))
+        assert dense.rel(host(op.H * dev(y0)), xo) < TOL["tc"]
+        assert np.array_equal(host(op * dev(w.x)), yg)
+        op.check()
+        op.close()
+
+
+@pytest.mark.parametrize("plan", range(5))
+@pytest.mark.parametrize("nCha", [8, 16])
+def test_tc_plans_long_pipeline(plan, nCha):
+    # 160x160 spiral, 9,000 samples: ~150-190 stages per CTA in each direction,
+    # so every plan wraps its stage ring and flushes its accumulators many times
+    maybe_skip("tc")
+    w = workloads.spiral_slice(23, 160, 9000, nCha, d=200e-3 / 160)
+    a = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", tc_plan=plan, **w.op_kwargs())
+    b = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())
+    x = dev(w.x)
+    yb = host(b * x)
+    assert dense.rel(host(a * x), yb) < TOL["tc"]
+    y = dev(yb)
+    assert dense.rel(host(a.H * y), host(b.H * y)) < TOL["tc"]
+    a.check()
+    a.close()
+    b.close()
+
+
+def test_autotune_times_every_tensor_core_plan():
+    # up to 16 coils the autotuner times five tensor-core plans besides the
+    # FP32 split factors, keeps the fastest and the products stay correct
+    maybe_skip("tc")
+    w = workloads.spiral_slice(29, 96, 4000, 12, d=200e-3 / 96)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    assert op.info()["tc_plans"] == 5
+    r = op.autotune(reps=2)
+    tc = [c for c in r["candidates"] if c["engine"] == "tc"]
+    assert sorted(c["plan"] for c in tc) == [0, 1, 2, 3, 4]
+    assert all(c["ms"] > 0 for c in r["candidates"])
+    best_tc = min(tc, key=lambda c: c["ms"])
+    assert r["tc_plan"] == best_tc["plan"] == op.info()["tc_plan"]
+    assert min(r["candidates"], key=lambda c: c["ms"])["engine"] == r["engine"]
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    rows = np.sort(np.random.default_rng(1).choice(w.nSam, 64, replace=False))
+    mr = oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=w.kspha.shape[0])
+    y = host(op * dev(w.x)).reshape(w.nCha, w.nSam)[:, rows].reshape(-1)
+    assert dense.rel(y, oracle.forward(mr, w.x[idx])) < TOL[r["engine"]]
+    op.check()
+    op.close()
+    # more than 16 coils: the default plan only
+    w = workloads.small(seed=5, shape=(10, 9, 1), nSam=300, nCha=20, nTerm=9)
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    assert op.info()["tc_plans"] == 1
+    with pytest.raises(ArgumentError):
+        HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", tc_plan=2, **w.op_kwargs())
+    op.close()
