@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -390,6 +391,9 @@ cudaError_t tc_prepare(hoe_handle *h) {
   h->tc.buf = buf;
   h->tc.bytes = bytes;
   h->tc.ready = true;
+  // failure detection test (host-side injection): HOE_INJECT_TC_STALL=k makes
+  // the first forward contraction of this operator stall CTA 0 at stage k
+  if (const char *inj = getenv("HOE_INJECT_TC_STALL")) b.injectStall1 = atoi(inj) + 1;
   h->tc_host = new TcBuffers(b);
   e = tc_anchor_tables(h, 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
@@ -546,7 +550,14 @@ cudaError_t launch_planned(const hoe_handle *h, const TcBuffers &b, const TcPara
 }
 
 cudaError_t contract_forward(const hoe_handle *h, const TcBuffers &b, cudaStream_t st) {
-  const TcParams<1> p = single_params(h, b, slice_forward(h, b));
+  TcParams<1> p = single_params(h, b, slice_forward(h, b));
+  if (b.injectStall1 > 0) {
+    // failure detection test: CTA 0 never receives this stage's operands and
+    // its waits run out after 1 ms; the kernel reports HOE_ERR_TIMEOUT
+    p.stallStage1 = b.injectStall1;
+    p.waitNs = 1000000;
+    b.injectStall1 = 0;
+  }
   trace(h, EV_FK0, st);
   cudaError_t e = launch_planned(h, b, p, b.gridF, st);
   trace(h, EV_FK1, st);

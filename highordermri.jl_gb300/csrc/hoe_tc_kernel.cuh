@@ -123,6 +123,11 @@ struct TcParams {
   // sample row 2 pi kdot_l as [row][KF]
   const float *bfT;
   const float *kd1;
+  // failure detection: every wait's limit in ns (0: the 2 s default), and a
+  // stage + 1 (0: none) whose operands CTA 0's loader does not fetch, so that
+  // the waits for them run out
+  uint64_t waitNs;
+  int stallStage1, pad1;
   TcSlice s[MS];
   // slice i (a compile-time index for single-slice launches)
   __host__ __device__ __forceinline__ const TcSlice &at(int i) const { return s[MS == 1 ? 0 : i]; }
@@ -312,6 +317,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int G = gridDim.x, b = blockIdx.x;
+  const uint64_t lim = p.waitNs ? p.waitNs : kWaitNs;
   const int64_t wb = (int64_t)b * p.work / G, we = (int64_t)(b + 1) * p.work / G;
   const int nIter = (int)(we - wb);
   Cursor<MS> c0;
@@ -390,7 +396,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
       // add group pendGrp into acc; write acc out if it closed its row tile
       if (warp >= FLW) { pendGrp = -1; return; }
       const int g = pendGrp, gb = g % ACCBUF, gr = g / ACCBUF;
-      bool got = ok && wait_bar(&segdone[gb], gr & 1, abort, p.err);
+      bool got = ok && wait_bar(&segdone[gb], gr & 1, abort, p.err, lim);
       tc_fence_after();
       if (got) {
 #pragma unroll
@@ -499,8 +505,8 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
           // the new row tile's residual vectors, hi and lo, from the shared
           // tile into TMEM once the previous row tile's residual MMAs are done
           ++kt;
-          if ((kt > 0 && !wait_bar_warp(&rtfree[0], (kt - 1) & 1, abort, p.err)) ||
-              !wait_bar_warp(&rfull[kt & 1], (kt >> 1) & 1, abort, p.err)) { ok = false; break; }
+          if ((kt > 0 && !wait_bar_warp(&rtfree[0], (kt - 1) & 1, abort, p.err, lim)) ||
+              !wait_bar_warp(&rfull[kt & 1], (kt >> 1) & 1, abort, p.err, lim)) { ok = false; break; }
           tc_fence_after();
           const float4 *rv = reinterpret_cast<const float4 *>(sRV + (size_t)(kt & 1) * 2 * S::RV_TILE);
           uint32_t hv[KP], lv[KP];
@@ -531,9 +537,9 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
       if (it % NG == par) {
         // phase of this stage in radians (TMEM), then release its buffer
         const int pb = it % PD, pbar = it % PB, pr = it / PB;
-        if (!wait_bar(&pfull[pbar], pr & 1, abort, p.err)) { ok = false; break; }
+        if (!wait_bar(&pfull[pbar], pr & 1, abort, p.err, lim)) { ok = false; break; }
         // derivative product: the stage's basis tile (loaded with the stage)
-        if (DERIV && !wait_bar(&full[it % NS], (it / NS) & 1, abort, p.err)) { ok = false; break; }
+        if (DERIV && !wait_bar(&full[it % NS], (it / NS) & 1, abort, p.err, lim)) { ok = false; break; }
         tc_fence_after();
         const uint32_t pBase = tmem + laneBase + P_COL + (uint32_t)(pb * TV + half * 32);
         const float *bt = reinterpret_cast<const float *>(sBF + (size_t)(it % NS) * S::BF_TILE) + half * 32;
@@ -566,7 +572,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
               split_bf16x2(-Fv[j] * sn, Fv[j] * cs, hv[j], lv[j]);
             }
             if (q == 0) {
-              if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err)) { ok = false; break; }
+              if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err, lim)) { ok = false; break; }
               tc_fence_after();
             }
             tmem_st8(ah, hv);
@@ -585,7 +591,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
             // it-ABUF is done, which the stage's `empty` barrier records (the
             // slot of stage it-ABUF cannot have been reused: that needs this
             // stage's tile)
-            if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err)) { ok = false; break; }
+            if (ar > 0 && !wait_bar(&empty[(it - ABUF) % NS], ((it - ABUF) / NS) & 1, abort, p.err, lim)) { ok = false; break; }
             tc_fence_after();
           }
           tmem_st16(ah, hi);
@@ -642,13 +648,13 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
           ++grp;
           // accumulator set grp%ACCBUF was last used by group grp-ACCBUF: wait until it was read out
           if (grp >= ACCBUF &&
-              !wait_bar_warp(&tmemfree[grp % ACCBUF], ((grp / ACCBUF) - 1) & 1, abort, p.err)) break;
+              !wait_bar_warp(&tmemfree[grp % ACCBUF], ((grp / ACCBUF) - 1) & 1, abort, p.err, lim)) break;
         }
         const bool last = (it == nIter - 1) || (ch + 1 == c.C) || ((ch + 1) % GROUP == 0);
         const int slot = it % NS, round = it / NS;
         const int ab = it % ABUF, ar = it / ABUF;
-        if (!wait_bar_warp(&full[slot], round & 1, abort, p.err)) break;
-        if (!wait_bar_warp(&afull[ab], ar & 1, abort, p.err)) break;
+        if (!wait_bar_warp(&full[slot], round & 1, abort, p.err, lim)) break;
+        if (!wait_bar_warp(&afull[ab], ar & 1, abort, p.err, lim)) break;
         tc_fence_after();
         const uint32_t dt = tmem + ACC_COL + (uint32_t)((grp % ACCBUF) * ACCW + q * QOFF);
         const uint32_t aHi = tmem + A_COL + (uint32_t)(ab * 2 * TV);
@@ -706,12 +712,12 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
         }
         const bool lastOfRow = (j == nIter - 1) || (c.ch + 1 == c.C);
         const int s = j % NS, r = j / NS;
-        if (!wait_bar_warp(&full[s], r & 1, abort, p.err)) break;
-        if (!wait_bar_warp(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err)) break;
-        if (RT && (j == 0 || c.ch == 0) && !wait_bar_warp(&rtfull[0], kj & 1, abort, p.err)) break;
+        if (!wait_bar_warp(&full[s], r & 1, abort, p.err, lim)) break;
+        if (!wait_bar_warp(&rfull[kj & 1], (kj >> 1) & 1, abort, p.err, lim)) break;
+        if (RT && (j == 0 || c.ch == 0) && !wait_bar_warp(&rtfull[0], kj & 1, abort, p.err, lim)) break;
         const int pb = j % PD, pbar = j % PB, pr = j / PB;
         // tile buffer pb was last used by stage j - PD
-        if (j >= PD && !wait_bar_warp(&pfree[(j - PD) % PB], ((j - PD) / PB) & 1, abort, p.err)) break;
+        if (j >= PD && !wait_bar_warp(&pfree[(j - PD) % PB], ((j - PD) / PB) & 1, abort, p.err, lim)) break;
         tc_fence_after();
         const uint32_t dt = tmem + P_COL + (uint32_t)(pb * TV);
         const uint32_t rHi = smem_u32(sRV + (size_t)(kj & 1) * 2 * S::RV_TILE);
@@ -758,6 +764,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
       const bool leader = elect_one();
       const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + S::XR_BYTES + S::XC_BYTES + S::BF_TILE;
       int issued = 0, kcount = -1, rowIssued = -1;
+      const int skip = b == 0 ? p.stallStage1 - 1 : -1;   // failure detection: never fetched
       Cursor<MS> c = c0;
       for (int it = 0; it < nIter; ++it) {
         if (it > 0) c.next(p);
@@ -766,7 +773,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
         if (it == 0 || ch == 0) {
           ++kcount;
           const int rb = kcount & 1;
-          if (kcount >= 2 && !wait_bar_warp(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err)) break;
+          if (kcount >= 2 && !wait_bar_warp(&rfree[rb], ((kcount >> 1) - 1) & 1, abort, p.err, lim)) break;
           if (leader) {
             mbar_expect_tx(&rfull[rb], 2 * S::RV_TILE);
             const size_t ro = (size_t)rt * TM * KP;
@@ -777,8 +784,8 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
           rowIssued = kcount;
         }
         const int slot = it % NS, round = it / NS;
-        if (round > 0 && !wait_bar_warp(&empty[slot], (round - 1) & 1, abort, p.err)) break;
-        if (leader) {
+        if (round > 0 && !wait_bar_warp(&empty[slot], (round - 1) & 1, abort, p.err, lim)) break;
+        if (leader && it != skip) {
           const size_t co = (size_t)ch * TV * KP;
           mbar_expect_tx(&full[slot], stageBytes);
           bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, sl.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
@@ -797,7 +804,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
       if (*abort) {
         // drain the copies still in flight into this CTA's shared memory
         for (int it = max(0, issued - NS); it < issued; ++it)
-          drain_bar(&full[it % NS], (it / NS) & 1);
+          if (it != skip) drain_bar(&full[it % NS], (it / NS) & 1);
         if (rowIssued >= 0) drain_bar(&rfull[rowIssued & 1], (rowIssued >> 1) & 1);
       }
     }

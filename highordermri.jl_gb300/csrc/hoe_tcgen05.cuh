@@ -22,6 +22,10 @@ struct TcBuffers {
   int *err = nullptr;
   int N = 0, nChaTC = 0;
   int plan = 0;                               // execution plan of the contraction (TcPlan)
+  // failure detection test: the next forward contraction stalls CTA 0 at
+  // this stage + 1 (0: none) with 1 ms waits; set from HOE_INJECT_TC_STALL
+  // when the engine is prepared, cleared after one launch
+  mutable int injectStall1 = 0;
   int gridF = 1, gridA = 1, slotsF = 1, slotsA = 1;
   size_t bopFElems = 0, bopAElems = 0, partElems = 0;
   // derivative product (kspha_dt mode), allocated on first use.  Up to 16
@@ -115,14 +119,15 @@ __device__ __forceinline__ bool mbar_try_wait_sleep(uint64_t *bar, uint32_t pari
   return ok != 0;
 }
 
-// Bounded wait; returns false on timeout or when another role aborted.
+// Bounded wait (at most lim ns); returns false on timeout or when another
+// role aborted.
 __device__ __noinline__ bool wait_bar_slow(uint64_t *bar, uint32_t parity, volatile int *abort,
-                                           int *gerr) {
+                                           int *gerr, uint64_t lim = kWaitNs) {
   const uint64_t t0 = globaltimer();
   for (;;) {
     if (mbar_try_wait_sleep(bar, parity)) return true;
     if (*abort) return false;
-    if (globaltimer() - t0 > kWaitNs) {
+    if (globaltimer() - t0 > lim) {
       *abort = 1;
       atomicExch(gerr, HOE_ERR_TIMEOUT);
       return false;
@@ -131,15 +136,16 @@ __device__ __noinline__ bool wait_bar_slow(uint64_t *bar, uint32_t parity, volat
 }
 
 __device__ __forceinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile int *abort,
-                                         int *gerr) {
+                                         int *gerr, uint64_t lim = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
-  return wait_bar_slow(bar, parity, abort, gerr);
+  return wait_bar_slow(bar, parity, abort, gerr, lim);
 }
 
 // Bounded wait made by every lane of a converged warp; the result is the same
 // in all lanes (any lane's failure counts), so the warp stays converged.
-__device__ __forceinline__ bool wait_bar_warp(uint64_t *bar, uint32_t parity, volatile int *abort, int *gerr) {
-  return __all_sync(0xffffffffu, wait_bar(bar, parity, abort, gerr));
+__device__ __forceinline__ bool wait_bar_warp(uint64_t *bar, uint32_t parity, volatile int *abort, int *gerr,
+                                              uint64_t lim = kWaitNs) {
+  return __all_sync(0xffffffffu, wait_bar(bar, parity, abort, gerr, lim));
 }
 
 // One lane of a converged warp (elect.sync).  MMA issuers run their loop with

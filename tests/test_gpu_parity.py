@@ -711,3 +711,41 @@ def test_autotune_times_every_tensor_core_plan():
     with pytest.raises(ArgumentError):
         HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", tc_plan=2, **w.op_kwargs())
     op.close()
+
+
+def test_tc_bounded_wait_runs_out_and_the_operator_recovers():
+    # failure detection without a GPU fault: HOE_INJECT_TC_STALL=4 makes the
+    # first forward contraction of the operator skip fetching the operands of
+    # CTA 0's fifth stage, with every wait limited to 1 ms.  The waits for that
+    # stage run out, the kernel sets its abort flag, drains its own copies and
+    # MMAs, frees tensor memory and returns; hoe_check reports HOE_ERR_TIMEOUT.
+    # The injection is one-shot: the next products are correct.
+    maybe_skip("tc")
+    from hoexplicit import HoeError
+    from hoexplicit import _lib as L
+    w = workloads.small(seed=12, shape=(64, 64, 1), nSam=4000, nCha=8, nTerm=16)  # ~13 stages per CTA
+    os.environ["HOE_INJECT_TC_STALL"] = "4"
+    try:
+        op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    finally:
+        del os.environ["HOE_INJECT_TC_STALL"]
+    x = dev(w.x)
+    op * x
+    with pytest.raises(HoeError) as exc:
+        op.check()
+    assert f"[{L.HOE_ERR_TIMEOUT}]" in str(exc.value)
+    op.check()   # the error word was cleared after reporting
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    rows = np.sort(np.random.default_rng(2).choice(w.nSam, 64, replace=False))
+    mr = oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=w.kspha.shape[0])
+    y_first = None
+    for _ in range(2):
+        yfull = host(op * x)
+        y = yfull.reshape(w.nCha, w.nSam)[:, rows].reshape(-1)
+        assert dense.rel(y, oracle.forward(mr, w.x[idx])) < TOL["tc"]
+        if y_first is not None:
+            assert np.array_equal(yfull, y_first)
+        y_first = yfull
+    op.check()
+    op.close()
