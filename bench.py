@@ -47,8 +47,8 @@ L2_FLUSH_BYTES = 256 << 20
 # taken on.  A figure is used only when that hash equals the hash of the
 # sources in this tree; otherwise the bench reports null and says why.
 KERNEL_SOURCES = {
-    "tc": ("hoe_tc_kernel.cuh", "hoe_tc.cu", "hoe_tcgen05.cuh", "hoe_internal.cuh", "hoe_api.cu"),
-    "fp32": ("hoe_simt.cu", "hoe_internal.cuh", "hoe_api.cu"),
+    "tc": ("hoe_tc_kernel.cuh", "hoe_tc.cu", "hoe_tcgen05.cuh"),
+    "fp32": ("hoe_simt.cu", "hoe_internal.cuh"),
 }
 NCU_FIGURES = ROOT / "profiles" / "ncu_figures.txt"
 
@@ -109,6 +109,8 @@ def parse_args():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the second engine")
     ap.add_argument("--no-recon", action="store_true", help="skip timing the device CGNR solve")
     ap.add_argument("--recon-iterations", type=int, default=20)
+    ap.add_argument("--no-recon-check", action="store_true",
+                    help="skip the FP64 check of the CGNR image (about a minute of host time at 200x200)")
     ap.add_argument("--autotune", action="store_true",
                     help="time every execution plan on the workload and keep the fastest (always on for config 3)")
     a = ap.parse_args()
@@ -321,7 +323,27 @@ def time_recon(op, w, y, flush, stream, iterations, reps):
                     "launches_per_solve": (op.timings()["launches"] - l0) / reps,
                     "status": st["status"], "residual_ratio": st["residual"] / max(st["residual0"], 1e-300)}
     res["graph_speedup"] = res["direct"]["ms_per_solve"] / res["graph"]["ms_per_solve"]
+    # the inputs and the image of the last solve, for the FP64 check
+    res["_check"] = (data.cpu().numpy(), weight.cpu().numpy(), out.cpu().numpy())
     return res
+
+
+def recon_fp64_check(w, data, weight, x_gpu, iterations: int):
+    """Relative L2 error of the device CGNR image against the oracle's FP64
+    CGNR of recon_HOOp on the same data and weights (the checker)."""
+    from hoexplicit import workloads
+    from oracle import dense, oracle
+    from oracle import recon as orecon
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    m = oracle.Model(bf, k, t, f, c, nTerm=w.kspha.shape[0])
+    t0 = time.perf_counter()
+    y = np.asarray(data, dtype=np.complex128).T.reshape(-1)   # (nSam, nCha) -> samples fastest
+    xo, so = orecon.recon(m, y, np.asarray(weight, dtype=np.complex128), iterations=iterations,
+                          rel_tol=0.0, lam=1e-9)
+    return {"image_rel_err_vs_fp64": dense.rel(np.asarray(x_gpu, dtype=np.complex128)[idx], xo),
+            "fp64_residual_ratio": so["residual"] / max(so["residual0"], 1e-300),
+            "fp64_seconds": time.perf_counter() - t0,
+            "note": "FP64 CGNR (same recurrence and iterations) over the oracle's operator, all host cores"}
 
 
 def run_batch(a):
@@ -767,10 +789,16 @@ def run_gb300(a):
                                           "ms_per_step": res["alloc"] * 1e3,
                                           "value": ws * units / res["alloc"]}}
 
+    check = out["recon"].pop("_check", None) if isinstance(out.get("recon"), dict) else None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(w, a.cpu_seconds, x, y, op)
         acc = {k: out["cpu_baseline"].pop(k) for k in list(out["cpu_baseline"]) if k.startswith("gpu_")}
         out["accuracy_vs_fp64"] = acc
+        if check is not None and not a.no_recon_check:
+            try:
+                out["recon"]["accuracy"] = recon_fp64_check(w, *check, a.recon_iterations)
+            except Exception as exc:  # report, do not substitute
+                out["recon"]["accuracy"] = {"error": str(exc)}
     if rank == 0:
         print(json.dumps(out), flush=True)
     op.close()

@@ -308,7 +308,8 @@ __global__ void __launch_bounds__(256) k_tc_adj_reduce(const float2 *__restrict_
 }
 
 // Anchor tables of the anchor k-step: v = 2*pi*tab[i] (radians) split into
-// TF32 hi + lo, stored as [hi, lo, 1, 1] (format 0) or [1, 1, hi, lo] (format 1).
+// TF32 hi + lo, stored as [hi, lo] (8 bytes; the kernels supply the
+// constant halves of the k-step operands in shared memory).
 __device__ __forceinline__ float tf32_rn(float f) {
   uint32_t b = __float_as_uint(f);
   if ((b & 0x7f800000u) != 0x7f800000u) {
@@ -318,13 +319,13 @@ __device__ __forceinline__ float tf32_rn(float f) {
   return __uint_as_float(b);
 }
 
-__global__ void k_tc_anchor_tf32(const float *__restrict__ tab, int64_t n, float4 *__restrict__ out, int format) {
+__global__ void k_tc_anchor_tf32(const float *__restrict__ tab, int64_t n, float2 *__restrict__ out) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double v = 6.283185307179586476925 * (double)tab[i];
   const float h = tf32_rn((float)v);
   const float l = tf32_rn((float)(v - (double)h));
-  out[i] = format == 0 ? make_float4(h, l, 1.f, 1.f) : make_float4(1.f, 1.f, h, l);
+  out[i] = make_float2(h, l);
 }
 
 int tc_ncha(int nCha) {
@@ -374,7 +375,7 @@ cudaError_t tc_prepare(hoe_handle *h) {
   b.partElems = std::max((size_t)b.slotsF * t.nSamPad, (size_t)b.slotsA * t.nVoxPad) * t.nChaPad;
   const size_t nAP = (size_t)t.nVt * t.nSamPad, nBQ = (size_t)t.nSt * t.nVoxPad;
   size_t bytes = b.bopFElems * 2 + 256 + b.bopAElems * 2 + 256 + b.partElems * sizeof(float2) + 256 + 256 +
-                 (nAP + nBQ) * 16 + 512;
+                 (nAP + nBQ) * 8 + 512;
   unsigned char *buf = nullptr;
   cudaError_t e = cudaMalloc(&buf, bytes);
   if (e != cudaSuccess) return e;
@@ -384,8 +385,8 @@ cudaError_t tc_prepare(hoe_handle *h) {
   b.bopA = (uint16_t *)take(b.bopAElems * 2);
   b.part = (float2 *)take(b.partElems * sizeof(float2));
   b.err = (int *)take(sizeof(int));
-  b.AtabP = (float *)take(nAP * 16);
-  b.BtabQ = (float *)take(nBQ * 16);
+  b.AtabP = (float *)take(nAP * 8);
+  b.BtabQ = (float *)take(nBQ * 8);
   e = cudaMemset(b.err, 0, sizeof(int));
   if (e != cudaSuccess) { cudaFree(buf); return e; }
   h->tc.buf = buf;
@@ -854,8 +855,8 @@ cudaError_t tc_anchor_tables(const hoe_handle *h, cudaStream_t st) {
   const auto &t = h->t;
   const TcBuffers &b = *(const TcBuffers *)h->tc_host;
   const int64_t nAP = (int64_t)t.nVt * t.nSamPad, nBQ = (int64_t)t.nSt * t.nVoxPad;
-  k_tc_anchor_tf32<<<(unsigned)((nAP + 255) / 256), 256, 0, st>>>(t.Atab, nAP, (float4 *)b.AtabP, 0);
-  k_tc_anchor_tf32<<<(unsigned)((nBQ + 255) / 256), 256, 0, st>>>(t.Btab, nBQ, (float4 *)b.BtabQ, 1);
+  k_tc_anchor_tf32<<<(unsigned)((nAP + 255) / 256), 256, 0, st>>>(t.Atab, nAP, (float2 *)b.AtabP);
+  k_tc_anchor_tf32<<<(unsigned)((nBQ + 255) / 256), 256, 0, st>>>(t.Btab, nBQ, (float2 *)b.BtabQ);
   h->launches += 2;
   return cudaGetLastError();
 }

@@ -96,7 +96,7 @@ constexpr int bw_stages() {
 
 struct BwParams {
   const float *kpHi, *kpLo, *dbHi, *dbLo;   // TF32 residual tables (row side: samples)
-  const float *AtabP, *BtabQ;               // anchor tables (TF32 [hi, lo, 1, 1] / [1, 1, hi, lo])
+  const float *AtabP, *BtabQ;               // anchor tables (TF32 [hi, lo] pairs)
   const uint16_t *ra;                       // [nSt][hi,lo][128 x KC] A of the W product
   const uint16_t *zb;                       // [nChunks][hi,lo][128 x KC] B of the W product
   const uint16_t *fb;                       // [nChunks][hi,lo][32 x 64] basis tiles
@@ -179,14 +179,18 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // the second core-matrix column of every anchor k-step operand is zero
+  // anchor k-step operands, per stage slot: row side [a_hi, a_lo, 1, 1 | 0],
+  // column side [1, 1, c_hi, c_lo | 0]; the constant halves and the zero
+  // core-matrix columns once, the [hi, lo] halves by the loader per stage
   for (int i = threadIdx.x; i < NS * (S::XR + S::XC) / 16; i += BW_THREADS) {
     const int nr = NS * S::XR / 16;
-    float4 *dst = i < nr
-        ? reinterpret_cast<float4 *>(smem + S::XR_OFF + (size_t)(i / (S::XR / 16)) * 2 * S::XR + S::XR) + i % (S::XR / 16)
-        : reinterpret_cast<float4 *>(smem + S::XC_OFF + (size_t)((i - nr) / (S::XC / 16)) * 2 * S::XC + S::XC) +
-              (i - nr) % (S::XC / 16);
-    *dst = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool isRow = i < nr;
+    const int slot = isRow ? i / (S::XR / 16) : (i - nr) / (S::XC / 16);
+    const int e = isRow ? i % (S::XR / 16) : (i - nr) % (S::XC / 16);
+    float4 *base = isRow ? reinterpret_cast<float4 *>(smem + S::XR_OFF + (size_t)slot * 2 * S::XR)
+                         : reinterpret_cast<float4 *>(smem + S::XC_OFF + (size_t)slot * 2 * S::XC);
+    base[e] = isRow ? make_float4(0.f, 0.f, 1.f, 1.f) : make_float4(1.f, 1.f, 0.f, 0.f);
+    base[(isRow ? S::XR : S::XC) / 16 + e] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == BW_PISS) {
@@ -449,38 +453,70 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
     }
     __syncwarp();
   } else if (warp == BW_LOAD) {
-    // ---------------- loader: row-tile tables per row tile, stage operands per stage
-    if (lane == 0) {
-      const uint32_t stageBytes = 2 * S::ZB + 2 * S::CV + S::XR + S::XC;
+    // ---------------- loader: row-tile tables per row tile, stage operands
+    // per stage (whole warp; the anchors are fetched one stage ahead by all
+    // lanes as TF32 [hi, lo] pairs, the elected lane issues the bulk copies)
+    {
+      const bool leader = elect_one();
+      const uint32_t stageBytes = 2 * S::ZB + 2 * S::CV;
       int issued = 0, kcount = -1, rowIssued = -1, rt = rt0, ch = ch0;
+      float2 ar[TM / 32], ac[TV / 32];
+      auto fetch = [&](int frt, int fch) {
+        const float2 *rx = reinterpret_cast<const float2 *>(p.AtabP) + (int64_t)(fch * TV / 128) * p.nSamPad +
+                           (int64_t)frt * TM;
+        const float2 *cx = reinterpret_cast<const float2 *>(p.BtabQ) + (int64_t)frt * p.nVoxPad + (int64_t)fch * TV;
+#pragma unroll
+        for (int j = 0; j < TM / 32; ++j) ar[j] = __ldg(rx + lane + 32 * j);
+#pragma unroll
+        for (int j = 0; j < TV / 32; ++j) ac[j] = __ldg(cx + lane + 32 * j);
+      };
+      if (nIter > 0) fetch(rt, ch);
       for (int it = 0; it < nIter; ++it) {
         if (it > 0 && ++ch == p.nChunks) { ch = 0; ++rt; }
         if (it == 0 || ch == 0) {
           // one buffer: the previous row tile's W and residual MMAs must be done
           ++kcount;
-          if (kcount >= 1 && !wait_bar(&rfree[0], (kcount - 1) & 1, abort, p.err)) break;
-          mbar_expect_tx(&rfull[0], 2 * S::RV + 2 * S::RA);
-          const size_t ro = (size_t)rt * TM * KP;
-          bulk_g2s(smem + S::RV_OFF, p.kpHi + ro, S::RV, &rfull[0]);
-          bulk_g2s(smem + S::RV_OFF + S::RV, p.kpLo + ro, S::RV, &rfull[0]);
-          bulk_g2s(smem + S::RA_OFF, p.ra + (size_t)rt * 2 * TM * KC, 2 * S::RA, &rfull[0]);
+          if (kcount >= 1 && !wait_bar_warp(&rfree[0], (kcount - 1) & 1, abort, p.err)) break;
+          if (leader) {
+            mbar_expect_tx(&rfull[0], 2 * S::RV + 2 * S::RA);
+            const size_t ro = (size_t)rt * TM * KP;
+            bulk_g2s(smem + S::RV_OFF, p.kpHi + ro, S::RV, &rfull[0]);
+            bulk_g2s(smem + S::RV_OFF + S::RV, p.kpLo + ro, S::RV, &rfull[0]);
+            bulk_g2s(smem + S::RA_OFF, p.ra + (size_t)rt * 2 * TM * KC, 2 * S::RA, &rfull[0]);
+          }
+          __syncwarp();
           rowIssued = kcount;
         }
         const int slot = it % NS, round = it / NS;
-        if (round > 0 && !wait_bar(&empty[slot], (round - 1) & 1, abort, p.err)) break;
-        mbar_expect_tx(&full[slot], stageBytes);
-        bulk_g2s(smem + S::ZB_OFF + (size_t)slot * 2 * S::ZB, p.zb + (size_t)ch * 2 * TM * KC, 2 * S::ZB, &full[slot]);
-        const size_t co = (size_t)ch * TV * KP;
-        unsigned char *cv = smem + S::CV_OFF + (size_t)slot * 2 * S::CV;
-        bulk_g2s(cv, p.dbHi + co, S::CV, &full[slot]);
-        bulk_g2s(cv + S::CV, p.dbLo + co, S::CV, &full[slot]);
-        bulk_g2s(smem + S::XR_OFF + (size_t)slot * 2 * S::XR,
-                 p.AtabP + ((int64_t)(ch * TV / 128) * p.nSamPad + (int64_t)rt * TM) * 4, S::XR, &full[slot]);
-        bulk_g2s(smem + S::XC_OFF + (size_t)slot * 2 * S::XC,
-                 p.BtabQ + ((int64_t)rt * p.nVoxPad + (int64_t)ch * TV) * 4, S::XC, &full[slot]);
+        if (round > 0 && !wait_bar_warp(&empty[slot], (round - 1) & 1, abort, p.err)) break;
+        // anchors into the [hi, lo] halves of the slot's 16-byte rows, made
+        // visible to the tensor cores before the stage barrier's arrival
+        float2 *xr = reinterpret_cast<float2 *>(smem + S::XR_OFF + (size_t)slot * 2 * S::XR);
+        float2 *xc = reinterpret_cast<float2 *>(smem + S::XC_OFF + (size_t)slot * 2 * S::XC);
+#pragma unroll
+        for (int j = 0; j < TM / 32; ++j) xr[2 * (lane + 32 * j)] = ar[j];
+#pragma unroll
+        for (int j = 0; j < TV / 32; ++j) xc[2 * (lane + 32 * j) + 1] = ac[j];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (leader) {
+          mbar_expect_tx(&full[slot], stageBytes);
+          bulk_g2s(smem + S::ZB_OFF + (size_t)slot * 2 * S::ZB, p.zb + (size_t)ch * 2 * TM * KC, 2 * S::ZB,
+                   &full[slot]);
+          const size_t co = (size_t)ch * TV * KP;
+          unsigned char *cv = smem + S::CV_OFF + (size_t)slot * 2 * S::CV;
+          bulk_g2s(cv, p.dbHi + co, S::CV, &full[slot]);
+          bulk_g2s(cv + S::CV, p.dbLo + co, S::CV, &full[slot]);
+        }
+        __syncwarp();
         issued = it + 1;
+        if (it + 1 < nIter) {
+          int nrt = rt, nch = ch + 1;
+          if (nch == p.nChunks) { nch = 0; ++nrt; }
+          fetch(nrt, nch);
+        }
       }
-      if (*abort) {
+      if (*abort && leader) {
         for (int it = max(0, issued - NS); it < issued; ++it) drain_bar(&full[it % NS], (it / NS) & 1);
         if (rowIssued >= 0) drain_bar(&rfull[0], rowIssued & 1);
       }

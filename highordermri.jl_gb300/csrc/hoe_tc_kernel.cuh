@@ -99,8 +99,8 @@ struct Warps {
 struct TcSlice {
   const float *rowHi, *rowLo;   // TF32 row-side residual tables: kappa (forward) / dbeta (adjoint)
   const float *colHi, *colLo;   // TF32 column-side residual tables: dbeta (forward) / kappa (adjoint)
-  const float *rowX;            // [colTile][rowXStride][4] TF32 anchor rows: AtabP (forward) / BtabQ (adjoint)
-  const float *colX;            // [rowTile][colXStride][4] TF32 anchor columns: BtabQ (forward) / AtabP (adjoint)
+  const float *rowX;            // [colTile][rowXStride][2] TF32 [hi, lo] anchor rows: AtabP (forward) / BtabQ (adjoint)
+  const float *colX;            // [rowTile][colXStride][2] TF32 [hi, lo] anchor columns: BtabQ (forward) / AtabP (adjoint)
   const uint16_t *Bop;          // [nColChunks][hi,lo][N x TK] BF16 tiles, canonical layout
   float2 *part;                 // [slot][nRowPad][nChaPad] partial sums (zeroed before launch)
   int64_t first;                // global index of the slice's first work item
@@ -346,13 +346,19 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // the second core-matrix column of every anchor k-step operand is zero
+  // anchor k-step operands, per stage slot: row side [a_hi, a_lo, 1, 1 | 0],
+  // column side [1, 1, c_hi, c_lo | 0].  The constant halves and the zero
+  // core-matrix columns are written here once; the loader writes the
+  // [hi, lo] halves per stage.
   for (int i = threadIdx.x; i < NS * (S::XR_BYTES + S::XC_BYTES) / 16; i += W::THREADS) {
     const int nr = NS * S::XR_BYTES / 16;
-    float4 *dst = i < nr
-        ? reinterpret_cast<float4 *>(sXR + (size_t)(i / (S::XR_BYTES / 16)) * 2 * S::XR_BYTES + S::XR_BYTES) + i % (S::XR_BYTES / 16)
-        : reinterpret_cast<float4 *>(sXC + (size_t)((i - nr) / (S::XC_BYTES / 16)) * 2 * S::XC_BYTES + S::XC_BYTES) + (i - nr) % (S::XC_BYTES / 16);
-    *dst = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool isRow = i < nr;
+    const int slot = isRow ? i / (S::XR_BYTES / 16) : (i - nr) / (S::XC_BYTES / 16);
+    const int e = isRow ? i % (S::XR_BYTES / 16) : (i - nr) % (S::XC_BYTES / 16);
+    float4 *base = isRow ? reinterpret_cast<float4 *>(sXR + (size_t)slot * 2 * S::XR_BYTES)
+                         : reinterpret_cast<float4 *>(sXC + (size_t)slot * 2 * S::XC_BYTES);
+    base[e] = isRow ? make_float4(0.f, 0.f, 1.f, 1.f) : make_float4(1.f, 1.f, 0.f, 0.f);
+    base[(isRow ? S::XR_BYTES : S::XC_BYTES) / 16 + e] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   if (warp == PISS_WARP) {
@@ -762,10 +768,26 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
     // lane issues the copies)
     {
       const bool leader = elect_one();
-      const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + S::XR_BYTES + S::XC_BYTES + S::BF_TILE;
+      const uint32_t stageBytes = 2 * S::B_TILE + 2 * S::CV_TILE + S::BF_TILE;
       int issued = 0, kcount = -1, rowIssued = -1;
       const int skip = b == 0 ? p.stallStage1 - 1 : -1;   // failure detection: never fetched
+      // the stage's anchors as TF32 [hi, lo] pairs (8 bytes each), fetched
+      // one stage ahead into registers: lane l holds rows l + 32 j of the
+      // row side and columns l + 32 j of the column side
+      float2 ar[TM / 32], ac[TV / 32];
+      auto fetch = [&](const Cursor<MS> &cc) {
+        const TcSlice &s2 = p.at(cc.si);
+        const float2 *rx = reinterpret_cast<const float2 *>(s2.rowX) +
+                           (int64_t)(cc.ch * TV / 128) * s2.rowXStride + (int64_t)cc.rt * TM;
+        const float2 *cx = reinterpret_cast<const float2 *>(s2.colX) +
+                           (int64_t)cc.rt * s2.colXStride + (int64_t)cc.ch * TV;
+#pragma unroll
+        for (int j = 0; j < TM / 32; ++j) ar[j] = __ldg(rx + lane + 32 * j);
+#pragma unroll
+        for (int j = 0; j < TV / 32; ++j) ac[j] = __ldg(cx + lane + 32 * j);
+      };
       Cursor<MS> c = c0;
+      if (nIter > 0) fetch(c);
       for (int it = 0; it < nIter; ++it) {
         if (it > 0) c.next(p);
         const TcSlice &sl = p.at(c.si);
@@ -785,21 +807,35 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
         }
         const int slot = it % NS, round = it / NS;
         if (round > 0 && !wait_bar_warp(&empty[slot], (round - 1) & 1, abort, p.err, lim)) break;
+        if (it != skip) {
+          // anchors into the [hi, lo] halves of the slot's 16-byte rows (row r
+          // at byte 16 r, column c's pair at byte 16 c + 8), made visible to
+          // the tensor cores before the stage barrier's arrival
+          float2 *xr = reinterpret_cast<float2 *>(sXR + (size_t)slot * 2 * S::XR_BYTES);
+          float2 *xc = reinterpret_cast<float2 *>(sXC + (size_t)slot * 2 * S::XC_BYTES);
+#pragma unroll
+          for (int j = 0; j < TM / 32; ++j) xr[2 * (lane + 32 * j)] = ar[j];
+#pragma unroll
+          for (int j = 0; j < TV / 32; ++j) xc[2 * (lane + 32 * j) + 1] = ac[j];
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        __syncwarp();
         if (leader && it != skip) {
           const size_t co = (size_t)ch * TV * KP;
           mbar_expect_tx(&full[slot], stageBytes);
           bulk_g2s(sB + (size_t)slot * 2 * S::B_TILE, sl.Bop + (size_t)ch * 2 * (N * TK), 2 * S::B_TILE, &full[slot]);
           bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, sl.colHi + co, S::CV_TILE, &full[slot]);
           bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, sl.colLo + co, S::CV_TILE, &full[slot]);
-          bulk_g2s(sXR + (size_t)slot * 2 * S::XR_BYTES,
-                   sl.rowX + ((int64_t)(ch * TV / 128) * sl.rowXStride + (int64_t)rt * TM) * 4, S::XR_BYTES, &full[slot]);
-          bulk_g2s(sXC + (size_t)slot * 2 * S::XC_BYTES,
-                   sl.colX + ((int64_t)rt * sl.colXStride + (int64_t)ch * TV) * 4, S::XC_BYTES, &full[slot]);
           if constexpr (DERIV)
             bulk_g2s(sBF + (size_t)slot * S::BF_TILE, p.bfT + (size_t)ch * KF * TV, S::BF_TILE, &full[slot]);
         }
         __syncwarp();
         issued = it + 1;
+        if (it + 1 < nIter) {
+          Cursor<MS> cn = c;
+          cn.next(p);
+          fetch(cn);
+        }
       }
       if (*abort) {
         // drain the copies still in flight into this CTA's shared memory

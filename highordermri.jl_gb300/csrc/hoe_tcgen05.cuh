@@ -17,7 +17,7 @@ namespace hoe {
 // Device buffers of the tensor-core engine for one operator (tc_prepare).
 struct TcBuffers {
   uint16_t *bopF = nullptr, *bopA = nullptr;
-  float *AtabP = nullptr, *BtabQ = nullptr;   // anchors in radians, TF32 [hi, lo, 1, 1] / [1, 1, hi, lo]
+  float *AtabP = nullptr, *BtabQ = nullptr;   // anchors in radians, TF32 [hi, lo] pairs
   float2 *part = nullptr;
   int *err = nullptr;
   int N = 0, nChaTC = 0;
