@@ -101,7 +101,7 @@ struct Scratch {
   size_t partElems = 0;
   float  *gpart = nullptr;   // backward partials
   size_t gpartElems = 0;
-  double *dred = nullptr;    // backward FP64 reduction slots
+  double *dred = nullptr;    // backward FP64 reduction slots (bwd_red_slots)
 };
 
 // Tensor-core operand staging (built lazily when the TC engine is selected).
@@ -305,6 +305,11 @@ void tc_backward_release(hoe_handle *h);
 // The reductions after either backward kernel: dk from nSplit partial slots
 // [nSplit][nSamPad][kRF], dL/dfieldmap and the fieldmap part of dL/dt0 from
 // nRows partial rows [nRows][nVoxPad] of sum_s G and sum_s G t_s, and dL/dt0.
+// FP64 block partials of the backward's final reductions: the voxel blocks
+// of k_bwd_vox, then the blocks of k_bwd_dk (the t0 coefficient part).
+inline int64_t bwd_red_slots(const Tables &t) {
+  return (t.nVoxPad + 255) / 256 + ((int64_t)t.nSamPad * kRF + 255) / 256 + 1;
+}
 cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const float *g1, const float *gt, int nRows,
                        double *vpart, double *dred, float *dk, float *ddf, double *dt0, int flags, cudaStream_t st);
 constexpr int kBwdVoxSplit = 16;   // row ranges of the first voxel reduction pass (vpart: 2 x 16 x nVoxPad)

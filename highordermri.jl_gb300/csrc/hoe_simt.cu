@@ -367,16 +367,32 @@ k_bwd_simt(const float *__restrict__ kappa, const float *__restrict__ dbeta,
   for (int l = 0; l < kRF; ++l) dst[l] = dk[l];
 }
 
-__global__ void k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamPad, int R0,
-                         int nSam, float *__restrict__ dk) {
+// dL/dkspha from the split partials (dk, when given) and, when coefPart is
+// given, the coefficient part of dL/dt0, -sum_{l < nTerm, s} kdot[l,s] dk[l,s],
+// as one FP64 partial per block (summed in a fixed order by k_bwd_t0).
+__global__ void __launch_bounds__(256) k_bwd_dk(const float *__restrict__ dkpart, int nSplit, int nSamPad, int R0,
+                                                int nSam, float *__restrict__ dk, const float *__restrict__ kdot,
+                                                int nTerm, double *__restrict__ coefPart) {
   pdl_wait();
   pdl_trigger();
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)nSam * R0) return;
-  int s = (int)(i / R0), l = (int)(i % R0);
-  float acc = 0.f;
-  for (int k = 0; k < nSplit; ++k) acc += dkpart[((int64_t)k * nSamPad + s) * kRF + l];
-  dk[(int64_t)s * R0 + l] = acc;  // [nTermEff x nSam] column-major
+  __shared__ double red[256];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double c = 0.0;
+  if (i < (int64_t)nSam * R0) {
+    const int s = (int)(i / R0), l = (int)(i % R0);
+    float acc = 0.f;
+    for (int k = 0; k < nSplit; ++k) acc += dkpart[((int64_t)k * nSamPad + s) * kRF + l];
+    if (dk) dk[(int64_t)s * R0 + l] = acc;  // [nTermEff x nSam] column-major
+    if (coefPart && l < nTerm) c = -(double)kdot[(int64_t)s * kRF + l] * (double)acc;
+  }
+  if (!coefPart) return;   // uniform over the block
+  red[threadIdx.x] = c;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) coefPart[blockIdx.x] = red[0];
 }
 
 // Per voxel: dL/dfieldmap and the fieldmap part of dL/dt0 (block partials in FP64).
@@ -432,23 +448,18 @@ __global__ void k_bwd_vox(const double *__restrict__ vpart, int nVoxPad, const i
   if (threadIdx.x == 0) blockAcc[blockIdx.x] = red[0];
 }
 
+// dL/dt0: the fieldmap part from k_bwd_vox's block partials (useB0) plus
+// the coefficient part from k_bwd_dk's block partials (nCoef > 0), summed by
+// one block in a fixed order.
 __global__ void k_bwd_t0(const double *__restrict__ blockAcc, int nBlocks, int useB0,
-                         const float *__restrict__ dkpart, int nSplit, int nSamPad,
-                         const float *__restrict__ kdot, int nSam, int nTerm, int useCoef,
-                         double *__restrict__ dt0) {
+                         const double *__restrict__ coefPart, int nCoef, double *__restrict__ dt0) {
   pdl_wait();
   pdl_trigger();
   __shared__ double red[256];
   double acc = 0.0;
   if (useB0)
     for (int i = threadIdx.x; i < nBlocks; i += blockDim.x) acc += blockAcc[i];
-  if (useCoef)
-    for (int64_t i = threadIdx.x; i < (int64_t)nSam * nTerm; i += blockDim.x) {
-      int s = (int)(i / nTerm), l = (int)(i % nTerm);
-      double g = 0.0;
-      for (int k = 0; k < nSplit; ++k) g += dkpart[((int64_t)k * nSamPad + s) * kRF + l];
-      acc -= (double)kdot[(int64_t)s * kRF + l] * g;
-    }
+  for (int i = threadIdx.x; i < nCoef; i += blockDim.x) acc += coefPart[i];
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int o = 128; o > 0; o >>= 1) {
@@ -610,10 +621,10 @@ cudaError_t simt_backward(const hoe_handle *hc, const float2 *, const float2 *r,
     h->s.gpart = nullptr; h->s.dred = nullptr; h->s.gpartElems = 0;
     cudaError_t e = cudaMalloc(&h->s.gpart, need * sizeof(float));
     if (e != cudaSuccess) return e;
-    e = cudaMalloc(&h->s.dred, (size_t)(nVB + 1) * sizeof(double));
+    e = cudaMalloc(&h->s.dred, (size_t)bwd_red_slots(t) * sizeof(double));
     if (e != cudaSuccess) return e;
     h->s.gpartElems = need;
-    h->bytes += (int64_t)(need * sizeof(float) + (nVB + 1) * sizeof(double));
+    h->bytes += (int64_t)(need * sizeof(float) + bwd_red_slots(t) * sizeof(double));
   }
   cudaError_t e = prep_Yt(h, r, nullptr, st);
   if (e != cudaSuccess) return e;
@@ -636,15 +647,17 @@ cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const flo
   const auto &t = h->t;
   const int nVB = (t.nVoxPad + 255) / 256;
   cudaError_t e = cudaSuccess;
-  h->launches += 2 + ((flags & HOE_GRAD_KSPHA) ? 1 : 0) + ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
+  const bool coef = (flags & HOE_GRAD_T0_COEF) != 0;
+  h->launches += 2 + ((flags & HOE_GRAD_KSPHA) || coef ? 1 : 0) + ((flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF)) ? 1 : 0);
   // programmatic dependent launches: each kernel waits for its predecessor
   // before its first global access (pdl_wait)
   auto ok = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
-  if (flags & HOE_GRAD_KSPHA) {
-    int64_t n = (int64_t)t.nSam * t.R0;
-    ok(launch_pdl(k_bwd_dk, dim3((unsigned)((n + 255) / 256)), dim3(256), 0, st, dkpart, nSplit, t.nSamPad, t.R0,
-                  t.nSam, dk));
-  }
+  const int64_t nDk = (int64_t)t.nSam * t.R0;
+  const int nCoef = coef ? (int)((nDk + 255) / 256) : 0;   // block partials after the nVB voxel ones
+  if ((flags & HOE_GRAD_KSPHA) || coef)
+    ok(launch_pdl(k_bwd_dk, dim3((unsigned)((nDk + 255) / 256)), dim3(256), 0, st, dkpart, nSplit, t.nSamPad, t.R0,
+                  t.nSam, (flags & HOE_GRAD_KSPHA) ? dk : (float *)nullptr, (const float *)t.kdot, t.nTerm,
+                  coef ? dred + nVB : (double *)nullptr));
   float *ddfOut = (flags & HOE_GRAD_FIELDMAP) ? ddf : nullptr;
   ok(launch_pdl(k_bwd_rows, dim3(nVB, kBwdVoxSplit), dim3(256), 0, st, g1, gt, nRows, t.nVoxPad, vpart, ddfOut,
                 (const int *)t.unmasked, t.nUnmasked));
@@ -652,8 +665,7 @@ cudaError_t bwd_finish(hoe_handle *h, const float *dkpart, int nSplit, const flo
                 (const float *)t.bfraw, t.R0, ddfOut, dred));
   if (flags & (HOE_GRAD_T0_B0 | HOE_GRAD_T0_COEF))
     ok(launch_pdl(k_bwd_t0, dim3(1), dim3(256), 0, st, (const double *)dred, nVB, (flags & HOE_GRAD_T0_B0) ? 1 : 0,
-                  dkpart, nSplit, t.nSamPad, (const float *)t.kdot, t.nSam, t.nTerm,
-                  (flags & HOE_GRAD_T0_COEF) ? 1 : 0, dt0));
+                  (const double *)(dred + nVB), nCoef, dt0));
   return e;
 }
 

@@ -17,9 +17,11 @@
 //     columns are (Re W, Im W) per voxel, both from shared memory;
 //   * 16 phase warps (two groups on alternate stages) read phi and W from
 //     tensor memory, form G, write it as BF16 hi/lo into a shared-memory A
-//     tile and sum G and G t over their 32 rows (a butterfly across the
-//     warp); the four row quarters of a tile store separate partial sums,
-//     which k_bwd_vox adds in a fixed order (no wait between warps);
+//     tile and sum G and G t over their 32 rows with warp MMAs (mma.sync
+//     m16n8k16: A = rows of ones, t_hi and t_lo; B = their part of the G tile
+//     read back transposed by ldmatrix); the four row quarters of a tile
+//     store separate partial sums, which k_bwd_vox adds in a fixed order (no
+//     wait between warps);
 //   * the dk issuer contracts G with the basis tile: hi x [bf_hi | bf_lo] as
 //     one 64-wide MMA and lo x bf_hi, into one accumulator set that the phase
 //     warps add into FP32 registers every 32 stages.
@@ -107,22 +109,6 @@ struct BwParams {
   int nSt, nChunks, nSamPad, nVoxPad;
   float scaleG;
 };
-
-// Column sums over the warp's 32 rows of 32 values per lane: afterwards lane
-// L holds the sum of column L (a butterfly that halves the vector per step).
-__device__ __forceinline__ float warp_column_sum(float (&a)[32], int lane) {
-#pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int i = 0; i < o; ++i) {
-      const float send = up ? a[i] : a[i + o];
-      const float keep = up ? a[i + o] : a[i];
-      a[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-    }
-  }
-  return a[0];
-}
 
 template <int KC, int KP, int NS>
 __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_constant__ BwParams p) {
@@ -248,10 +234,35 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
       pendGrp = -1;
     };
     int rt = rt0, ch = ch0;
-    float ts = 0.f;   // sample time of this thread's row in the current row tile
+    // A fragments of the column-sum MMAs (mma.sync m16n8k16, rows = the
+    // fragment's groupID lane / 4): row 0 ones, row 1 t_hi(s), row 9 t_lo(s)
+    // for the warp's samples s of each 16-sample half kk, so that lanes 0-3
+    // end with sum_s G and lanes 4-7 with the hi and lo parts of sum_s G t
+    uint32_t ta[2][4];
+    const int g4 = lane >> 2, t4 = lane & 3;
     for (int it = 0; it < nIter && ok; ++it) {
       if (it > 0 && ++ch == p.nChunks) { ch = 0; ++rt; }
-      if (it == 0 || ch == 0) ts = p.times[(int64_t)rt * TM + row];
+      if (it == 0 || ch == 0) {
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk) {
+#pragma unroll
+          for (int h8 = 0; h8 < 2; ++h8) {   // k columns 2 t4 + {0, 1} (+ 8 h8)
+            const int s0 = q * 32 + kk * 16 + h8 * 8 + 2 * t4;
+            uint32_t hi = 0u, lo = 0u;
+            if (g4 == 0) {
+              hi = 0x3f803f80u;   // (1, 1) in BF16
+            } else if (g4 == 1) {
+              const float a = p.times[(int64_t)rt * TM + s0], c = p.times[(int64_t)rt * TM + s0 + 1];
+              const __nv_bfloat162 th = __floats2bfloat162_rn(a, c);
+              const __nv_bfloat162 tl = __floats2bfloat162_rn(a - __low2float(th), c - __high2float(th));
+              hi = *reinterpret_cast<const uint32_t *>(&th);
+              lo = *reinterpret_cast<const uint32_t *>(&tl);
+            }
+            ta[kk][2 * h8] = hi;       // rows groupID (0: ones, 1: t_hi)
+            ta[kk][2 * h8 + 1] = lo;   // rows groupID + 8 (9: t_lo)
+          }
+        }
+      }
       if (it == 0 || ch % BW_GROUP == 0) ++grp;
       if ((it & 1) == par) {
         const int pb = it & 1, pr = (it >> 1) & 1;
@@ -298,15 +309,43 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncwarp();
         if (lane == 0) mbar_arrive(&gfull[pb]);
-        // column sums of G and G*t over the tile's 128 rows
-        float gt[32];
+        // column sums of G and G t over the warp's 32 rows on the tensor cores:
+        // D[m, v] = sum_s A[m, s] G[s, v] from the G tile just written (BF16
+        // hi and lo, read back transposed by ldmatrix), FP32 accumulation
+        float acc[4][4];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) gt[j] = g[j] * ts;
-        const float s1 = warp_column_sum(g, lane);
-        const float st = warp_column_sum(gt, lane);
-        const int64_t o = ((int64_t)rt * 4 + q) * p.nVoxPad + (int64_t)ch * TV + half * 32 + lane;
-        p.g1part[o] = s1;
-        p.gtpart[o] = st;
+        for (int n = 0; n < 4; ++n)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) acc[n][i] = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < 2; ++kk) {
+#pragma unroll
+          for (int np = 0; np < 2; ++np) {
+            // lane L gives row L % 8 of core matrix L / 8: samples of group
+            // (L / 8) & 1 of this half, voxels of group L / 16 of this pair
+            const int sl = q * 32 + kk * 16 + ((lane >> 3) & 1) * 8 + (lane & 7);
+            const int vl = half * 32 + np * 16 + (lane >> 4) * 8;
+            const uint32_t off = kmaj(sl, vl, TV);
+            uint32_t h0, h1, h2, h3, l0, l1, l2, l3;
+            ldmatrix_x4_trans(smem_u32(gHi + off), h0, h1, h2, h3);
+            ldmatrix_x4_trans(smem_u32(gHi + S::GT + off), l0, l1, l2, l3);
+            mma_bf16_16816(acc[2 * np], ta[kk], h0, h1);
+            mma_bf16_16816(acc[2 * np], ta[kk], l0, l1);
+            mma_bf16_16816(acc[2 * np + 1], ta[kk], h2, h3);
+            mma_bf16_16816(acc[2 * np + 1], ta[kk], l2, l3);
+          }
+        }
+        // lanes 0-3: sum_s G (row 0); lanes 4-7: sum_s G t (rows 1 + 9), for
+        // the columns n*8 + 2 t4 + {0, 1} of the warp's 32
+        if (g4 < 2) {
+          float *dst = (g4 == 0 ? p.g1part : p.gtpart) + ((int64_t)rt * 4 + q) * p.nVoxPad + (int64_t)ch * TV +
+                       half * 32 + 2 * t4;
+#pragma unroll
+          for (int n = 0; n < 4; ++n)
+            *reinterpret_cast<float2 *>(dst + n * 8) =
+                g4 == 0 ? make_float2(acc[n][0], acc[n][1])
+                        : make_float2(acc[n][0] + acc[n][2], acc[n][1] + acc[n][3]);
+        }
       }
       if (pendGrp >= 0 && it >= pendIt + 1) flush();
       const bool endRT = (it == nIter - 1) || (ch + 1 == p.nChunks);
@@ -681,7 +720,7 @@ cudaError_t bw_prepare(hoe_handle *h) {
   const size_t raB = (size_t)t.nSamPad * b.KC * 2 * 2, zbB = (size_t)t.nVoxPad * 2 * b.KC * 2 * 2;
   const size_t fbB = (size_t)t.nVoxPad * BW_NF * 2 * 2;
   const size_t dkB = (size_t)b.slots * t.nSamPad * kRF * 4, gB = (size_t)t.nSt * 4 * t.nVoxPad * 4;
-  const size_t redB = (size_t)(nVB + 1) * 8, vpB = (size_t)2 * kBwdVoxSplit * t.nVoxPad * 8;
+  const size_t redB = (size_t)bwd_red_slots(t) * 8, vpB = (size_t)2 * kBwdVoxSplit * t.nVoxPad * 8;
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
   b.bytes = al(raB) + al(zbB) + al(fbB) + al(dkB) + 2 * al(gB) + al(vpB) + al(redB);
   cudaError_t e = cudaMalloc(&b.mem, b.bytes);

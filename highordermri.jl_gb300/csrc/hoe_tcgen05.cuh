@@ -308,6 +308,26 @@ __device__ __forceinline__ uint64_t fma_f32x2(uint64_t a, uint64_t b, uint64_t c
   return d;
 }
 
+// Four 8x8 BF16 matrices from shared memory, transposed (ldmatrix): lanes
+// 8j..8j+7 give the 16-byte row addresses of matrix j; register j of lane t
+// then holds elements (2(t%4), t/4) and (2(t%4)+1, t/4) of matrix j, which is
+// the B fragment of mma.sync m16n8k16 for a matrix stored with K along rows.
+__device__ __forceinline__ void ldmatrix_x4_trans(uint32_t saddr, uint32_t &r0, uint32_t &r1, uint32_t &r2,
+                                                  uint32_t &r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(saddr)
+               : "memory");
+}
+
+// D[16x8] += A[16x16] B[16x8], BF16 operands, FP32 accumulation (warp MMA).
+__device__ __forceinline__ void mma_bf16_16816(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
 // CTA that owns work item w when W items are split into G contiguous ranges
 // [b*W/G, (b+1)*W/G).
 __host__ __device__ inline int work_owner(int64_t w, int64_t W, int G) {
