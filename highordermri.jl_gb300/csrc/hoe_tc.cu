@@ -647,18 +647,26 @@ cudaError_t tc_derivative_prepare(hoe_handle *h) {
   constexpr int ND = 128;
   if (b.memD) return cudaSuccess;
   if (b.N <= 32) {
-    if (tc_configure_deriv(t.KP, b.N) < 1) return cudaErrorInvalidConfiguration;
     const size_t bfB = ((size_t)t.nVoxPad * KF * sizeof(float) + 255) / 256 * 256;
-    const size_t kdB = (size_t)t.nSamPad * KF * sizeof(float);
-    b.bytesD = bfB + kdB;
+    const size_t kdB = ((size_t)t.nSamPad * KF * sizeof(float) + 255) / 256 * 256;
+    b.bytesD = bfB + kdB + KF * KF * sizeof(float);
     cudaError_t e = cudaMalloc(&b.memD, b.bytesD);
     if (e != cudaSuccess) { b.memD = nullptr; return e; }
     b.bfT = (float *)b.memD;
     b.kd1 = (float *)((unsigned char *)b.memD + bfB);
-    b.fusedD = true;
+    b.Md = (float *)((unsigned char *)b.memD + bfB + kdB);
     h->bytes += (int64_t)b.bytesD;
-    e = tc_deriv_tables(h, b.bfT, nullptr, 0);   // voxel side: fixed for the operator
-    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    // voxel side of the reduced basis: fixed for the operator
+    e = tc_deriv_basis(h, b.bfT, b.Md, &b.rankD, &b.kfD);
+    if (e == cudaSuccess && tc_configure_deriv(t.KP, b.N, b.kfD) < 1) e = cudaErrorInvalidConfiguration;
+    if (e == cudaSuccess) {
+      b.fusedD = true;
+    } else {
+      cudaFree(b.memD);
+      h->bytes -= (int64_t)b.bytesD;
+      b.memD = nullptr;
+      b.bfT = b.kd1 = b.Md = nullptr;
+    }
     return e;
   }
   const int bps = configure_kernel<1>(t.KP, ND);
@@ -681,15 +689,15 @@ cudaError_t tc_derivative(hoe_handle *h, const float2 *x, float2 *y, cudaStream_
   const TcBuffers &b = *(const TcBuffers *)h->tc_host;
   const auto &t = h->t;
   if (b.fusedD) {
-    // 2 pi kdot from the current kspha_dt (hoe_set_kspha may replace it)
-    e = tc_deriv_tables(h, nullptr, b.kd1, st);
+    // the reduced 2 pi kdot from the current kspha_dt (hoe_set_kspha may replace it)
+    e = tc_deriv_kdot(h, b.Md, b.kd1, st);
     if (e == cudaSuccess) e = bop_forward(h, b, x, st);
     if (e == cudaSuccess) {
       TcParams<1> p = single_params(h, b, slice_forward(h, b));
       p.bfT = b.bfT;
       p.kd1 = b.kd1;
       trace(h, EV_FK0, st);
-      e = tc_launch_deriv(h, p, t.KP, b.N, b.gridF, st);
+      e = tc_launch_deriv(h, p, t.KP, b.N, b.kfD, b.gridF, st);
       trace(h, EV_FK1, st);
     }
     if (e == cudaSuccess) e = reduce_forward(h, b, single_map_forward(h, b), y, nullptr, false, st);

@@ -118,9 +118,9 @@ struct TcParams {
   int *err;
   int64_t work;                 // all slices' work items, split evenly over gridDim.x CTAs
   int nSlices, nChaPad, nChaTC, pad;
-  // derivative product only (single slice, rows = samples): the basis of
-  // each column chunk, term-major [chunk][KF][TV] in tile order, and per
-  // sample row 2 pi kdot_l as [row][KF]
+  // derivative product only (single slice, rows = samples): the reduced
+  // basis of each column chunk, term-major [chunk][KFD][TV] in tile order,
+  // and per sample row the reduced 2 pi kdot as [row][KF] (first KFD used)
   const float *bfT;
   const float *kd1;
   // failure detection: every wait's limit in ns (0: the 2 s default), and a
@@ -143,9 +143,11 @@ int tc_configure_plan16(int KP, int plan);
 int tc_configure_plan32(int KP, int plan);
 
 // The derivative product's instances and tables (hoe_tc_deriv.cu).
-cudaError_t tc_launch_deriv(const hoe_handle *h, const TcParams<1> &p, int KP, int N, int G, cudaStream_t st);
-int tc_configure_deriv(int KP, int N);
-cudaError_t tc_deriv_tables(const hoe_handle *h, float *bfT, float *kd1, cudaStream_t st);
+cudaError_t tc_launch_deriv(const hoe_handle *h, const TcParams<1> &p, int KP, int N, int KFD, int G,
+                            cudaStream_t st);
+int tc_configure_deriv(int KP, int N, int KFD);
+cudaError_t tc_deriv_basis(const hoe_handle *h, float *bfT, float *Mdev, int *rank, int *kfd);
+cudaError_t tc_deriv_kdot(const hoe_handle *h, const float *Mdev, float *kd1, cudaStream_t st);
 
 namespace {
 
@@ -220,7 +222,7 @@ struct Tmem {
 // (nTerm <= 16, zero padded).
 constexpr int KF = 16;
 
-template <int N, int KP, int NS, bool DERIV = false, int V = 0>
+template <int N, int KP, int NS, int KFD = 0, int V = 0>
 struct Smem {
   static constexpr int ABUF = Tmem<N, V>::ABUF;
   // Residual widths up to 16: the row tile's TF32 residual vectors (hi, lo)
@@ -242,7 +244,7 @@ struct Smem {
   static constexpr size_t XR_OFF = RV_OFF + (size_t)2 * 2 * RV_TILE;
   static constexpr size_t XC_OFF = XR_OFF + (size_t)NS * 2 * XR_BYTES;
   // derivative product: the stage's basis tile [KF][TV] FP32 (term-major)
-  static constexpr int BF_TILE = DERIV ? KF * TV * 4 : 0;
+  static constexpr int BF_TILE = KFD * TV * 4;
   static constexpr size_t BF_OFF = XC_OFF + (size_t)NS * 2 * XC_BYTES;
   static constexpr size_t BAR_OFF = (BF_OFF + (size_t)NS * BF_TILE + 7) / 8 * 8;
   // pfull/pfree barriers: stage s uses barrier s % PB.  A parity wait for s
@@ -261,22 +263,24 @@ struct Smem {
   static constexpr size_t BYTES = MISC_OFF + 16 + 1024;  // + alignment slack
 };
 
-template <int N, int KP, bool DERIV = false, int V = 0>
+template <int N, int KP, int KFD = 0, int V = 0>
 constexpr int pick_stages() {
   return TcPlan<V>::NS ? TcPlan<V>::NS
-       : Smem<N, KP, 6, DERIV, V>::BYTES <= 227 * 1024 ? 6
-       : Smem<N, KP, 5, DERIV, V>::BYTES <= 227 * 1024 ? 5
-       : Smem<N, KP, 4, DERIV, V>::BYTES <= 227 * 1024 ? 4
-       : Smem<N, KP, 3, DERIV, V>::BYTES <= 227 * 1024 ? 3 : 2;
+       : Smem<N, KP, 6, KFD, V>::BYTES <= 227 * 1024 ? 6
+       : Smem<N, KP, 5, KFD, V>::BYTES <= 227 * 1024 ? 5
+       : Smem<N, KP, 4, KFD, V>::BYTES <= 227 * 1024 ? 4
+       : Smem<N, KP, 3, KFD, V>::BYTES <= 227 * 1024 ? 3 : 2;
 }
 
 // DERIV: the derivative product (array_operator.jl:216-218) in one pass of
 // the forward: the phase warps scale e^{i phi} by 2 pi i F[s,v] before the
 // BF16 split, F formed from the stage's basis tile and the row's kdot.
-template <int N, int KP, int NS, int MS, bool DERIV = false, int V = 0>
+template <int N, int KP, int NS, int MS, int KFD = 0, int V = 0>
 __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const __grid_constant__ TcParams<MS> p) {
+  constexpr bool DERIV = KFD > 0;
   static_assert(!DERIV || MS == 1, "the derivative product serves one operator per launch");
-  using S = Smem<N, KP, NS, DERIV, V>;
+  static_assert(KFD % 2 == 0 && KFD <= KF, "derivative factor terms");
+  using S = Smem<N, KP, NS, KFD, V>;
   using TM_ = Tmem<N, V>;
   constexpr int ABUF = S::ABUF, PD = S::PD, PB = S::PB, NISS = TM_::NISS;
   constexpr int ACCBUF = TM_::ACCBUF, NPART = TM_::NPART, ACCW = TM_::ACCW;
@@ -478,7 +482,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = 0ull;   // (0.f, 0.f)
 #pragma unroll
-      for (int l = 0; l < KF; ++l) {
+      for (int l = 0; l < KFD; ++l) {
         const uint64_t kp = pack_f32x2(kr[l], kr[l]);
         const float4 *b4 = reinterpret_cast<const float4 *>(bcol + l * TV);
 #pragma unroll
@@ -493,16 +497,17 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
     };
     Cursor<MS> c = c0;
     int kt = -1;   // row tiles whose residual vectors warps 0-3 wrote to TMEM
-    float kreg[DERIV ? KF : 1];   // derivative product: this row's 2 pi kdot
+    float kreg[DERIV ? KFD : 1];   // derivative product: this row's reduced 2 pi kdot
     for (int it = 0; it < nIter && ok; ++it) {
       if (it > 0) c.next(p);
       if constexpr (DERIV) {
         if (it == 0 || c.ch == 0) {
-          const float4 *k4 = reinterpret_cast<const float4 *>(p.kd1 + ((int64_t)c.rt * TM + row) * KF);
+          const float2 *k2 = reinterpret_cast<const float2 *>(p.kd1 + ((int64_t)c.rt * TM + row) * KF);
 #pragma unroll
-          for (int i = 0; i < KF / 4; ++i) {
-            const float4 v = __ldg(k4 + i);
-            kreg[4 * i] = v.x; kreg[4 * i + 1] = v.y; kreg[4 * i + 2] = v.z; kreg[4 * i + 3] = v.w;
+          for (int i = 0; i < KFD / 2; ++i) {
+            const float2 v = __ldg(k2 + i);
+            kreg[2 * i] = v.x;
+            kreg[2 * i + 1] = v.y;
           }
         }
       }
@@ -827,7 +832,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
           bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE, sl.colHi + co, S::CV_TILE, &full[slot]);
           bulk_g2s(sCV + (size_t)slot * 2 * S::CV_TILE + S::CV_TILE, sl.colLo + co, S::CV_TILE, &full[slot]);
           if constexpr (DERIV)
-            bulk_g2s(sBF + (size_t)slot * S::BF_TILE, p.bfT + (size_t)ch * KF * TV, S::BF_TILE, &full[slot]);
+            bulk_g2s(sBF + (size_t)slot * S::BF_TILE, p.bfT + (size_t)ch * KFD * TV, S::BF_TILE, &full[slot]);
         }
         __syncwarp();
         issued = it + 1;
@@ -858,19 +863,19 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
 // Every launch asks for at least 116 KB of shared memory, more than half of
 // an SM's, so that at most one CTA is resident per SM: each CTA allocates all
 // 512 tensor-memory columns.
-template <int N, int KP, bool DERIV = false, int V = 0>
+template <int N, int KP, int KFD = 0, int V = 0>
 struct Kern {
-  static constexpr int NS = pick_stages<N, KP, DERIV, V>();
-  static_assert(Smem<N, KP, NS, DERIV, V>::PD >= 1, "residual-phase look-ahead");
-  using S = Smem<N, KP, NS, DERIV, V>;
+  static constexpr int NS = pick_stages<N, KP, KFD, V>();
+  static_assert(Smem<N, KP, NS, KFD, V>::PD >= 1, "residual-phase look-ahead");
+  using S = Smem<N, KP, NS, KFD, V>;
   static_assert(S::BYTES <= 227 * 1024, "shared memory plan exceeds 227 KB");
   static constexpr size_t LAUNCH_BYTES = S::BYTES < 116 * 1024 ? 116 * 1024 : S::BYTES;
 };
 
-template <int N, int KP, int MS, bool DERIV = false, int V = 0>
+template <int N, int KP, int MS, int KFD = 0, int V = 0>
 cudaError_t launch_contract(const hoe_handle *h, const TcParams<MS> &p, int G, cudaStream_t st) {
-  using K = Kern<N, KP, DERIV, V>;
-  auto kern = k_tc_contract<N, KP, K::NS, MS, DERIV, V>;
+  using K = Kern<N, KP, KFD, V>;
+  auto kern = k_tc_contract<N, KP, K::NS, MS, KFD, V>;
   const cudaError_t e = launch_pdl(kern, dim3(G), dim3(Warps<N, V>::THREADS), K::LAUNCH_BYTES, st, p);
   h->launches += 1;
   return e;
@@ -878,10 +883,10 @@ cudaError_t launch_contract(const hoe_handle *h, const TcParams<MS> &p, int G, c
 
 // One-time per (process, instantiation): shared-memory limit; returns the
 // resident CTAs per SM.
-template <int N, int KP, int MS, bool DERIV = false, int V = 0>
+template <int N, int KP, int MS, int KFD = 0, int V = 0>
 int configure() {
-  using K = Kern<N, KP, DERIV, V>;
-  auto kern = k_tc_contract<N, KP, K::NS, MS, DERIV, V>;
+  using K = Kern<N, KP, KFD, V>;
+  auto kern = k_tc_contract<N, KP, K::NS, MS, KFD, V>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)K::LAUNCH_BYTES) != cudaSuccess)
     return 0;
   int nb = 0;
@@ -935,30 +940,31 @@ int configure_kernel(int KP, int N) {
 template <int N, int KP>
 cudaError_t launch_plan_nk(const hoe_handle *h, const TcParams<1> &p, int plan, int G, cudaStream_t st) {
   switch (plan) {
-    case 1: return launch_contract<N, KP, 1, false, 1>(h, p, G, st);
-    case 2: return launch_contract<N, KP, 1, false, 2>(h, p, G, st);
-    case 3: return launch_contract<N, KP, 1, false, 3>(h, p, G, st);
-    default: return launch_contract<N, KP, 1, false, 4>(h, p, G, st);
+    case 1: return launch_contract<N, KP, 1, 0, 1>(h, p, G, st);
+    case 2: return launch_contract<N, KP, 1, 0, 2>(h, p, G, st);
+    case 3: return launch_contract<N, KP, 1, 0, 3>(h, p, G, st);
+    default: return launch_contract<N, KP, 1, 0, 4>(h, p, G, st);
   }
 }
 template <int N, int KP>
 int configure_plan_nk(int plan) {
   switch (plan) {
-    case 1: return configure<N, KP, 1, false, 1>();
-    case 2: return configure<N, KP, 1, false, 2>();
-    case 3: return configure<N, KP, 1, false, 3>();
-    default: return configure<N, KP, 1, false, 4>();
+    case 1: return configure<N, KP, 1, 0, 1>();
+    case 2: return configure<N, KP, 1, 0, 2>();
+    case 3: return configure<N, KP, 1, 0, 3>();
+    default: return configure<N, KP, 1, 0, 4>();
   }
 }
 
-// The derivative product for up to 16 coils (N = 16 or 32).
-template <int KP>
-cudaError_t launch_deriv_n(const hoe_handle *h, const TcParams<1> &p, int N, int G, cudaStream_t st) {
-  return N == 16 ? launch_contract<16, KP, 1, true>(h, p, G, st) : launch_contract<32, KP, 1, true>(h, p, G, st);
+// The derivative product for up to 16 coils (N = 16 or 32), KFD = 6, 10 or
+// 16 terms of the reduced factor.
+template <int KP, int KFD>
+cudaError_t launch_deriv_nk(const hoe_handle *h, const TcParams<1> &p, int N, int G, cudaStream_t st) {
+  return N == 16 ? launch_contract<16, KP, 1, KFD>(h, p, G, st) : launch_contract<32, KP, 1, KFD>(h, p, G, st);
 }
-template <int KP>
-int configure_deriv_n(int N) {
-  return N == 16 ? configure<16, KP, 1, true>() : configure<32, KP, 1, true>();
+template <int KP, int KFD>
+int configure_deriv_nk(int N) {
+  return N == 16 ? configure<16, KP, 1, KFD>() : configure<32, KP, 1, KFD>();
 }
 }  // namespace
 }  // namespace hoe

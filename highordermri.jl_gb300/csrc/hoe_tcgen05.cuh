@@ -35,6 +35,8 @@ struct TcBuffers {
   float2 *partD = nullptr;
   float *bfT = nullptr;
   float *kd1 = nullptr;
+  float *Md = nullptr;      // reduced-basis rotation [KF x KF] of the one-pass path
+  int rankD = 0, kfD = 16;  // its rank and the kernel's term count (6, 10 or 16)
   bool fusedD = false;
   void *memD = nullptr;
   size_t bytesD = 0;
