@@ -538,7 +538,7 @@ def time_extras(w, x, reps=10):
         yd = torch.empty(opd.nrow, dtype=torch.complex64, device=x.device)
         ms = timed_ms(lambda: opd.prod_(yd, x))
         out["derivative"] = {"ms_per_call": ms, "value": w.nVox * w.nSam / (ms / 1e3), "unit": UNIT,
-                             "engine": ("tc (one pass: phase tile scaled by 2 pi i F, F on the CUDA cores)" if opd.nCha <= 16
+                             "engine": ("tc (one pass: phase tile scaled by 2 pi i F, F in the basis's reduced rank on the CUDA cores)" if opd.nCha <= 16
                                         else "tc (virtual-coil passes)") if opd.engine == "tc" else "fp32 (CUDA cores)"}
         opd.close()
     dt = float(w.times[1] - w.times[0])
@@ -670,13 +670,15 @@ def run_gb300(a):
         pipe_cycles = pipe_contract + mma_resid * 32
         t_mma = stages * mma_busiest * MMA_ISSUE_CYCLES / hz
         t_pipe = stages * pipe_cycles / hz
-        t_sfu = 2.0 * w.nVox * w.nSam / (16.0 * nsm * hz)
+        from hoexplicit.operator import sfu_rate
+        sfu = sfu_rate()   # measured sin/cos lane operations per clock per SM
+        t_sfu = 2.0 * w.nVox * w.nSam / (sfu * nsm * hz)
         inst, inst_src = ncu_figure("inst", w.name, engine, dom)
         t_issue = inst / (4.0 * nsm * hz) if inst else None
         dom_s = dom_ms / 1e3
         roofline["ceilings"] = [
             {"pipe": "sfu (MUFU sin/cos)", "ms": t_sfu * 1e3, "frac": t_sfu / dom_s,
-             "note": "2 MUFU ops per (voxel, sample), 16 per clock per SM"},
+             "note": f"2 MUFU ops per (voxel, sample) at the measured {sfu:.1f} per clock per SM (hoe_sfu_rate)"},
             {"pipe": "warp instruction issue", "ms": t_issue * 1e3 if t_issue else None,
              "frac": t_issue / dom_s if t_issue else None,
              "note": f"ncu warp instructions of one launch / (4 per clock per SM); {inst_src}"},
@@ -687,10 +689,10 @@ def run_gb300(a):
              "note": f"{mma_busiest} MMAs per stage on the busiest issuer x {MMA_ISSUE_CYCLES:.0f} cycles "
                      "(converged warp, elected lane, isolated)"},
         ]
-        roofline["binding"] = {"pipe": "phase generator (sfu + issue, latency-bound)", "frac": t_sfu / dom_s,
+        roofline["binding"] = {"pipe": "phase generator (sfu + issue) and the stage pipeline", "frac": t_sfu / dom_s,
                                "note": "timing variants: sin/cos removed or the lo split removed each cut the "
-                                       "kernel 11%; with the phase work removed it runs at 0.23 ms, and the "
-                                       "residual-phase MMA count then matters, not before"}
+                                       "kernel 11%; with the phase work removed it still takes 0.23 ms (the "
+                                       "tensor pipe alone needs 0.11)"}
     if engine == "fp32":
         sm_mhz = clk.summary().get("sm_mhz") or 1900.0
         fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12

@@ -1037,6 +1037,12 @@ int hoe_kdot_stencil(const double *traj, int64_t nField, int32_t nTerm, double d
   return finish(nullptr, e, "hoe_kdot_stencil");
 }
 
+int hoe_sfu_rate(double *lanes_per_clock_per_sm, void *stream) {
+  if (!lanes_per_clock_per_sm) return fail(nullptr, HOE_ERR_ARG, "lanes_per_clock_per_sm must not be NULL");
+  cudaError_t e = hoe::sfu_rate(lanes_per_clock_per_sm, (cudaStream_t)stream);
+  return finish(nullptr, e, "hoe_sfu_rate");
+}
+
 int hoe_interp_traj_time(const double *traj, int64_t nField, int32_t nTerm, double dt, double delTime,
                          const double *datatime, int64_t nData, double *out, int32_t layout, void *stream) {
   if (!traj || !datatime || !out) return fail(nullptr, HOE_ERR_ARG, "traj, datatime and out must be device pointers");

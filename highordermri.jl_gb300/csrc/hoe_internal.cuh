@@ -259,6 +259,7 @@ cudaError_t replan_samples(hoe_handle *h, const double *kspha, int ldk, const do
 
 // Trajectory preprocessing and delay estimation (hoe_sync.cu).
 cudaError_t kdot_stencil(const double *traj, int64_t n, int nTerm, double dt, double *out, cudaStream_t st);
+cudaError_t sfu_rate(double *lanesPerClkPerSm, cudaStream_t st);
 cudaError_t interp_akima(const double *traj, int64_t n, int nTerm, double dt, const double *delTimeDev,
                          double delTimeHost, const double *datatime, int64_t nData, double *out, int layout,
                          int ldo, const double *termMask, cudaStream_t st);

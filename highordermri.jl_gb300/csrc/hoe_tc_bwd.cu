@@ -114,7 +114,7 @@ template <int KC, int KP, int NS>
 __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_constant__ BwParams p) {
   using S = BwSmem<KC, KP, NS>;
   extern __shared__ unsigned char smem_raw[];
-  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char *smem = align_smem_1024(smem_raw);
   constexpr int NF = S::NF;
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + S::BAR_OFF);
   uint64_t *empty = full + NS;        // [NS] stage read by the W and residual-phase MMAs

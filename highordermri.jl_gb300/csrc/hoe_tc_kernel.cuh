@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
   constexpr int CISS_WARP = W::CISS, PISS_WARP = W::PISS, LOAD_WARP = W::LOAD;
   static_assert(PD >= 1, "residual-phase look-ahead");
   extern __shared__ unsigned char smem_raw[];
-  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char *smem = align_smem_1024(smem_raw);
   unsigned char *sB = smem + S::B_OFF;
   unsigned char *sCV = smem + S::CV_OFF;
   unsigned char *sRV = smem + S::RV_OFF;

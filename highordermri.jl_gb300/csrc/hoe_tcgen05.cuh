@@ -77,6 +77,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// The dynamic shared-memory base rounded up to 1024 bytes by pointer
+// arithmetic on the shared array itself.  The compiler then keeps the shared
+// address space for every pointer derived from it; rounding through an
+// integer yields a generic pointer, and each access through that becomes a
+// generic load or store (tracked like a global access, with its latency).
+__device__ __forceinline__ unsigned char *align_smem_1024(unsigned char *raw) {
+  return raw + ((1024u - (smem_u32(raw) & 1023u)) & 1023u);
+}
+
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
   // D = F32, A = B = TF32 (2 at bits 7-9, 10-12), K-major, N>>3 at 17, M>>4 at 24
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);

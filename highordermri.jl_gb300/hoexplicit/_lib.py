@@ -39,7 +39,7 @@ EXPORTED = (
     "hoe_batch_create", "hoe_batch_free", "hoe_batch_last_error", "hoe_batch_get_info",
     "hoe_batch_forward", "hoe_batch_adjoint", "hoe_batch_normal", "hoe_batch_recon", "hoe_batch_check",
     "hoe_set_kspha", "hoe_kdot_stencil", "hoe_interp_traj_time", "hoe_find_delay", "hoe_autotune",
-    "hoe_coil_gram", "hoe_coil_fit", "hoe_coil_apply",
+    "hoe_coil_gram", "hoe_coil_fit", "hoe_coil_apply", "hoe_sfu_rate",
 )
 
 HOE_CG_ITERATION_LIMIT = 0
@@ -214,6 +214,7 @@ def load():
                                  ctypes.c_double, DP, DP, ctypes.POINTER(ctypes.c_int32), DP, vp]
     lib.hoe_coil_apply.argtypes = [vp, I64, ctypes.c_int32, vp, ctypes.c_int32, vp, vp]
     lib.hoe_kdot_stencil.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, vp, vp]
+    lib.hoe_sfu_rate.argtypes = [DP, vp]
     lib.hoe_interp_traj_time.argtypes = [vp, I64, ctypes.c_int32, ctypes.c_double, ctypes.c_double, vp, I64, vp,
                                          ctypes.c_int32, vp]
     lib.hoe_find_delay.argtypes = [H, ctypes.POINTER(HoeDelayParams), vp, vp, vp, I64, vp,

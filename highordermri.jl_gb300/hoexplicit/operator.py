@@ -202,6 +202,17 @@ def plan(grid: Grid, kspha, times, **kwargs) -> dict:
     return {name: getattr(inf, name) for name, _ in inf._fields_}
 
 
+def sfu_rate(stream=None) -> float:
+    """sin/cos rate of the special-function unit of the current CUDA device
+    (hoe_sfu_rate), in lane operations per clock per SM: the denominator of
+    the phase generator's ceiling (2 operations per voxel-sample pair)."""
+    torch = _torch()
+    st = stream if stream is not None else torch.cuda.current_stream()
+    out = ctypes.c_double(0.0)
+    _lib.check(_lib.load().hoe_sfu_rate(ctypes.byref(out), ctypes.c_void_p(st.cuda_stream)))
+    return float(out.value)
+
+
 class ExplicitGB300Op:
     """Resident explicit encoding operator on one GB300 (the ``:gb300`` backend).
 

@@ -307,6 +307,13 @@ HOE_API int  hoe_kdot_stencil(const double *traj_dev, int64_t nField, int32_t nT
 HOE_API int  hoe_interp_traj_time(const double *traj_dev, int64_t nField, int32_t nTerm, double dt,
                                   double delTime, const double *datatime_dev, int64_t nData,
                                   double *out_dev, int32_t layout, void *stream);
+/* Calibration (no handle): the sin/cos rate of the special-function unit of
+ * the current device in lane operations per clock per SM (sin and cos
+ * counted separately), measured by a kernel that keeps every SM's unit busy
+ * and reads clock64.  It allocates a few KB on `stream` and synchronises it.
+ * The phase generator's ceiling is 2 operations per (voxel, sample) pair at
+ * this rate. */
+HOE_API int  hoe_sfu_rate(double *lanes_per_clock_per_sm, void *stream);
 /* Replaces the operator's coefficients on the device: kspha_dev float64
  * [nTermEff x nSam] as desc.kspha (after prep_kspha / prep_concomitant),
  * kspha_dt_dev float64 [nTerm x nSam] or NULL (keeps the derivative table).

@@ -749,3 +749,13 @@ def test_tc_bounded_wait_runs_out_and_the_operator_recovers():
         y_first = yfull
     op.check()
     op.close()
+
+
+def test_sfu_rate_calibration():
+    """hoe_sfu_rate: the special-function unit's sin/cos rate is a positive
+    number of lane operations per clock per SM, at most one per lane of the
+    SM's four 32-wide sub-partitions, and stable between calls."""
+    from hoexplicit.operator import sfu_rate
+    a, b = sfu_rate(), sfu_rate()
+    assert 4.0 <= a <= 128.0, a
+    assert abs(a - b) <= 0.1 * a, (a, b)
