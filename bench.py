@@ -137,6 +137,25 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(ms: float, ws: int, device) -> float:
+    """The largest of the ranks' timed durations (ms): one all-reduce (MAX)
+    of the process group, then a barrier; the value itself at world size 1.
+    Every rank returns the same number."""
+    if ws <= 1:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def replica_value(units_per_step: float, ms_per_step: float, ws: int) -> float:
+    """Whole-job throughput of ws replicas that each process units_per_step
+    per step, timed by the slowest rank (weak scaling)."""
+    return ws * units_per_step / (ms_per_step / 1e3)
+
+
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
@@ -390,13 +409,10 @@ def run_batch(a):
     with Clocks(dev) as clk:
         ms = timed(lambda: (B.forward(xs), B.adjoint(ys)), a.steps, a.warmup)
     launches = (B.info()["launches"] - l0) / (a.steps + a.warmup)
-    if ws_ > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, ws_, dev)
     bf16_peak, _, peak_src = measured_peaks()
     flops = 8.0 * 16 * pairs  # contraction flops per direction
-    out = {"metric": METRIC, "value": ws_ * units / (ms / 1e3), "unit": UNIT, "n_gpus": ws_,
+    out = {"metric": METRIC, "value": replica_value(units, ms, ws_), "unit": UNIT, "n_gpus": ws_,
            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None,
            "dtype": "bf16x3/f32-acc" if engine == "tc" else "f32",
@@ -455,8 +471,8 @@ def run_batch(a):
         for _ in range(n_e2e):
             e2e()
         torch.cuda.synchronize()
-        e2e_s = (time.perf_counter() - t0) / n_e2e
-        out["e2e"] = {"value": ws_ * units / e2e_s, "unit": UNIT,
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e * 1e3, ws_, dev) / 1e3
+        out["e2e"] = {"value": replica_value(units, e2e_s * 1e3, ws_), "unit": UNIT,
                       "h2d_bytes_per_step": int(sum(x.numel() * 8 for x in xh) + sum(y.numel() * 8 for y in yh)),
                       "d2h_bytes_per_step": int(sum(x.numel() * 8 for x in xo) + sum(y.numel() * 8 for y in yo)),
                       "ms_per_step": e2e_s * 1e3}
@@ -629,14 +645,9 @@ def run_gb300(a):
     with Clocks(dev) as clk:
         r = time_engine(op, x, y, a.steps, a.warmup, flush, stream)
     torch.cuda.synchronize()
-    total_ms = sum(r["step_ms"])
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-        torch.distributed.barrier()
+    total_ms = max_over_ranks(sum(r["step_ms"]), ws, dev)
     ms_per_step = total_ms / a.steps
-    value = ws * units / (ms_per_step / 1e3)
+    value = replica_value(units, ms_per_step, ws)
 
     # dominant kernel roofline (contraction flops: 8*nCha per voxel·sample per direction)
     fk = statistics.mean(r["fwd_kernel_ms"])
@@ -780,16 +791,17 @@ def run_gb300(a):
                 step()
             torch.cuda.synchronize()
             res[name] = (time.perf_counter() - t0) / n_e2e
-        e2e_s = res["in_place"]
-        out["e2e"] = {"value": ws * units / e2e_s, "unit": UNIT,
+        e2e_s = max_over_ranks(res["in_place"] * 1e3, ws, dev) / 1e3
+        alloc_s = max_over_ranks(res["alloc"] * 1e3, ws, dev) / 1e3
+        out["e2e"] = {"value": replica_value(units, e2e_s * 1e3, ws), "unit": UNIT,
                       "h2d_bytes_per_step": int(xh.numel() * 8 + yh.numel() * 8),
                       "d2h_bytes_per_step": int(yo.numel() * 8 + xo.numel() * 8),
                       "ms_per_step": e2e_s * 1e3,
                       "api": "op.prod_(y, x) + op.ctprod_(x, y) on page-locked host tensors, one "
                              "stream synchronise per step",
                       "allocating_form": {"api": "y = op * x; x = op.H * y on page-locked host tensors",
-                                          "ms_per_step": res["alloc"] * 1e3,
-                                          "value": ws * units / res["alloc"]}}
+                                          "ms_per_step": alloc_s * 1e3,
+                                          "value": replica_value(units, alloc_s * 1e3, ws)}}
 
     check = out["recon"].pop("_check", None) if isinstance(out.get("recon"), dict) else None
     if rank == 0 and ws == 1 and not a.no_cpu_baseline:
