@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(BW_THREADS, 1) k_tc_backward(const __grid_cons
           tmem_ld16_async(pBase + j0, d);
           tmem_ld16_async(wBase + 2 * j0, w);
           tmem_ld16_async(wBase + 2 * j0 + 16, w + 16);
-          tmem_wait_ld();
+          tmem_wait_ld(d, w);
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             float sn, cs;

@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
             float Fv[8];
             tmem_ld8_async(ph, r);
             factor8(bt + q * 8, kreg, Fv);
-            tmem_wait_ld();
+            tmem_wait_ld(r);
             if (q == 4 * H - 1) {
               tc_fence_before();
               __syncwarp();

@@ -245,7 +245,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// 16 columns into registers without waiting: call tmem_wait_ld() before use.
+// 16 columns into registers without waiting: call tmem_wait_ld(r) before use.
 __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
@@ -253,8 +253,23 @@ __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *r) {
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-// 8 columns into registers without waiting: call tmem_wait_ld() before use.
+// Wait for this thread's tensor-memory loads, then pass each destination
+// register through an empty asm after the wait: the registers are outputs of
+// the load's asm, so without this the compiler could move arithmetic on them
+// (which is not a memory access) above the wait.  Costs no instruction.
+template <int K>
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[K]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < K; ++i) asm volatile("" : "+r"(r[i]));
+}
+template <int K1, int K2>
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&a)[K1], uint32_t (&b)[K2]) {
+  tmem_wait_ld(a);
+#pragma unroll
+  for (int i = 0; i < K2; ++i) asm volatile("" : "+r"(b[i]));
+}
+// 8 columns into registers without waiting: call tmem_wait_ld(r) before use.
 __device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t *r) {
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
