@@ -561,21 +561,19 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
         // once its last 16 columns are in registers
         constexpr int H = W::WIDE ? 2 : 1;
         if constexpr (DERIV) {
-          // 8 columns a step, the factor formed while the tensor-memory load
-          // is in flight; the same release and A-buffer wait points
+          // 8 columns a step; the next step's tensor-memory load is in flight
+          // while this step's factor, sin/cos and split run (the phase tile is
+          // released once its last columns are in registers)
+          uint32_t r[8];
+          tmem_ld8_async(pBase, r);
+          tmem_wait_ld(r);
 #pragma unroll 1
           for (int q = 0; q < 4 * H; ++q) {
-            const uint32_t ph = pBase + (uint32_t)(q * 8), ah = aBase + (uint32_t)(q * 8);
-            uint32_t r[8], hv[8], lv[8];
+            const uint32_t ah = aBase + (uint32_t)(q * 8);
+            uint32_t rn[8], hv[8], lv[8];
             float Fv[8];
-            tmem_ld8_async(ph, r);
+            if (q + 1 < 4 * H) tmem_ld8_async(pBase + (uint32_t)((q + 1) * 8), rn);
             factor8(bt + q * 8, kreg, Fv);
-            tmem_wait_ld(r);
-            if (q == 4 * H - 1) {
-              tc_fence_before();
-              __syncwarp();
-              if (lane == 0) mbar_arrive(&pfree[pbar]);
-            }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
               float sn, cs;
@@ -588,6 +586,16 @@ __global__ void __launch_bounds__(Warps<N, V>::THREADS, 1) k_tc_contract(const _
             }
             tmem_st8(ah, hv);
             tmem_st8(ah + TV, lv);
+            if (q + 1 < 4 * H) {
+              tmem_wait_ld(rn);
+              if (q + 2 == 4 * H) {
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&pfree[pbar]);
+              }
+#pragma unroll
+              for (int j = 0; j < 8; ++j) r[j] = rn[j];
+            }
           }
         } else {
         float d[16];
