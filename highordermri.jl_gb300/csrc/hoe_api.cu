@@ -1074,9 +1074,41 @@ int hoe_find_delay(hoe_handle *h, const hoe_delay_params *p, const void *data, c
   if (p->iter_max < 0 || p->max_outer < 1) return fail(h, HOE_ERR_ARG, "iter_max >= 0 and max_outer >= 1 required");
   DeviceGuard guard(h->device);
   memset(out, 0, sizeof(*out));
-  cudaError_t e = hoe::find_delay(h, *p, (const float2 *)data, (const float2 *)weights, traj, nField, (float2 *)x,
-                                  out, (cudaStream_t)stream);
+  cudaError_t e = hoe::find_delay(h, h, 1, nullptr, *p, (const float2 *)data, (const float2 *)weights, traj, nField,
+                                  (float2 *)x, out, (cudaStream_t)stream);
   return finish(h, e, "hoe_find_delay");
+}
+
+int hoe_find_delay_multishot(hoe_handle *h, hoe_handle *h_resid, const hoe_delay_params *p, int32_t nShot,
+                             const double *start_times, const void *data, const void *weights, const double *traj,
+                             int64_t nField, void *x, hoe_delay_result *out, void *stream) {
+  int rc = check_usable(h);
+  if (rc) return rc;
+  hoe_handle *hr = h_resid ? h_resid : h;
+  if (hr != h && (rc = check_usable(hr)) != 0) return rc;
+  if (!p || !out || !start_times) return fail(h, HOE_ERR_ARG, "params, start_times and out must not be NULL");
+  if (!data || !traj) return fail(h, HOE_ERR_ARG, "data and traj must be device pointers");
+  if (nShot < 1) return fail(h, HOE_ERR_ARG, "nShot must be positive");
+  if (h->t.nSam % nShot != 0) return fail(h, HOE_ERR_DIM, "the operator's samples must split evenly into nShot shots");
+  if (h->t.R0 != h->t.nTerm || hr->t.R0 != hr->t.nTerm)
+    return fail(h, HOE_ERR_ARG, "delay estimation needs operators without concomitant terms");
+  if (hr != h && (hr->device != h->device || hr->t.nSam != h->t.nSam || hr->t.nCha != h->t.nCha ||
+                  hr->t.nTerm != h->t.nTerm || hr->t.nFull != h->t.nFull || hr->t.nVox != h->t.nVox))
+    return fail(h, HOE_ERR_DIM, "h_resid must have the operator's device, samples, coils, terms and voxels");
+  if (nField < 2) return fail(h, HOE_ERR_ARG, "need at least two coefficient samples");
+  if (!(p->dt > 0.0) || !std::isfinite(p->dt)) return fail(h, HOE_ERR_ARG, "dt must be finite and positive");
+  if (!(p->dtau_min > 0.0) || !std::isfinite(p->dtau_min))
+    return fail(h, HOE_ERR_ARG, "dtau_min must be finite and positive");
+  if (!(p->jump_fact >= 1.0) || !std::isfinite(p->jump_fact)) return fail(h, HOE_ERR_ARG, "jump_fact must be >= 1");
+  if (!(p->lambda >= 0.0) || !std::isfinite(p->lambda)) return fail(h, HOE_ERR_ARG, "lambda must be finite and >= 0");
+  for (int s = 0; s < nShot; ++s)
+    if (!std::isfinite(start_times[s])) return fail(h, HOE_ERR_ARG, "start_times must be finite");
+  if (p->iter_max < 0 || p->max_outer < 1) return fail(h, HOE_ERR_ARG, "iter_max >= 0 and max_outer >= 1 required");
+  DeviceGuard guard(h->device);
+  memset(out, 0, sizeof(*out));
+  cudaError_t e = hoe::find_delay(h, hr, nShot, start_times, *p, (const float2 *)data, (const float2 *)weights, traj,
+                                  nField, (float2 *)x, out, (cudaStream_t)stream);
+  return finish(h, e, "hoe_find_delay_multishot");
 }
 
 }  // extern "C"

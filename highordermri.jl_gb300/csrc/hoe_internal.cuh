@@ -263,7 +263,8 @@ cudaError_t sfu_rate(double *lanesPerClkPerSm, cudaStream_t st);
 cudaError_t interp_akima(const double *traj, int64_t n, int nTerm, double dt, const double *delTimeDev,
                          double delTimeHost, const double *datatime, int64_t nData, double *out, int layout,
                          int ldo, const double *termMask, cudaStream_t st);
-cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *data, const float2 *weights,
+cudaError_t find_delay(hoe_handle *h, hoe_handle *hr, int nShot, const double *startTimes,
+                       const hoe_delay_params &q, const float2 *data, const float2 *weights,
                        const double *traj, int64_t nField, float2 *xOut, hoe_delay_result *res, cudaStream_t st);
 
 // Solver building blocks for larger captured sequences (hoe_cg.cu):

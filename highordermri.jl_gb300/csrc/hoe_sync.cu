@@ -143,7 +143,7 @@ __global__ void k_akima_eval(const double *__restrict__ traj, int64_t n, int nTe
   if (i >= nData * nTerm) return;
   const int64_t s = i % nData;
   const int l = (int)(i / nData);
-  const double del = delTimeDev ? *delTimeDev : delTimeHost;
+  const double del = (delTimeDev ? *delTimeDev : 0.0) + delTimeHost;   // device state plus a fixed offset
   const double *y = traj + (int64_t)l * n;
   const double t = datatime[s];
   const double x0 = -del, xl = (double)(n - 1) * dt - del;
@@ -270,15 +270,32 @@ cudaError_t interp_akima(const double *traj, int64_t n, int nTerm, double dt, co
 
 // FindDelay on the device.  The operator h (no concomitant terms, times =
 // the ADC times) is re-planned in place at every outer iteration.
-cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *data, const float2 *weights,
+//
+// nShot > 1 (FindDelay_multishot.jl:65-158): h holds all shots' samples
+// shot-major (sample j of shot s at s*nSPI + j, nSPI = nSam / nShot) and traj
+// one coefficient series per shot, [nField x nTerm] column-major, shots
+// consecutive.  Shot s is interpolated at delay tau + startTimes[s] (host
+// array) with its own k-dot stencil; q.start_time is not used.  The image
+// update uses h; the residual and derivative products use hr (h, or an
+// operator with the same model on other ADC times: the reference builds its
+// per-shot operators on the concatenated time vector, so every shot gets the
+// first shot's times).  nShot == 1 is FindDelay.jl:139-214 with q.start_time.
+cudaError_t find_delay(hoe_handle *h, hoe_handle *hr, int nShot, const double *startTimes,
+                       const hoe_delay_params &q, const float2 *data, const float2 *weights,
                        const double *traj, int64_t nField, float2 *xOut, hoe_delay_result *res, cudaStream_t st) {
   auto &t = h->t;
   const int nTerm = t.nTerm;
   const int64_t nD = (int64_t)t.nSam * t.nCha;
+  const bool multi = startTimes != nullptr;
+  const int nSPI = t.nSam / nShot;
+  const int64_t trajStride = nField * nTerm;
+  // delTime state: start + tau for one shot, tau (plus each shot's start
+  // time, passed per launch) for several
+  const double base = multi ? 0.0 : q.start_time;
   // scratch
   size_t bytes = 0;
   auto add = [&](size_t b) { size_t o = bytes; bytes += (b + 255) & ~(size_t)255; return o; };
-  const size_t oKd = add((size_t)nField * nTerm * sizeof(double));
+  const size_t oKd = add((size_t)nShot * nField * nTerm * sizeof(double));
   const size_t oKs = add((size_t)t.nSam * nTerm * sizeof(double));
   const size_t oKdt = add((size_t)t.nSam * nTerm * sizeof(double));
   const size_t oYf = add((size_t)nD * sizeof(float2));
@@ -300,7 +317,7 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
   S0.dtau = INFINITY;
   S0.dtauPrev = INFINITY;
   S0.J = q.jump_fact;
-  S0.delTime = q.start_time;
+  S0.delTime = base;
   S0.result = 0.0;
   S0.nIter = 1;
   std::vector<double> hm(kRmax, 1.0);
@@ -322,43 +339,54 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
   };
   e = cudaMemcpyAsync(S, &S0, sizeof(S0), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(mask, hm.data(), kRmax * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = kdot_stencil(traj, nField, nTerm, q.dt, kd, st);
+  for (int s = 0; s < nShot && e == cudaSuccess; ++s)
+    e = kdot_stencil(traj + s * trajStride, nField, nTerm, q.dt, kd + s * trajStride, st);
   if (e == cudaSuccess) e = cg_prepare(h);
   // the replan below supplies kspha_dt, so the tensor-core derivative runs
   // in the captured iteration: its buffers are allocated before the capture
-  if (e == cudaSuccess && h->engine == HOE_ENGINE_TC_BF16X3 && h->tc.ready) e = tc_derivative_prepare(h);
+  if (e == cudaSuccess && hr->engine == HOE_ENGINE_TC_BF16X3 && hr->tc.ready) e = tc_derivative_prepare(hr);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host staging above must be consumed
   if (e != cudaSuccess) { cleanup(); return e; }
 
   // one outer iteration, captured once and replayed
   auto enqueue = [&](cudaStream_t s) -> cudaError_t {
-    cudaError_t err = interp_akima(traj, nField, nTerm, q.dt, &S->delTime, 0.0, t.times64, t.nSam, ks, 1, nTerm,
-                                   nullptr, s);
-    if (err == cudaSuccess)
-      err = interp_akima(kd, nField, nTerm, q.dt, &S->delTime, 0.0, t.times64, t.nSam, kdt, 1, nTerm, nullptr, s);
-    h->launches += 2;
+    cudaError_t err = cudaSuccess;
+    for (int sh = 0; sh < nShot && err == cudaSuccess; ++sh) {
+      const double off = multi ? startTimes[sh] : 0.0;
+      const int64_t o = (int64_t)sh * nSPI;
+      err = interp_akima(traj + sh * trajStride, nField, nTerm, q.dt, &S->delTime, off, t.times64 + o, nSPI,
+                         ks + o * nTerm, 1, nTerm, nullptr, s);
+      if (err == cudaSuccess)
+        err = interp_akima(kd + sh * trajStride, nField, nTerm, q.dt, &S->delTime, off, t.times64 + o, nSPI,
+                           kdt + o * nTerm, 1, nTerm, nullptr, s);
+      h->launches += 2;
+    }
     if (err == cudaSuccess) err = replan_samples(h, ks, nTerm, kdt, nTerm, mask, s);
+    if (err == cudaSuccess && hr != h) err = replan_samples(hr, ks, nTerm, kdt, nTerm, mask, s);
     if (err == cudaSuccess) err = cg_enqueue(h, data, weights, x, r, s);
-    if (err == cudaSuccess) err = apply_forward(h, x, yf, s);
-    if (err == cudaSuccess) err = apply_derivative(h, x, yd, s);
+    if (err == cudaSuccess) err = apply_forward(hr, x, yf, s);
+    if (err == cudaSuccess) err = apply_derivative(hr, x, yd, s);
     if (err == cudaSuccess) {
       k_delay_dots<<<G, kThreads, 0, s>>>(data, yf, yd, nD, S, part);
-      k_delay_update<<<1, kThreads, 0, s>>>(part, G, S, q.start_time, q.dtau_min);
+      k_delay_update<<<1, kThreads, 0, s>>>(part, G, S, base, q.dtau_min);
       h->launches += 2;
       err = cudaGetLastError();
     }
     return err;
   };
   h->timing = 0;
+  const int savedTimingR = hr->timing;
+  hr->timing = 0;
   e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
   if (e == cudaSuccess) {
-    const int64_t l0 = h->launches;
+    const int64_t l0 = h->launches, lr0 = hr->launches;
     e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
     cudaError_t eq = e == cudaSuccess ? enqueue(cap) : e;
     cudaGraph_t g = nullptr;
     if (e == cudaSuccess) e = cudaStreamEndCapture(cap, &g);
-    const int64_t per = h->launches - l0;
+    const int64_t per = h->launches - l0 + (hr != h ? hr->launches - lr0 : 0);
     h->launches = l0;
+    if (hr != h) hr->launches = lr0;
     if (eq != cudaSuccess) e = eq;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
     if (g) cudaGraphDestroy(g);
@@ -383,6 +411,7 @@ cudaError_t find_delay(hoe_handle *h, const hoe_delay_params &q, const float2 *d
     }
   }
   cudaGetLastError();
+  hr->timing = savedTimingR;
   cleanup();
   return e;
 }

@@ -13,7 +13,7 @@ from .operator import (AdjointOp, ExplicitGB300Op, HighOrderExplicitOp, NormalOp
                        normalOperator)
 from .recon import CGNR, L2Regularization, recon_HOOp  # noqa: F401
 from .batch import OperatorBatch  # noqa: F401
-from .sync import FindDelay, InterpTrajTime, kspha_dt, set_kspha  # noqa: F401
+from .sync import FindDelay, FindDelay_multishot, InterpTrajTime, kspha_dt, set_kspha  # noqa: F401
 from .coils import (CoilCompressionTransform, apply_coil_compression, compress_coils,  # noqa: F401
                     estimate_noise_covariance, fit_coil_compression, noise_prewhitening_scale_factor)
 
@@ -22,7 +22,7 @@ __all__ = [
     "basisfunc_spha", "prep_kspha", "prep_concomitant", "HighOrderExplicitOp", "ExplicitGB300Op",
     "AdjointOp", "NormalOp", "WeightingOp", "WeightedOp", "compose", "normalOperator",
     "explicit_gpu_normal", "close", "load", "CGNR", "L2Regularization", "recon_HOOp",
-    "OperatorBatch", "FindDelay", "InterpTrajTime", "kspha_dt", "set_kspha",
+    "OperatorBatch", "FindDelay", "FindDelay_multishot", "InterpTrajTime", "kspha_dt", "set_kspha",
     "CoilCompressionTransform", "apply_coil_compression", "compress_coils", "estimate_noise_covariance",
     "fit_coil_compression", "noise_prewhitening_scale_factor",
 ]

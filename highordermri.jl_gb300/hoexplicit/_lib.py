@@ -39,7 +39,7 @@ EXPORTED = (
     "hoe_batch_create", "hoe_batch_free", "hoe_batch_last_error", "hoe_batch_get_info",
     "hoe_batch_forward", "hoe_batch_adjoint", "hoe_batch_normal", "hoe_batch_recon", "hoe_batch_check",
     "hoe_set_kspha", "hoe_kdot_stencil", "hoe_interp_traj_time", "hoe_find_delay", "hoe_autotune",
-    "hoe_coil_gram", "hoe_coil_fit", "hoe_coil_apply", "hoe_sfu_rate",
+    "hoe_coil_gram", "hoe_coil_fit", "hoe_coil_apply", "hoe_sfu_rate", "hoe_find_delay_multishot",
 )
 
 HOE_CG_ITERATION_LIMIT = 0
@@ -219,6 +219,8 @@ def load():
                                          ctypes.c_int32, vp]
     lib.hoe_find_delay.argtypes = [H, ctypes.POINTER(HoeDelayParams), vp, vp, vp, I64, vp,
                                    ctypes.POINTER(HoeDelayResult), vp]
+    lib.hoe_find_delay_multishot.argtypes = [H, H, ctypes.POINTER(HoeDelayParams), ctypes.c_int32, DP, vp, vp,
+                                             vp, I64, vp, ctypes.POINTER(HoeDelayResult), vp]
     for name in EXPORTED:
         if name not in ("hoe_free", "hoe_batch_free"):
             getattr(lib, name).restype = getattr(lib, name).restype or ctypes.c_int

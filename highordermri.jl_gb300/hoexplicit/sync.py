@@ -147,6 +147,84 @@ def FindDelay(gridding: Grid, data, kspha, datatime, StartTime: float, dt: float
     return (res.tau, info) if return_info else res.tau
 
 
+def FindDelay_multishot(gridding: Grid, data, kspha, datatime, StartTime, dt: float, *, JumpFact: float = 3,
+                        dtau_min: float = 5e-9, fieldmap=None, csm=None, recon_terms: str = "111",
+                        iter_max: int = 10, reg=None, weights=None, max_outer: int = 50, engine: str | None = None,
+                        return_info: bool = False):
+    """One synchronisation delay τ (seconds) shared by all shots of a 2-D image
+    (FindDelay_multishot.jl:65-158), on the device (hoe_find_delay_multishot).
+
+    data (nShot*nSPI, nCha) with the samples of a shot consecutive; kspha
+    (nShot, nField, nTerm); datatime (nShot, nSPI) ADC times, or None for
+    dt*(0:nField-1) in every shot (the overload without datatime,
+    FindDelay_multishot.jl:161-189); StartTime (nShot,).  As in the reference,
+    the per-shot residual and derivative products use the first shot's ADC
+    times (an operator on those times is built when the shots' times differ
+    and the fieldmap is not zero).  Density weights are the fixed ``weights``."""
+    from .operator import DEFAULT_ENGINE, HighOrderExplicitOp
+    from .recon import _device_vector
+    torch = _torch()
+    if gridding.nZ != 1:
+        raise ArgumentError("FindDelay_multishot needs a two-dimensional grid (nZ == 1)")
+    data = np.asarray(data) if not isinstance(data, torch.Tensor) else data
+    nSample, nCha = tuple(data.shape)
+    kspha = np.asarray(kspha, dtype=np.float64)
+    if kspha.ndim != 3:
+        raise DimensionMismatch("kspha must be (nShot, nFieldSample, nTerm)")
+    nShot, nField, nTerm = kspha.shape
+    if datatime is None:
+        datatime = np.tile(dt * np.arange(nField), (nShot, 1))
+    datatime = np.asarray(datatime, dtype=np.float64)
+    if datatime.ndim != 2 or datatime.shape[0] != nShot:
+        raise DimensionMismatch("kspha and datatime must have the same number of shots")
+    nSPI = datatime.shape[1]
+    if nShot * nSPI != nSample:
+        raise DimensionMismatch(f"data has {nSample} samples, expected nShot*nSPI = {nShot * nSPI}")
+    start = np.asarray(StartTime, dtype=np.float64).reshape(-1)
+    if start.size != nShot:
+        raise DimensionMismatch("StartTime must have one entry per shot")
+    mask = term_mask(recon_terms, nTerm)
+    if fieldmap is None:
+        fieldmap = np.zeros((gridding.nX, gridding.nY))
+    if csm is None:
+        csm = np.ones((gridding.nX, gridding.nY, 1), dtype=np.complex128)
+    if np.asarray(csm).shape[-1] != nCha:
+        raise DimensionMismatch("data and csm must have the same number of coil channels")
+    lam = 0.0 if reg is None else (reg.λ if isinstance(reg, L2Regularization) else float(reg))
+    k0 = np.concatenate([InterpTrajTime(kspha[s], dt, start[s], datatime[s]) for s in range(nShot)], axis=0).T
+    kw = dict(fieldmap=np.asarray(fieldmap).reshape(gridding.nX, gridding.nY, 1),
+              csm=np.asarray(csm).reshape(gridding.nX, gridding.nY, 1, nCha), recon_terms=recon_terms,
+              engine=engine or DEFAULT_ENGINE)
+    op = HighOrderExplicitOp(gridding, k0, datatime.reshape(-1), **kw)
+    opr = None
+    try:
+        if np.any(np.asarray(fieldmap) != 0) and np.any(datatime != datatime[0]):
+            opr = HighOrderExplicitOp(gridding, k0, np.tile(datatime[0], nShot), **kw)
+        d = _device_vector(op, data, nSample, nCha, "data")
+        w = None if weights is None else _device_vector(op, weights, nSample, 1, "weights")
+        traj = torch.from_numpy(np.concatenate([kspha[s].reshape(-1, order="F") for s in range(nShot)])).to(
+            op.torch_device)
+        x = torch.empty(op.ncol, dtype=torch.complex64, device=op.torch_device)
+        mask_c = (ctypes.c_double * nTerm)(*mask)
+        start_c = (ctypes.c_double * nShot)(*start)
+        p = _lib.HoeDelayParams(0.0, float(dt), float(dtau_min), float(JumpFact), float(lam),
+                                ctypes.cast(mask_c, ctypes.POINTER(ctypes.c_double)), int(iter_max), int(max_outer))
+        res = _lib.HoeDelayResult()
+        _lib.check(_lib.load().hoe_find_delay_multishot(
+            op._handle(), None if opr is None else opr._handle(), ctypes.byref(p), nShot,
+            ctypes.cast(start_c, ctypes.POINTER(ctypes.c_double)), d.data_ptr(),
+            None if w is None else w.data_ptr(), traj.data_ptr(), nField, x.data_ptr(), ctypes.byref(res),
+            op._stream()), op._h)
+        info = {"tau_last": res.tau_last, "dtau": res.dtau, "jump": res.jump, "iterations": res.iterations,
+                "status": STATUS.get(res.status, res.status), "resid_operator": opr is not None,
+                "image": x.cpu().numpy().reshape(gridding.matrixSize, order="F")}
+    finally:
+        op.close()
+        if opr is not None:
+            opr.close()
+    return (res.tau, info) if return_info else res.tau
+
+
 def set_kspha(op, kspha, kspha_dt=None) -> None:
     """Replace the operator's coefficients on the device (hoe_set_kspha):
     kspha (nTermEff, nSam) prepared as at construction, kspha_dt (nTerm, nSam)."""

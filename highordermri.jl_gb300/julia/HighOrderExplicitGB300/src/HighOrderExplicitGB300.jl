@@ -450,4 +450,41 @@ function find_delay(op::GB300ExplicitOp, data::CuMatrix{ComplexF32}, kspha::CuMa
     return res[].tau
 end
 
+"""
+    find_delay_multishot(op, data, kspha, StartTime, dt; op_resid=nothing, weights=nothing, JumpFact=3,
+                         Δτ_min, iter_max=10, λ=0, term_mask=nothing, max_outer=50)
+
+FindDelay_multishot (FindDelay_multishot.jl:65-158) for an operator built on
+all shots' samples, shot-major, with the concatenated ADC times and without
+concomitant terms.  `kspha::CuArray{Float64,3}` holds each shot's
+(nFieldSample, nTerm) series, shots last; `StartTime` one start per shot.
+`op_resid`: the operator for the per-shot residual and derivative products
+(`nothing` for `op`); the reference builds them on the concatenated time
+vector, i.e. on the first shot's times, which an operator on those times
+repeated reproduces.  Returns the delay τ.
+"""
+function find_delay_multishot(op::GB300ExplicitOp, data::CuMatrix{ComplexF32}, kspha::CuArray{Float64,3},
+                              StartTime::AbstractVector{<:Real}, dt::Real;
+                              op_resid::Union{Nothing,GB300ExplicitOp}=nothing,
+                              weights::Union{Nothing,CuVector{ComplexF32}}=nothing, JumpFact::Real=3,
+                              Δτ_min::Real, iter_max::Integer=10, λ::Real=0,
+                              term_mask::Union{Nothing,Vector{Float64}}=nothing, max_outer::Integer=50)
+    h = activate(op)
+    hr = op_resid === nothing ? C_NULL : activate(op_resid)
+    starts = Vector{Float64}(StartTime)
+    GC.@preserve term_mask starts begin
+        p = Ref(HoeDelayParams(0.0, Float64(dt), Float64(Δτ_min), Float64(JumpFact), Float64(λ),
+                               term_mask === nothing ? Ptr{Float64}(C_NULL) : pointer(term_mask),
+                               Int32(iter_max), Int32(max_outer)))
+        res = Ref(HoeDelayResult(0, 0, 0, 0, 0, 0))
+        check(ccall((:hoe_find_delay_multishot, libhoe), Cint,
+                    (Ptr{Cvoid}, Ptr{Cvoid}, Ref{HoeDelayParams}, Int32, Ptr{Float64}, CuPtr{ComplexF32},
+                     CuPtr{ComplexF32}, CuPtr{Float64}, Int64, CuPtr{ComplexF32}, Ref{HoeDelayResult}, CUDA.CUstream),
+                    h, hr, p, Int32(size(kspha, 3)), pointer(starts), data,
+                    weights === nothing ? CU_NULL : weights, kspha, size(kspha, 1), CU_NULL, res,
+                    stream_handle()), h)
+    end
+    return res[].tau
+end
+
 end # module

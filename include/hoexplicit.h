@@ -50,9 +50,12 @@
  *   hoe_interp_traj_time
  *                     InterpTrajTime, src/Synchronization/InterpTraj.jl:18-40 (Akima)
  *   hoe_find_delay    FindDelay, src/Synchronization/FindDelay.jl:139-214
+ *   hoe_find_delay_multishot
+ *                     FindDelay_multishot, src/Synchronization/FindDelay_multishot.jl:65-158
  *   hoe_coil_gram / hoe_coil_fit / hoe_coil_apply
  *                     estimate_noise_covariance, fit_coil_compression and
  *                     apply_coil_compression, src/Recon/CoilCompression.jl:127-301
+ *   hoe_sfu_rate      no reference counterpart (calibration of the roofline ceiling)
  *   hoe_autotune      no reference counterpart (the reference's backend and nBlock
  *                     are chosen by the caller, HighOrderExplicitOp.jl:48-50)
  *   hoe_close         Base.close(::ExplicitGPUOp), explicit_gpu_operator.jl:435-446
@@ -331,6 +334,26 @@ HOE_API int  hoe_set_kspha(hoe_handle *h, const double *kspha_dev, const double 
 HOE_API int  hoe_find_delay(hoe_handle *h, const hoe_delay_params *params, const void *data_dev,
                             const void *weights_dev, const double *traj_dev, int64_t nField,
                             void *x_dev, hoe_delay_result *out, void *stream);
+/* FindDelay_multishot (src/Synchronization/FindDelay_multishot.jl:65-158): one
+ * delay shared by nShot shots of a 2-D image, on the device like hoe_find_delay.
+ * h is built on all nShot*nSPI samples, shot-major (sample j of shot s at
+ * s*nSPI + j, the reference's reshape of (nSPI, nShot)), with the
+ * concatenated ADC times.  traj_dev: each shot's coefficient series, float64
+ * [nField x nTerm] column-major, shots consecutive (the reference's
+ * kspha[s, :, :]); start_times: HOST float64 [nShot], the per-shot StartTime
+ * (params->start_time is not used).  Shot s is interpolated at its own ADC
+ * times and delay start_times[s] + tau, with its own k-dot stencil.  The image
+ * update (weighted CGNR) uses h.  The residual y1 = data - E x and y2 = B x use
+ * h_resid, or h when NULL: the reference builds its per-shot operators on the
+ * concatenated time vector, so each shot gets the first shot's ADC times; to
+ * reproduce that when the shots' times differ and the fieldmap is not zero,
+ * pass an operator with the same model on the first shot's times repeated.
+ * Both operators are re-planned every iteration and keep the last
+ * coefficients. */
+HOE_API int  hoe_find_delay_multishot(hoe_handle *h, hoe_handle *h_resid, const hoe_delay_params *params,
+                                      int32_t nShot, const double *start_times, const void *data_dev,
+                                      const void *weights_dev, const double *traj_dev, int64_t nField,
+                                      void *x_dev, hoe_delay_result *out, void *stream);
 
 /* SVD coil compression (src/Recon/CoilCompression.jl:150-353).  Matrices are
  * column-major: A [nObs x nCoil] observations by coils on the device

@@ -18,6 +18,12 @@ preprocessing (src/Synchronization/FindDelay.jl, InterpTraj.jl).
   change, until |Δτ| ≤ Δτ_min; return τ − Δτ/J·(J−1).  The density weights
   are a fixed input here (the reference recomputes them with NFFT's density
   compensation at every τ).
+* ``find_delay_multishot`` — FindDelay_multishot.jl:65-158: one delay for
+  several shots.  Each shot's series and its own k̇ are interpolated at its ADC
+  times and delay StartTime[s] + τ; the image update uses all shots with the
+  concatenated times; the per-shot residual and derivative products are built
+  on the concatenated time vector, so every shot gets the first shot's ADC
+  times (FindDelay_multishot.jl:111-116), as restated here.
 """
 from __future__ import annotations
 
@@ -117,6 +123,47 @@ def find_delay(bf, fieldmap, csm, data, traj, datatime, start_time, dt, *, weigh
         x, _ = _r.recon(m, data, weights, iter_max, 0.0, lam, nBlock)
         y1 = data - _o.forward(m, x, nBlock)
         y2 = _o.derivative(m, kd_tau, x)
+        dtau = J * float(np.real(np.vdot(y2, y1) / np.vdot(y2, y2)))
+        tau += dtau
+        if n_iter > 1 and np.sign(dtau_prev) != np.sign(dtau):
+            J = max(1.0, J / 2)
+        dtau_prev = dtau
+        n_iter += 1
+        hist.append(tau)
+    return tau - dtau / J * (J - 1), {"history": hist, "iterations": n_iter - 1, "jump": J}
+
+
+def find_delay_multishot(bf, fieldmap, csm, data, traj, datatime, start_times, dt, *, weights=None, jump_fact=3,
+                         dtau_min=5e-9, iter_max=10, lam=0.0, term_mask=None, max_outer=50, nBlock=50):
+    """Delay estimate τ (seconds) shared by all shots, and its history.
+
+    traj (nShot, nField, nTerm), datatime (nShot, nSPI) ADC times per shot,
+    start_times (nShot,), data (nShot*nSPI*nCha,) samples fastest with the
+    samples of a shot consecutive (sample j of shot s at s*nSPI + j).
+    """
+    traj = np.asarray(traj, dtype=np.float64)
+    datatime = np.asarray(datatime, dtype=np.float64)
+    start_times = np.asarray(start_times, dtype=np.float64).reshape(-1)
+    nShot, _, nTerm = traj.shape
+    mask = np.ones(nTerm) if term_mask is None else np.asarray(term_mask, dtype=np.float64)
+    kd_full = np.stack([kdot_stencil(traj[s], dt) for s in range(nShot)])
+    times = datatime.reshape(-1)
+    times_res = np.tile(datatime[0], nShot)   # the per-shot operators' times
+
+    def series(src, tau):
+        return np.concatenate([interp_traj_time(src[s], dt, tau + start_times[s], datatime[s])
+                               for s in range(nShot)], axis=0).T * mask[:, None]
+
+    tau, J, n_iter = 0.0, float(jump_fact), 1
+    dtau_prev = dtau = np.inf
+    hist = [tau]
+    while abs(dtau) > dtau_min and n_iter <= max_outer:
+        k_tau, kd_tau = series(traj, tau), series(kd_full, tau)
+        m = _o.Model(bf, k_tau, times, fieldmap, csm, nTerm=nTerm)
+        x, _ = _r.recon(m, data, weights, iter_max, 0.0, lam, nBlock)
+        mr = _o.Model(bf, k_tau, times_res, fieldmap, csm, nTerm=nTerm)
+        y1 = data - _o.forward(mr, x, nBlock)
+        y2 = _o.derivative(mr, kd_tau, x)
         dtau = J * float(np.real(np.vdot(y2, y1) / np.vdot(y2, y2)))
         tau += dtau
         if n_iter > 1 and np.sign(dtau_prev) != np.sign(dtau):

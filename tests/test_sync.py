@@ -71,6 +71,51 @@ def test_oracle_find_delay_recovers_a_known_delay():
     assert info["iterations"] < 50
 
 
+def multishot_problem(n=24, nSPI=750, nShot=2, nCha=2, tau_true=3.7e-6, dt=2e-6, seed=5, margin=8, shift=0.0):
+    """A spiral slice read in nShot consecutive shots, each with its own
+    coefficient series (with margins), start time and ADC times (shot s at
+    dt*(0:nSPI-1) + s*shift); the data were acquired at delay tau_true."""
+    from hoexplicit import workloads
+    from hoexplicit.model import basisfunc_spha
+    w = workloads.spiral_slice(seed, n, nSPI * nShot, nCha, d=200e-3 / n, dwell=dt)
+    k9 = w.kspha[:9]
+    traj = np.stack([np.concatenate([k9[:, s * nSPI:s * nSPI + 1].repeat(margin, 1), k9[:, s * nSPI:(s + 1) * nSPI],
+                                     k9[:, (s + 1) * nSPI - 1:(s + 1) * nSPI].repeat(margin, 1)], axis=1).T
+                     for s in range(nShot)])
+    start = margin * dt + 0.25 * dt * np.arange(nShot)
+    datatime = np.stack([np.arange(nSPI) * dt + s * shift for s in range(nShot)])
+    g = w.grid
+    bf = basisfunc_spha(g.x, g.y, g.z, list(range(1, 10)))
+    fm = np.asarray(w.fieldmap).reshape(-1, order="F")
+    csm = np.asarray(w.csm).reshape(n * n, nCha, order="F")
+    k_true = np.concatenate([osync.interp_traj_time(traj[s], dt, start[s] + tau_true, datatime[s])
+                             for s in range(nShot)], axis=0).T
+    m = oracle.Model(bf, k_true, datatime.reshape(-1), fm, csm, nTerm=9)
+    y = oracle.forward(m, w.x)
+    rng = np.random.default_rng(2)
+    y = y + 0.001 * np.linalg.norm(y) / np.sqrt(y.size) * (rng.standard_normal(y.size) + 1j * rng.standard_normal(y.size))
+    return dict(w=w, traj=traj, start=start, datatime=datatime, bf=bf, fm=fm, csm=csm, y=y, dt=dt, tau=tau_true)
+
+
+def test_oracle_find_delay_multishot_recovers_a_known_delay():
+    P = multishot_problem()
+    # the shots' increments shrink by ~6% an iteration, so this estimator
+    # needs a larger Δτ_min and more iterations than the single-shot problem
+    tau, info = osync.find_delay_multishot(P["bf"], P["fm"], P["csm"], P["y"], P["traj"], P["datatime"], P["start"],
+                                           P["dt"], dtau_min=1e-8, iter_max=10, max_outer=100)
+    assert abs(tau - P["tau"]) < 0.1 * P["tau"], tau
+    assert info["iterations"] < 100
+
+
+def test_oracle_find_delay_multishot_with_one_shot_is_find_delay():
+    P = delay_problem()
+    a = osync.find_delay(P["bf"], P["fm"], P["csm"], P["y"], P["traj"], P["datatime"], P["start"], P["dt"],
+                         dtau_min=5e-9, iter_max=10)
+    b = osync.find_delay_multishot(P["bf"], P["fm"], P["csm"], P["y"], P["traj"][None], P["datatime"][None],
+                                   [P["start"]], P["dt"], dtau_min=5e-9, iter_max=10)
+    assert a[0] == b[0] and a[1]["history"] == b[1]["history"]
+
+
 # --------------------------------------------------------------------- GPU
 torch = pytest.importorskip("torch")
 
@@ -145,3 +190,72 @@ def test_find_delay_matches_oracle(engine):
     assert abs(tau - to) < (0.02 if engine == "fp32" else 0.05) * P["tau"], (tau, to)
     assert abs(tau - P["tau"]) < 0.1 * P["tau"]
     assert info["image"].shape == (n, n, 1)
+
+
+def _multishot_device(P, engine, **kw):
+    n, nCha = P["w"].grid.nX, P["csm"].shape[1]
+    data = P["y"].reshape(nCha, -1).T
+    return hsync.FindDelay_multishot(P["w"].grid, data.astype(np.complex64), P["traj"], P["datatime"], P["start"],
+                                     P["dt"], dtau_min=1e-8, fieldmap=P["fm"].reshape(n, n, order="F"),
+                                     csm=P["csm"].reshape(n, n, nCha, order="F"), recon_terms="111", iter_max=10,
+                                     max_outer=100, engine=engine, return_info=True, **kw)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_find_delay_multishot_matches_oracle(engine):
+    maybe_skip(engine)
+    P = multishot_problem()
+    tau, info = _multishot_device(P, engine)
+    to, _ = osync.find_delay_multishot(P["bf"], P["fm"], P["csm"], P["y"], P["traj"], P["datatime"], P["start"],
+                                       P["dt"], dtau_min=1e-8, iter_max=10, max_outer=100)
+    assert info["status"] == "converged" and not info["resid_operator"]
+    assert abs(tau - to) < (0.02 if engine == "fp32" else 0.05) * P["tau"], (tau, to)
+    assert abs(tau - P["tau"]) < 0.1 * P["tau"]
+    assert info["image"].shape == (P["w"].grid.nX, P["w"].grid.nY, 1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("engine", ENGINE_PARAMS)
+def test_find_delay_multishot_residuals_on_the_first_shots_times(engine):
+    """Shot 2 acquired 6 us later than shot 1 with a fieldmap: the image update
+    uses each shot's times, the residual and derivative products the first
+    shot's (an operator on those times), as in the reference."""
+    maybe_skip(engine)
+    P = multishot_problem(shift=6e-6)
+    tau, info = _multishot_device(P, engine)
+    to, _ = osync.find_delay_multishot(P["bf"], P["fm"], P["csm"], P["y"], P["traj"], P["datatime"], P["start"],
+                                       P["dt"], dtau_min=1e-8, iter_max=10, max_outer=100)
+    assert info["resid_operator"] and info["status"] == "converged"
+    assert abs(tau - to) < (0.02 if engine == "fp32" else 0.05) * P["tau"], (tau, to)
+
+
+@pytest.mark.gpu
+def test_find_delay_multishot_with_one_shot_is_find_delay():
+    P = delay_problem()
+    n, nCha = P["w"].grid.nX, P["csm"].shape[1]
+    data = (P["y"].reshape(nCha, -1).T).astype(np.complex64)
+    kw = dict(dtau_min=5e-9, fieldmap=P["fm"].reshape(n, n, order="F"), csm=P["csm"].reshape(n, n, nCha, order="F"),
+              recon_terms="111", iter_max=10, engine="fp32", return_info=True)
+    a, ia = hsync.FindDelay(P["w"].grid, data, P["traj"], P["datatime"], P["start"], P["dt"], **kw)
+    b, ib = hsync.FindDelay_multishot(P["w"].grid, data, P["traj"][None], P["datatime"][None], [P["start"]], P["dt"],
+                                      **kw)
+    assert a == b and ia["iterations"] == ib["iterations"]
+    np.testing.assert_array_equal(ia["image"], ib["image"])
+
+
+def test_find_delay_multishot_argument_checks():
+    from hoexplicit import ArgumentError, DimensionMismatch
+    P = multishot_problem(nSPI=100)
+    n, nCha = P["w"].grid.nX, P["csm"].shape[1]
+    data = np.zeros((200, nCha), np.complex64)
+    with pytest.raises(DimensionMismatch):
+        hsync.FindDelay_multishot(P["w"].grid, data, P["traj"], P["datatime"][:1], P["start"], P["dt"])
+    with pytest.raises(DimensionMismatch):
+        hsync.FindDelay_multishot(P["w"].grid, data[:150], P["traj"], P["datatime"], P["start"], P["dt"])
+    with pytest.raises(DimensionMismatch):
+        hsync.FindDelay_multishot(P["w"].grid, data, P["traj"], P["datatime"], P["start"][:1], P["dt"])
+    with pytest.raises(DimensionMismatch):
+        hsync.FindDelay_multishot(P["w"].grid, data, P["traj"][0], P["datatime"], P["start"], P["dt"])
+    with pytest.raises(ArgumentError):
+        hsync.FindDelay_multishot(P["w"].grid, data, P["traj"], P["datatime"], P["start"], P["dt"], recon_terms="11")
