@@ -67,9 +67,24 @@ def kspha_dt(kspha, dt: float):
     return _out(out, n, nT, kind)
 
 
-def InterpTrajTime(traj, dt: float, delTime: float, datatime=None):
+def InterpTrajTime(traj, dt: float, delTime, datatime=None):
     """(nFieldSample, nTerm) -> (len(datatime), nTerm); datatime defaults to
-    dt*(0:nFieldSample-1) (InterpTraj.jl:48-70)."""
+    dt*(0:nFieldSample-1) (InterpTraj.jl:18-66).  A (nShot, nFieldSample,
+    nTerm) series with one delTime per shot and datatime (nShot, nADCSample)
+    gives (nShot, nADCSample, nTerm), each shot interpolated on its own
+    (InterpTraj.jl:79-99)."""
+    if getattr(traj, "ndim", 2) == 3:
+        if datatime is None:
+            raise ArgumentError("the per-shot overload needs datatime (nShot, nADCSample)")
+        delTime = np.asarray(delTime, dtype=np.float64).reshape(-1)
+        nShot = traj.shape[0]
+        if nShot != delTime.size:
+            raise DimensionMismatch("Number of shots in trajectory must match length of delTime vector")
+        if getattr(datatime, "ndim", 0) != 2 or datatime.shape[0] != delTime.size:
+            raise DimensionMismatch("Number of shots in datatime must match length of delTime vector")
+        shots = [InterpTrajTime(traj[i], dt, float(delTime[i]), datatime[i]) for i in range(nShot)]
+        torch = _torch()
+        return torch.stack(shots) if isinstance(shots[0], torch.Tensor) else np.stack(shots)
     torch = _torch()
     buf, (n, nT), kind = _colmajor(traj, "traj")
     if datatime is None:

@@ -415,6 +415,19 @@ function HighOrderMRI.InterpTrajTime(traj::CuMatrix{Float64}, dt::Real, delTime:
     return out
 end
 
+# the per-shot overload (InterpTraj.jl:79-99): (nShot, nField, nTerm) series,
+# one delay per shot, datatime (nShot, nADC) -> (nShot, nADC, nTerm)
+function HighOrderMRI.InterpTrajTime(traj::CuArray{Float64,3}, dt::Real, delTime::AbstractVector{Float64},
+                                     datatime::CuMatrix{Float64}; kwargs...)
+    @assert size(traj, 1) == length(delTime) "Number of shots in trajectory must match length of delTime vector"
+    @assert size(datatime, 1) == length(delTime) "Number of shots in datatime must match length of delTime vector"
+    out = CuArray{Float64}(undef, size(traj, 1), size(datatime, 2), size(traj, 3))
+    for i in axes(traj, 1)
+        out[i, :, :] = HighOrderMRI.InterpTrajTime(traj[i, :, :], dt, delTime[i], datatime[i, :])
+    end
+    return out
+end
+
 struct HoeDelayParams
     start_time::Float64; dt::Float64; dtau_min::Float64; jump_fact::Float64; lambda::Float64
     term_mask::Ptr{Float64}; iter_max::Int32; max_outer::Int32

@@ -259,3 +259,30 @@ def test_find_delay_multishot_argument_checks():
         hsync.FindDelay_multishot(P["w"].grid, data, P["traj"][0], P["datatime"], P["start"], P["dt"])
     with pytest.raises(ArgumentError):
         hsync.FindDelay_multishot(P["w"].grid, data, P["traj"], P["datatime"], P["start"], P["dt"], recon_terms="11")
+
+
+@pytest.mark.gpu
+def test_interp_traj_time_per_shot_overload():
+    """InterpTrajTime of a (nShot, nField, nTerm) series: each shot with its own
+    delay and ADC times (InterpTraj.jl:79-99), against the oracle per shot."""
+    rng = np.random.default_rng(4)
+    traj = np.cumsum(rng.standard_normal((3, 60, 4)), axis=1)
+    dt = 2e-6
+    delTime = np.array([3e-6, 7.5e-6, -1e-6])
+    datatime = np.stack([np.arange(50) * dt + s * 0.3e-6 for s in range(3)])
+    out = hsync.InterpTrajTime(traj, dt, delTime, datatime)
+    assert out.shape == (3, 50, 4)
+    for s in range(3):
+        ref = osync.interp_traj_time(traj[s], dt, delTime[s], datatime[s])
+        assert np.max(np.abs(out[s] - ref)) <= 1e-12 * np.max(np.abs(ref))
+
+
+def test_interp_traj_time_per_shot_argument_checks():
+    from hoexplicit import ArgumentError, DimensionMismatch
+    traj = np.zeros((2, 10, 3))
+    with pytest.raises(DimensionMismatch):
+        hsync.InterpTrajTime(traj, 1e-6, np.zeros(3), np.zeros((2, 5)))
+    with pytest.raises(DimensionMismatch):
+        hsync.InterpTrajTime(traj, 1e-6, np.zeros(2), np.zeros((3, 5)))
+    with pytest.raises(ArgumentError):
+        hsync.InterpTrajTime(traj, 1e-6, np.zeros(2))
