@@ -547,11 +547,55 @@ def explicit_gpu_normal(op, weights=None):
     return normalOperator(op, np.abs(np.asarray(weights)) ** 2)
 
 
+_KERNEL_OPTIONS = dict(backend="legacy", block_size=320, phase_backend="kernel", gemm_backend="cublas",
+                       phase_cache_bytes=0, forward_threads=256, adjoint_threads=512)
+
+
+def check_kernel_options(kspha_dt=None, **opts) -> None:
+    """The reference's validation of its CUDA implementation's execution
+    keywords (kernel_operator.jl:223-236, explicit_gpu_operator.jl:313-320),
+    with the same ArgumentError messages.  They choose among that
+    implementation's execution strategies (direct kernels, blocked phase
+    tiles with a kernel- or GEMM-generated phase, a cached phase matrix),
+    which the GB300 engine replaces: they are checked for drop-in use and do
+    not change the arithmetic."""
+    o = dict(_KERNEL_OPTIONS, **opts)
+    sym = lambda v: str(v).lstrip(":")  # noqa: E731
+    backend = sym(o["backend"])
+    if backend != "legacy":
+        if backend not in ("direct", "blocked", "cached", "cached_full"):
+            raise ArgumentError(f"unknown explicit backend {backend}")
+        if kspha_dt is not None:
+            raise ArgumentError("kspha_dt requires backend=:legacy")
+        if int(o["phase_cache_bytes"]) < 0:
+            raise ArgumentError("phase_cache_bytes must be nonnegative")
+        if int(o["phase_cache_bytes"]) != 0 and backend != "blocked":
+            raise ArgumentError("phase_cache_bytes applies to backend=:blocked; cached backends already retain "
+                                "the complete phase matrix")
+        if sym(o["phase_backend"]) not in ("kernel", "gemm"):
+            raise ArgumentError(f"unknown phase backend {sym(o['phase_backend'])}")
+        if sym(o["gemm_backend"]) not in ("cublas", "auto"):
+            raise ArgumentError("gemm_backend must be :cublas or :auto")
+        if int(o["block_size"]) <= 0:
+            raise ArgumentError("block_size must be positive")
+        if int(o["forward_threads"]) not in (64, 128, 256, 512):
+            raise ArgumentError("unsupported forward_threads")
+        if int(o["adjoint_threads"]) not in (64, 128, 256, 512):
+            raise ArgumentError("unsupported adjoint_threads")
+    elif int(o["phase_cache_bytes"]) != 0:
+        raise ArgumentError("phase_cache_bytes requires backend=:blocked")
+
+
 def HighOrderExplicitOp(grid: Grid, kspha, times, *, implementation: str = "gb300", **kwargs):
     """Construct the explicit encoding operator (HighOrderExplicitOp.jl:44-51).
 
     This package provides the ``:gb300`` implementation only; the reference's
-    ``:array`` and ``:kernel`` implementations are not part of it.
+    ``:array`` and ``:kernel`` implementations are not part of it.  Their
+    execution keywords are accepted so that a call written for either works
+    unchanged: ``arrayType``, ``nBlock`` and ``verbose`` (the Array path) are
+    ignored; ``backend``, ``block_size``, ``phase_backend``, ``gemm_backend``,
+    ``phase_cache_bytes``, ``forward_threads`` and ``adjoint_threads`` (the
+    CUDA path) get the reference's validation (check_kernel_options).
     """
     impl = str(implementation).lstrip(":")
     if impl != "gb300":
@@ -559,6 +603,8 @@ def HighOrderExplicitOp(grid: Grid, kspha, times, *, implementation: str = "gb30
     kwargs.pop("arrayType", None)
     kwargs.pop("nBlock", None)
     kwargs.pop("verbose", None)
+    opts = {k: kwargs.pop(k) for k in list(kwargs) if k in _KERNEL_OPTIONS}
+    check_kernel_options(kspha_dt=kwargs.get("kspha_dt"), **opts)
     return ExplicitGB300Op(grid, kspha, times, **kwargs)
 
 

@@ -135,7 +135,28 @@ function GB300ExplicitOp(grid::Grid{T}, kspha::AbstractMatrix{T}, times::Abstrac
     fieldmap=zeros(T, grid.matrixSize...), csm=ones(Complex{T}, grid.matrixSize..., 1),
     mask=trues(grid.matrixSize...), concomitant=nothing, recon_terms=nothing,
     k_nominal=kspha[2:4, :], kspha_dt=nothing, kdot=nothing, gpus=nothing, engine::Symbol=:auto,
+    # the reference implementations' execution keywords, for calls written for
+    # them: the Array path's are ignored, the CUDA path's get its validation
+    # (kernel_operator.jl:223-236, explicit_gpu_operator.jl:313-320) and
+    # change nothing (the GB300 engine replaces those execution strategies)
+    nBlock::Integer=50, arrayType=CuArray, verbose::Bool=false,
+    backend::Symbol=:legacy, block_size::Int=320, phase_backend::Symbol=:kernel, gemm_backend::Symbol=:cublas,
+    phase_cache_bytes::Integer=0, forward_threads::Int=256, adjoint_threads::Int=512,
 ) where {T<:AbstractFloat}
+    if backend !== :legacy
+        backend in (:direct, :blocked, :cached, :cached_full) || throw(ArgumentError("unknown explicit backend $backend"))
+        isnothing(kspha_dt) || throw(ArgumentError("kspha_dt requires backend=:legacy"))
+        phase_cache_bytes >= 0 || throw(ArgumentError("phase_cache_bytes must be nonnegative"))
+        phase_cache_bytes == 0 || backend === :blocked || throw(ArgumentError(
+            "phase_cache_bytes applies to backend=:blocked; cached backends already retain the complete phase matrix"))
+        phase_backend in (:kernel, :gemm) || throw(ArgumentError("unknown phase backend $phase_backend"))
+        gemm_backend in (:cublas, :auto) || throw(ArgumentError("gemm_backend must be :cublas or :auto"))
+        block_size > 0 || throw(ArgumentError("block_size must be positive"))
+        forward_threads in (64, 128, 256, 512) || throw(ArgumentError("unsupported forward_threads"))
+        adjoint_threads in (64, 128, 256, 512) || throw(ArgumentError("unsupported adjoint_threads"))
+    else
+        iszero(phase_cache_bytes) || throw(ArgumentError("phase_cache_bytes requires backend=:blocked"))
+    end
     if gpus !== nothing
         ids = Int.(collect(gpus))
         length(ids) == 1 || throw(ArgumentError("the :gb300 operator uses exactly one GPU"))

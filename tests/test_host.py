@@ -145,3 +145,29 @@ def test_host_plan_needs_no_device():
     assert plan(w.grid, w.kspha, w.times, engine="fp32", **w.op_kwargs())["engine"] == _lib.HOE_ENGINE_FP32_SIMT
     with pytest.raises(ArgumentError):
         plan(w.grid, w.kspha, w.times, engine="fp16", **w.op_kwargs())
+
+
+def test_kernel_execution_keywords_get_the_reference_validation():
+    """The CUDA implementation's execution keywords (kernel_operator.jl:223-236,
+    explicit_gpu_operator.jl:313-320) are accepted by the :gb300 front with
+    the reference's ArgumentErrors; valid ones reach the operator unchanged."""
+    from hoexplicit import ArgumentError
+    from hoexplicit.operator import check_kernel_options
+    check_kernel_options()                                   # :legacy defaults
+    check_kernel_options(backend=":blocked", phase_backend=":gemm", block_size=4, phase_cache_bytes=96)
+    check_kernel_options(backend="cached_full", gemm_backend="auto", forward_threads=64, adjoint_threads=128)
+    bad = [dict(backend=":blocked", phase_cache_bytes=-1),
+           dict(backend=":direct", phase_cache_bytes=1),
+           dict(backend=":cached", phase_cache_bytes=1),
+           dict(phase_cache_bytes=1),                        # :legacy
+           dict(backend=":fancy"),
+           dict(backend=":blocked", phase_backend=":fft"),
+           dict(backend=":blocked", gemm_backend=":cutlass"),
+           dict(backend=":blocked", block_size=0),
+           dict(backend=":blocked", forward_threads=96),
+           dict(backend=":blocked", adjoint_threads=1024)]
+    for kw in bad:
+        with pytest.raises(ArgumentError):
+            check_kernel_options(**kw)
+    with pytest.raises(ArgumentError, match="kspha_dt requires backend=:legacy"):
+        check_kernel_options(kspha_dt=np.zeros((9, 3)), backend=":blocked")
