@@ -325,3 +325,32 @@ def test_config2_recon_vs_fp64_cgnr(engine, cfg2_recon):
     assert abs(dense.rel(xg[idx], xt) - dense.rel(xo, xt)) < 0.01 * dense.rel(xo, xt)
     op.check()
     op.close()
+
+
+def test_tc_volume_beyond_2_31_pairs():
+    """The largest case: a 256x256x64 volume (4.2M voxels) read by 16 kz
+    partitions x 1,250 samples with 8 coils, 8.4e10 voxel-sample pairs per
+    direction (beyond 2^31) and about 17 GB of anchor tables and operands on
+    the device.  FP64 oracle on 12 sampled samples of E x (all coils) and on
+    12 sampled voxels of E^H y, adjoint identity, bitwise repeatability."""
+    maybe_skip("tc")
+    w = workloads.volume3d(shape=(256, 256, 64), d=1e-3, parts=16, per=1250, nCha=8, frac=0.5)
+    assert w.nVox * w.nSam > 2 ** 31
+    op = HighOrderExplicitOp(w.grid, w.kspha, w.times, engine="tc", **w.op_kwargs())
+    rng = np.random.default_rng(21)
+    x = dev(w.x)
+    ynp = host(op * x)
+    bf, k, t, f, c, idx = workloads.prepared_model(w)
+    rows = np.sort(rng.choice(w.nSam, 12, replace=False))
+    yo = oracle.forward(oracle.Model(bf, k[:, rows], t[rows], f, c, nTerm=16), w.x[idx])
+    assert dense.rel(ynp.reshape(w.nCha, w.nSam)[:, rows].reshape(-1), yo) < TOL["tc"]
+    y = ynp + _noise(rng, ynp.size, 0.05 * np.linalg.norm(ynp) / np.sqrt(ynp.size))
+    xa = host(op.H * dev(y))
+    vox = np.sort(rng.choice(w.nVox, 12, replace=False))
+    xo = _voxel_adjoint_fp64(bf, k, t, f, c, y, vox, w.nVox)
+    assert dense.rel(xa[idx[vox]], xo) < TOL["tc"]
+    lhs, rhs = np.vdot(y, ynp), np.vdot(xa, host(x))
+    assert abs(lhs - rhs) / (np.linalg.norm(ynp) * np.linalg.norm(y)) < 1e-5
+    assert np.array_equal(host(op * x), ynp)
+    op.check()
+    op.close()
