@@ -265,7 +265,7 @@ class ExplicitGB300Op:
         self.engine = _ENGINE_NAMES[self.info()["engine"]]
         self.nprod = self.ntprod = self.nctprod = 0
         self.tprod = None
-        self._stage = {}   # device buffers for host operands of prod_/ctprod_, per (stream, role)
+        self._stage = {}   # device buffers for host operands of prod_/ctprod_, per (stream, role, length)
 
     # ------------------------------------------------------------------ misc
     def _handle(self):
@@ -327,38 +327,43 @@ class ExplicitGB300Op:
         return self._h is None or bool(_lib.load().hoe_is_closed(self._h))
 
     # ------------------------------------------------------------ products
-    def _io(self, t, n, name, role):
+    def _io(self, t, n, name, role, torch, stream):
         """Device view of an in-place product operand.  A CUDA tensor is used
         as is; a host tensor goes through a device buffer that the operator
-        keeps per (stream, role), reused in stream order.  Returns (device
-        tensor, host tensor to copy the result into or None, pinned)."""
-        torch = _torch()
+        keeps per (stream, role, length), reused in stream order.  Returns
+        (device tensor, host tensor to copy the result into or None, pinned)."""
         if not isinstance(t, torch.Tensor) or t.dtype != torch.complex64 or not t.is_contiguous():
             raise ArgumentError(f"{name} must be a contiguous complex64 torch tensor")
         if t.numel() != n:
             raise DimensionMismatch(f"{name} has length {t.numel()}, expected {n}")
-        if t.device.type == "cuda":
-            if t.device.index != self.device:
-                raise ArgumentError(f"{name} is on cuda:{t.device.index}, operator on cuda:{self.device}")
+        if t.is_cuda:
+            if t.get_device() != self.device:
+                raise ArgumentError(f"{name} is on cuda:{t.get_device()}, operator on cuda:{self.device}")
             return t, None, False
-        key = (self._stream(), role)
+        key = (stream, role, n)
         buf = self._stage.get(key)
-        if buf is None or buf.numel() != n:
+        if buf is None:
             buf = torch.empty(n, dtype=torch.complex64, device=self.torch_device)
             self._stage[key] = buf
-        return buf, t, bool(t.is_pinned())
+        return buf, t, t.is_pinned()
 
     def _product(self, fn, out, v, nout, nin, counter):
         """Queue out = op(v) on the current stream.  Host operands are copied
         in and out around the kernels; with page-locked host memory nothing
         waits, so `out` holds the result once the stream has been synchronised
         (as with torch's non_blocking copies).  Other host memory is copied
-        synchronously."""
-        dv, hv, pv = self._io(v, nin, "input", 0)
-        dout, hout, pout = self._io(out, nout, "out", 1)
+        synchronously.  The library checks that the operator is open."""
+        if self._h is None:
+            raise ArgumentError("operator is closed")
+        torch = _torch()
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        dv, hv, pv = self._io(v, nin, "input", 0, torch, st)
+        dout, hout, pout = self._io(out, nout, "out", 1, torch, st)
         if hv is not None:
             dv.copy_(hv, non_blocking=pv)
-        _lib.check(fn(self._handle(), dv.data_ptr(), dout.data_ptr(), self._stream()), self._h)
+        rc = fn(self._h, dv.data_ptr(), dout.data_ptr(), st)
+        if rc:
+            _lib.check(rc, self._h)
         if hout is not None:
             hout.copy_(dout, non_blocking=pout)
         setattr(self, counter, getattr(self, counter) + 1)
