@@ -1,6 +1,7 @@
 """The C-ABI library loads and exports every symbol include/hoexplicit.h
 declares; argument validation that happens before any CUDA call."""
 import ctypes
+import os
 import re
 from pathlib import Path
 
@@ -129,3 +130,20 @@ def test_error_mapping():
         _lib.check(_lib.HOE_ERR_UNSUPPORTED)   # engine unavailable for this operator
     with pytest.raises(_lib.HoeError):
         _lib.check(_lib.HOE_ERR_TIMEOUT)
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without the built library the package raises ImportError on first use;
+    there is no CPU or PyTorch fallback of any product."""
+    import subprocess
+    import sys
+    code = ("import sys; sys.path[:0] = ['.', 'highordermri.jl_gb300']\n"
+            "from hoexplicit import _lib\n"
+            "try:\n"
+            "    _lib.load()\n"
+            "except ImportError as e:\n"
+            "    print('ImportError', 'not found' in str(e))\n")
+    env = dict(os.environ, HOE_LIBRARY=str(tmp_path / "absent" / "libhoexplicit.so"))
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                         cwd=str(Path(__file__).resolve().parent.parent), timeout=120)
+    assert out.stdout.strip() == "ImportError True", (out.stdout, out.stderr)
