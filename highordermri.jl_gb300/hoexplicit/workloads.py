@@ -358,7 +358,7 @@ def small(seed: int = 7, shape=(9, 7, 1), nSam=300, nCha=3, nTerm=16, conc=False
     return Workload(f"small-{nX}x{nY}x{nZ}-{nSam}s-{nCha}c-{nTerm}t", grid, kspha, t,
                     fm.reshape(sh, order="F"), csm.reshape(sh + (nCha,), order="F"),
                     mask.reshape(sh, order="F"), x, concomitant=conc_arr, dwell=dwell,
-                    kspha_dt=np.gradient(kspha, dwell, axis=1))
+                    kspha_dt=np.gradient(kspha, dwell, axis=1) if nSam > 1 else np.zeros_like(kspha))
 
 
 def prepared_model(w: Workload, derivative=False):

@@ -182,6 +182,14 @@ SMALL = [
     dict(shape=(6, 5, 4), nSam=300, nCha=3, nTerm=16),
     dict(shape=(6, 5, 4), nSam=300, nCha=3, nTerm=16, conc=True),
     dict(shape=(16, 16, 1), nSam=640, nCha=8, nTerm=16, masked=False),
+    # degenerate sizes: one voxel and one sample, two samples, one sample of
+    # a 3-D grid with concomitant terms, the tensor cores' largest coil count
+    # (64) on one voxel row, fewer samples than one 64-column stage
+    dict(shape=(1, 1, 1), nSam=1, nCha=1, nTerm=9, masked=False),
+    dict(shape=(3, 1, 1), nSam=2, nCha=2, nTerm=16, masked=False),
+    dict(shape=(2, 2, 2), nSam=1, nCha=8, nTerm=16, conc=True, masked=False),
+    dict(shape=(1, 7, 1), nSam=65, nCha=64, nTerm=16),
+    dict(shape=(5, 3, 1), nSam=63, nCha=17, nTerm=9),
 ]
 
 
