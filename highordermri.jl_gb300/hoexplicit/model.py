@@ -119,11 +119,40 @@ def _term(t: int, x, y, z):
         return x ** 2 * z - y ** 2 * z
     if t == 16:
         return x ** 3 - 3 * x * y ** 2
-    raise ArgumentError(f"basis term {t} is not used by the explicit operator (terms 1-16)")
+    if 17 <= t <= 36:
+        return _HIGHER[t](x, y, z, r2)
+    raise ArgumentError("Basis function undefined.")
+
+
+# Fourth- (terms 17-25) and fifth-order (26-36) solid harmonics of
+# basisfunction.jl:79-118 (the explicit operator itself uses terms 1-16).
+_HIGHER = {
+    17: lambda x, y, z, r2: x * y * (x ** 2 - y ** 2),
+    18: lambda x, y, z, r2: y * z * (3 * x ** 2 - y ** 2),
+    19: lambda x, y, z, r2: x * y * (7 * z ** 2 - r2),
+    20: lambda x, y, z, r2: y * (7 * z ** 3 - 3 * z * r2),
+    21: lambda x, y, z, r2: 35 * z ** 4 - 30 * z ** 2 * r2 + 3 * r2 ** 2,
+    22: lambda x, y, z, r2: x * (7 * z ** 3 - 3 * z * r2),
+    23: lambda x, y, z, r2: (x ** 2 - y ** 2) * (7 * z ** 2 - r2),
+    24: lambda x, y, z, r2: x * (x ** 2 - 3 * y ** 2) * z,
+    25: lambda x, y, z, r2: x ** 2 * (x ** 2 - 3 * y ** 2) - y ** 2 * (3 * x ** 2 - y ** 2),
+    26: lambda x, y, z, r2: y * (5 * x ** 4 - 10 * x ** 2 * y ** 2 + y ** 4),
+    27: lambda x, y, z, r2: x * y * z * (x ** 2 - y ** 2),
+    28: lambda x, y, z, r2: y * (r2 - 9 * z ** 2) * (y ** 2 - 3 * x ** 2),
+    29: lambda x, y, z, r2: x * y * z * (3 * z ** 2 - r2),
+    30: lambda x, y, z, r2: y * (r2 ** 2 - 14 * r2 * z ** 2 + 21 * z ** 4),
+    31: lambda x, y, z, r2: 63 * z ** 5 - 70 * z ** 3 * r2 + 15 * z * r2 ** 2,
+    32: lambda x, y, z, r2: x * (r2 ** 2 - 14 * r2 * z ** 2 + 21 * z ** 4),
+    33: lambda x, y, z, r2: z * (3 * z ** 2 - r2) * (x ** 2 - y ** 2),
+    34: lambda x, y, z, r2: x * (r2 - 9 * z ** 2) * (3 * y ** 2 - x ** 2),
+    35: lambda x, y, z, r2: z * (x ** 4 - 6 * x ** 2 * y ** 2 + y ** 4),
+    36: lambda x, y, z, r2: x ** 5 - 10 * x ** 3 * y ** 2 + 5 * x * y ** 4,
+}
 
 
 def basisfunc_spha(x, y, z, terms):
-    """Unnormalised real solid harmonics (basisfunction.jl:27-126), terms 1-16.
+    """Unnormalised real solid harmonics (basisfunction.jl:27-126), terms 1-36
+    (orders 0-5; the explicit operator uses 1-9 or 1-16).
 
     Returns ``(len(x), len(terms))``, columns in the requested order.
     """

@@ -171,3 +171,28 @@ def test_kernel_execution_keywords_get_the_reference_validation():
             check_kernel_options(**kw)
     with pytest.raises(ArgumentError, match="kspha_dt requires backend=:legacy"):
         check_kernel_options(kspha_dt=np.zeros((9, 3)), backend=":blocked")
+
+
+def test_basis_terms_17_to_36():
+    """Fourth- and fifth-order terms of basisfunction.jl: the reference's
+    known answer for term 17 (test_Concomitant.jl:92), and for every term the
+    defining properties of a real solid harmonic: homogeneous of degree 4
+    (terms 17-25) or 5 (26-36) with zero Laplacian, and each order's terms
+    linearly independent (they span the 9- and 11-dimensional spaces)."""
+    np.testing.assert_array_equal(basisfunc_spha([1.0, 2.0], [3.0, 4.0], [5.0, 6.0], 17).ravel(), [-24.0, -96.0])
+    sp = pytest.importorskip("sympy")
+    from hoexplicit.model import _term
+    x, y, z = sp.symbols("x y z")
+    for order, terms in ((4, range(17, 26)), (5, range(26, 37))):
+        polys = []
+        for t in terms:
+            e = sp.expand(_term(t, x, y, z))
+            P = sp.Poly(e, x, y, z)
+            assert P.is_homogeneous and P.total_degree() == order, t
+            assert sp.expand(sp.diff(e, x, 2) + sp.diff(e, y, 2) + sp.diff(e, z, 2)) == 0, t
+            polys.append(P)
+        monoms = sorted({m for P in polys for m in P.monoms()})
+        A = sp.Matrix([[P.coeff_monomial(x ** m[0] * y ** m[1] * z ** m[2]) for m in monoms] for P in polys])
+        assert A.rank() == 2 * order + 1
+    with pytest.raises(ArgumentError):
+        basisfunc_spha([0.0], [0.0], [0.0], 37)
